@@ -1,0 +1,158 @@
+/*
+ * qgcore.h - C ABI of the GB300-native multilayer quasi-geostrophic (QG) time step.
+ *
+ * The library (libqgcore.so) replaces somax's QG hot path below the model classes'
+ * public API.  Each entry point names the reference symbol it stands in for:
+ *
+ *   qg_plan_create   BaroclinicQG.create / BarotropicQG.create + ModalTransform.from_physics
+ *                    (somax/_src/models/qg/baroclinic.py:230-332,
+ *                     somax/_src/models/qg/barotropic.py:186-248,
+ *                     somax/_src/core/transforms.py:172-200)
+ *   qg_invert        BaroclinicQG._invert_pv (baroclinic.py:135-159),
+ *                    BarotropicQG._invert_pv (barotropic.py:113-121)
+ *   qg_rhs           BaroclinicQG.vector_field (baroclinic.py:161-190),
+ *                    BarotropicQG.vector_field (barotropic.py:123-152); with QG_RHS_APPLY_BC
+ *                    it is SomaxModel.build_terms._rhs (somax/_src/core/model.py:47-49)
+ *   qg_step          SomaxModel.integrate with ConstantStepSize (core/model.py:53-88)
+ *   qg_diagnose      BaroclinicQG.diagnose KE / enstrophy (baroclinic.py:197-228)
+ *   qg_status        non-finite check of the runner (somax/_src/cli/_run.py:671-686)
+ *
+ * Conventions: every field is float32, layout (n_layers, Ny, Nx) row-major per member with
+ * Ny = ny + 2, Nx = nx + 2 (one ghost ring); members of an ensemble are concatenated in
+ * the order given to qg_plan_create (qg_plan_member_offset gives each member's offset in
+ * floats).  All device pointers are owned by the caller; the plan owns its constants and
+ * workspace, and no entry point below allocates device memory after qg_plan_create.
+ * Calls are asynchronous on the given stream; a plan must not be used from two streams
+ * at the same time.  Every entry point returns QG_OK or a QG_ERR_* code; nothing throws
+ * across the ABI.
+ */
+#ifndef QGCORE_H
+#define QGCORE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QG_MAX_LAYERS 8
+
+/* status codes */
+#define QG_OK 0
+#define QG_ERR_NULL 1         /* a required pointer is NULL */
+#define QG_ERR_SHAPE 2        /* bad grid size / layer count / member count */
+#define QG_ERR_CUDA 3         /* a CUDA runtime call failed */
+#define QG_ERR_NONFINITE 4    /* a kernel saw a non-finite value (qg_status) */
+#define QG_ERR_TIMEOUT 5      /* a bounded device-side wait gave up */
+#define QG_ERR_ARG 6          /* bad enum / option value */
+#define QG_ERR_UNSUPPORTED 7  /* option not available on this device */
+
+/* dst_precision: arithmetic of the DST-I GEMMs of the PV inversion */
+#define QG_DST_FP32 0    /* plain FP32 on the CUDA cores (the baseline path) */
+#define QG_DST_TF32 1    /* tcgen05 kind::tf32, FP32 accumulate */
+#define QG_DST_BF16X3 2  /* tcgen05 kind::f16, split bf16 hi/lo, 3 products, FP32 accumulate */
+
+/* eigs_mode: where the Helmholtz eigenvalues come from (transforms.py:192-194) */
+#define QG_EIGS_CONSISTENT 0 /* eig(A), paired with the modes */
+#define QG_EIGS_REFERENCE 1  /* eigh((A + A^T) / 2), as jnp.linalg.eigh does */
+
+/* time schemes for qg_step */
+#define QG_SCHEME_EULER 0
+#define QG_SCHEME_HEUN 1   /* diffrax.Heun */
+#define QG_SCHEME_SSPRK3 2 /* Shu-Osher SSP-RK3 */
+#define QG_SCHEME_TSIT5 3  /* diffrax.Tsit5 (the reference default) */
+
+/* wind profile (baroclinic.py:313-318) */
+#define QG_WIND_DOUBLEGYRE 0 /* -sin(2 pi y / Ly) */
+#define QG_WIND_SINGLE 1     /* sin(pi y / Ly) */
+
+/* flags for qg_rhs */
+#define QG_RHS_APPLY_BC 1 /* zero the ghost ring of q first (core/model.py:47-49) */
+
+/* params layout: per member, QG_NPARAMS floats in device memory */
+#define QG_NPARAMS 4
+#define QG_P_NU 0    /* lateral_viscosity (m^2/s) */
+#define QG_P_KAPPA 1 /* bottom_drag (1/s) */
+#define QG_P_TAU0 2  /* wind_amplitude (wind-stress curl amplitude, 1/s^2) */
+#define QG_P_NU4 3   /* biharmonic viscosity (m^4/s), extension; 0 = off */
+
+typedef struct qg_member_desc {
+    int nx, ny;         /* interior cells */
+    int n_layers;       /* 1..QG_MAX_LAYERS */
+    int barotropic;     /* 1: BarotropicQG semantics (Poisson, psi ring kept, wind not / H) */
+    double Lx, Ly;      /* domain size (m) */
+    double f0, beta;    /* Coriolis parameter (1/s), its meridional gradient (1/(m s)) */
+    double H[QG_MAX_LAYERS];       /* layer thicknesses, top to bottom (m) */
+    double g_prime[QG_MAX_LAYERS]; /* reduced gravities at each interface (m/s^2) */
+    int wind_profile;   /* QG_WIND_* */
+    int eigs_mode;      /* QG_EIGS_* */
+    /* optional override of the modal matrices (row-major nl x nl) and the Helmholtz
+       lambdas f0^2 * eig (nl); used when has_modes != 0 */
+    int has_modes;
+    double Cl2m[QG_MAX_LAYERS * QG_MAX_LAYERS];
+    double Cm2l[QG_MAX_LAYERS * QG_MAX_LAYERS];
+    double lambdas[QG_MAX_LAYERS];
+} qg_member_desc;
+
+typedef struct qg_options {
+    int dst_precision;  /* QG_DST_* */
+    int refine_sweeps;  /* FP32 residual-refinement sweeps of the Helmholtz solve (0 or 1) */
+    int use_graphs;     /* 1: qg_step replays a captured CUDA graph per step */
+    int reserved[5];
+} qg_options;
+
+typedef struct qg_plan qg_plan;
+
+/* Build a plan for an ensemble of members (n_members >= 1). opts may be NULL (defaults:
+   FP32, no refinement, graphs on).  Allocates the plan's device constants and workspace on
+   the current device. */
+int qg_plan_create(const qg_member_desc* members, int n_members, const qg_options* opts,
+                   qg_plan** out);
+void qg_plan_destroy(qg_plan* plan);
+
+/* Number of floats in one packed field (all members), and member i's offset into it. */
+int64_t qg_plan_state_size(const qg_plan* plan);
+int64_t qg_plan_member_offset(const qg_plan* plan, int member);
+/* Helmholtz lambdas f0^2 * eig (nl values) and the modal matrices the plan uses. */
+int qg_plan_member_modes(const qg_plan* plan, int member, double* lambdas, double* Cl2m,
+                         double* Cm2l);
+
+/* psi = _invert_pv(q) for every member. q and psi: packed fields (device). */
+int qg_invert(qg_plan* plan, const float* q, float* psi, void* stream);
+
+/* dq = vector_field(q) for every member. params: n_members * QG_NPARAMS floats (device). */
+int qg_rhs(qg_plan* plan, const float* q, float* dq, const float* params, int flags,
+           void* stream);
+
+/* Advance q in place by n_steps steps of size dt with the given scheme.  Like
+   SomaxModel.integrate, the ghost ring of q is zeroed first and the BC is applied to every
+   stage input; the returned state's ring is the stepped (not re-zeroed) ring. */
+int qg_step(qg_plan* plan, float* q, const float* params, double dt, int n_steps, int scheme,
+            void* stream);
+
+/* Kinetic energy and enstrophy per layer: ke, ens each sum(n_layers) floats (device). */
+int qg_diagnose(qg_plan* plan, const float* q, float* ke, float* ens, void* stream);
+
+/* Device-side status: synchronises the stream, returns QG_OK or QG_ERR_NONFINITE /
+   QG_ERR_TIMEOUT, writes the raw flag word to *flags (may be NULL) and clears it. */
+int qg_status(qg_plan* plan, int* flags, void* stream);
+
+const char* qg_strerror(int code);
+
+/* Per-kernel-class timing with CUDA events recorded on the launch stream around every
+   launch while profiling is on (graphs are bypassed then).  Used by the benchmark to turn
+   algorithmic bytes / flops into achieved bandwidth / throughput per kernel. */
+#define QG_K_PREP 0    /* layer -> mode prologue (BC, Cl2m, operand format) */
+#define QG_K_GEMM 1    /* DST-I GEMMs of the inversion */
+#define QG_K_STENCIL 2 /* fused RHS stencil (+ RK stage update, + next-stage prologue) */
+#define QG_K_OTHER 3   /* mode -> layer epilogue, residual, diagnostics, packing */
+#define QG_K_COUNT 4
+int qg_set_profiling(qg_plan* plan, int enable); /* resets the counters */
+int qg_kernel_stats(qg_plan* plan, int kclass, double* total_ms, int64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QGCORE_H */

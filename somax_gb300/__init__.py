@@ -1,0 +1,10 @@
+"""GB300-native (sm_103a) multilayer quasi-geostrophic time step, a drop-in below somax's
+QG model API.  The compute path is libqgcore.so (hand-written CUDA, C ABI in
+include/qgcore.h); this package is the Python host side that mirrors somax's classes."""
+
+from .qg import (  # noqa: F401
+    SSPRK3, BaroclinicQG, BaroclinicQGDiagnostics, BaroclinicQGParams, BaroclinicQGState,
+    BarotropicQG, BarotropicQGDiagnostics, BarotropicQGParams, BarotropicQGState, Euler, Heun,
+    MemberSpec, Plan, QGDiagnostics, QGParams, SaveAt, Solution, SomaxModel, State, Tsit5,
+)
+from .transforms import ModalTransform, StratificationProfile  # noqa: F401

@@ -1,0 +1,124 @@
+// Internal declarations shared by the libqgcore translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/qgcore.h"
+
+namespace qg {
+
+constexpr int kMaxLayers = QG_MAX_LAYERS;
+
+// Per-member constants, resident in device memory (an array indexed by member id) so that
+// one launch can serve every member of an ensemble.
+struct MemberDev {
+    int nl, Ny, Nx;
+    int Px, Py;      // padded pitches (floats): x-row planes (nl, Ny, Px), y-row planes (nl, Nx, Py)
+    int barotropic;  // BarotropicQG semantics
+    float dx, dy;
+    float inv_dx2, inv_dy2;
+    float inv_12dxdy;  // 1 / (12 dx dy): Arakawa normalisation
+    float beta_12dx;   // beta / (12 dx): the beta-term of J(psi, beta y) for a linear beta y
+    float invH0;       // 1 / H[0] (1 for barotropic)
+    float Cl2m[kMaxLayers * kMaxLayers];
+    float Cm2l[kMaxLayers * kMaxLayers];
+    float lam[kMaxLayers];  // f0^2 * eig
+    int64_t off_state;      // offset (floats) of this member in a caller's packed field
+    int64_t off_x;          // offset (floats) in the internal x-row planes
+    int64_t off_y;          // offset (floats) in the internal y-row planes
+    int64_t off_layer;      // offset of this member's first layer in per-layer outputs
+    const float* by;        // beta * (y_j - Ly/2), Ny
+    const float* F;         // wind pattern, Ny
+    const float* ex;        // DST-I eigenvalues along x (Nx)
+    const float* ey;        // along y (Ny)
+    const float* Sx;        // orthonormal DST-I matrix Nx x Nx, pitch Px
+    const float* Sy;        // Ny x Ny, pitch Py
+    const uint16_t* Sx_bf;  // bf16 hi/lo planes of Sx (pitch Px, hi then lo), or null
+    const uint16_t* Sy_bf;
+};
+
+// Stencil work item: one 2-D tile of one member (all layers).
+struct StencilTile {
+    int member, ty, tx;
+};
+
+// GEMM work item: one output tile of one member for one pass.
+struct GemmTile {
+    int member, mt, nt;
+};
+
+// The four DST-I GEMM passes of the inversion, psi_hat = S_y (S_y q S_x ./ L) S_x.
+// Each is C = A * S with A row-major (rows = (layer, r), K contiguous) and S symmetric.
+enum GemmPass : int {
+    G1_FWD_X = 0,  // A = q_modal rows (l, y), K = x  -> T1t[l][kx][y]   (transposed store)
+    G2_FWD_Y = 1,  // A = T1t rows (l, kx), K = y     -> U[l][kx][ky] / (ex+ey-lam)
+    G3_INV_Y = 2,  // A = U rows (l, kx), K = ky      -> Vt[l][y][kx]   (transposed store)
+    G4_INV_X = 3,  // A = Vt rows (l, y), K = kx      -> psi_hat[l][y][x]
+};
+
+// Operand / output formats of the internal planes.
+enum PlaneFmt : int {
+    FMT_F32 = 0,     // float32 plane
+    FMT_BF16X2 = 1,  // bf16 hi plane followed by bf16 lo plane (same byte size as f32)
+};
+
+struct StencilArgs {
+    const MemberDev* members;
+    const StencilTile* tiles;
+    const float* q;        // stage input (layer space), caller packing or internal packing
+    int q_internal;        // 1: q uses the internal x-row packing (off_x, pitch Px)
+    const float* psi_hat;  // modal psi, x-row planes
+    const float* params;   // n_members * QG_NPARAMS
+    int apply_bc;          // zero the ring of q on read
+    // rhs mode
+    float* dq;             // caller packing; null in step mode
+    // step mode: y_next = a * y0 + b * (y_s + dt * dq)
+    const float* y0;       // caller packing (state); read pointwise
+    float* y_next;         // destination (caller packing if final, internal otherwise)
+    int y_next_internal;
+    int final_stage;
+    float a, b, dt;
+    void* xa;              // next-stage GEMM operand (modal q, x-row planes); may be null
+    int xa_fmt;
+    float* xq;             // FP32 copy of the modal q for the refinement residual; may be null
+    int* flags;            // device status word
+};
+
+// launchers (return cudaError_t of the launch)
+cudaError_t launch_prep(const MemberDev* members, const StencilTile* tiles, int ntiles,
+                        const float* q, float* q_bc_inplace, int apply_bc, void* xa, int xa_fmt,
+                        float* xq, int64_t xplane, cudaStream_t s);
+cudaError_t launch_stencil(const StencilArgs& a, int ntiles, int max_nl, int64_t xplane,
+                           cudaStream_t s);
+size_t stencil_smem_bytes(int max_nl);
+cudaError_t launch_mode_to_layer(const MemberDev* members, const StencilTile* tiles, int ntiles,
+                                 const float* psi_hat, float* psi, cudaStream_t s);
+cudaError_t launch_diag_acc(const MemberDev* members, const StencilTile* tiles, int ntiles,
+                            const float* q, const float* psi_hat, double* acc, cudaStream_t s);
+cudaError_t launch_diag_finish(const double* acc, int64_t n_layers, float* ke, float* ens,
+                               cudaStream_t s);
+void stencil_init();
+cudaError_t launch_residual(const MemberDev* members, const StencilTile* tiles, int ntiles,
+                            const float* qm, const float* psi_hat, void* out, int out_fmt,
+                            int64_t xplane, cudaStream_t s);
+
+struct GemmArgs {
+    const MemberDev* members;
+    int64_t xplane, yplane;  // elements of one x-row / y-row plane (bf16 lo-plane offset)
+    const GemmTile* tiles;
+    int pass;
+    const void* A;   // plane base (internal packing)
+    void* C;         // plane base
+    int a_fmt, c_fmt;
+    int accumulate;  // C += result (refinement of psi_hat)
+};
+cudaError_t launch_gemm_simt(const GemmArgs& g, int ntiles, cudaStream_t s);
+cudaError_t launch_gemm_tc(const GemmArgs& g, int ntiles, int precision, cudaStream_t s);
+
+constexpr int kStencilTX = 32;
+constexpr int kStencilTY = 16;
+constexpr int kSimtBM = 64;
+constexpr int kSimtBN = 64;
+
+}  // namespace qg

@@ -1,0 +1,699 @@
+// Host side of libqgcore: plan construction (FP64 modal matrices, DST-I matrices and
+// eigenvalues, grids of tiles), the C-ABI entry points and their launch sequences, CUDA
+// graph capture of a whole time step, and per-kernel event timing.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "qg_internal.cuh"
+
+namespace qg {
+cudaError_t gemm_tc_init();
+int gemm_tc_tile_n(int precision);
+}  // namespace qg
+
+using namespace qg;
+
+namespace {
+
+// ---------------------------------------------------------------------------------------
+// Small dense linear algebra in double (nl <= 8)
+// ---------------------------------------------------------------------------------------
+
+// Cyclic Jacobi eigen-decomposition of a symmetric n x n matrix (row-major).  On return
+// w holds the eigenvalues (ascending) and V's columns the orthonormal eigenvectors.
+void jacobi_eigh(int n, const double* Ain, double* w, double* V) {
+    double A[kMaxLayers * kMaxLayers];
+    std::memcpy(A, Ain, sizeof(double) * n * n);
+    for (int i = 0; i < n * n; ++i) V[i] = 0.0;
+    for (int i = 0; i < n; ++i) V[i * n + i] = 1.0;
+    for (int sweep = 0; sweep < 100; ++sweep) {
+        double off = 0.0, tot = 0.0;
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) {
+                tot += A[i * n + j] * A[i * n + j];
+                if (i != j) off += A[i * n + j] * A[i * n + j];
+            }
+        if (off <= 1e-30 * tot || off == 0.0) break;
+        for (int p = 0; p < n - 1; ++p)
+            for (int q = p + 1; q < n; ++q) {
+                const double apq = A[p * n + q];
+                if (apq == 0.0) continue;
+                const double theta = (A[q * n + q] - A[p * n + p]) / (2.0 * apq);
+                const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+                const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+                for (int k = 0; k < n; ++k) {  // A <- A J
+                    const double akp = A[k * n + p], akq = A[k * n + q];
+                    A[k * n + p] = c * akp - s * akq;
+                    A[k * n + q] = s * akp + c * akq;
+                }
+                for (int k = 0; k < n; ++k) {  // A <- J^T A
+                    const double apk = A[p * n + k], aqk = A[q * n + k];
+                    A[p * n + k] = c * apk - s * aqk;
+                    A[q * n + k] = s * apk + c * aqk;
+                }
+                for (int k = 0; k < n; ++k) {  // V <- V J
+                    const double vkp = V[k * n + p], vkq = V[k * n + q];
+                    V[k * n + p] = c * vkp - s * vkq;
+                    V[k * n + q] = s * vkp + c * vkq;
+                }
+            }
+    }
+    // sort ascending
+    int idx[kMaxLayers];
+    for (int i = 0; i < n; ++i) idx[i] = i;
+    std::sort(idx, idx + n, [&](int a, int b) { return A[a * n + a] < A[b * n + b]; });
+    double Vs[kMaxLayers * kMaxLayers];
+    for (int c = 0; c < n; ++c) {
+        w[c] = A[idx[c] * n + idx[c]];
+        for (int r = 0; r < n; ++r) Vs[r * n + c] = V[r * n + idx[c]];
+    }
+    std::memcpy(V, Vs, sizeof(double) * n * n);
+}
+
+// Layered QG coupling A = diag(1/H) M with M symmetric tridiagonal (the stretching
+// operator of finitevolx build_coupling_matrix, transforms.py:192).  Its right
+// eigenvectors are R = diag(H^-1/2) V with V the eigenvectors of the symmetric
+// diag(H^-1/2) M diag(H^-1/2); Cl2m = R^-1 = V^T diag(H^1/2).
+void vertical_modes(const qg_member_desc& d, double* Cl2m, double* Cm2l, double* lam) {
+    const int n = d.n_layers;
+    double Msym[kMaxLayers * kMaxLayers] = {0};
+    if (n == 1) {
+        Msym[0] = 1.0 / d.g_prime[0];
+    } else {
+        for (int k = 0; k < n; ++k) {
+            double dk = (k < n - 1) ? 1.0 / d.g_prime[k + 1] : 0.0;
+            dk += (k == 0) ? 1.0 / d.g_prime[0] : 0.0;
+            if (k > 0) dk += 1.0 / d.g_prime[k];
+            Msym[k * n + k] = dk;
+            if (k < n - 1) Msym[k * n + k + 1] = Msym[(k + 1) * n + k] = -1.0 / d.g_prime[k + 1];
+        }
+    }
+    double S[kMaxLayers * kMaxLayers], w[kMaxLayers], V[kMaxLayers * kMaxLayers];
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) S[i * n + j] = Msym[i * n + j] / std::sqrt(d.H[i] * d.H[j]);
+    jacobi_eigh(n, S, w, V);
+    for (int i = 0; i < n; ++i)
+        for (int m = 0; m < n; ++m) {
+            Cm2l[i * n + m] = V[i * n + m] / std::sqrt(d.H[i]);
+            Cl2m[m * n + i] = V[i * n + m] * std::sqrt(d.H[i]);
+        }
+    if (d.eigs_mode == QG_EIGS_REFERENCE) {
+        // jnp.linalg.eigh symmetrises its input: eigenvalues of (A + A^T)/2
+        double As[kMaxLayers * kMaxLayers], Vr[kMaxLayers * kMaxLayers];
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j)
+                As[i * n + j] = 0.5 * (Msym[i * n + j] / d.H[i] + Msym[j * n + i] / d.H[j]);
+        jacobi_eigh(n, As, w, Vr);
+    }
+    for (int m = 0; m < n; ++m) lam[m] = d.f0 * d.f0 * w[m];
+}
+
+int round_up(int v, int m) { return (v + m - 1) / m * m; }
+
+// Orthonormal DST-I matrix (n x n, pitch ld): sqrt(2/(n+1)) sin(pi (i+1)(j+1)/(n+1)),
+// the argument reduced modulo 2(n+1) for accuracy.
+void dst_matrix(int n, int ld, std::vector<float>& out) {
+    out.assign((size_t)n * ld, 0.f);
+    const double s = std::sqrt(2.0 / (n + 1));
+    const long long per = 2LL * (n + 1);
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+            const long long k = ((long long)(i + 1) * (j + 1)) % per;
+            out[(size_t)i * ld + j] = (float)(s * std::sin(M_PI * (double)k / (n + 1)));
+        }
+}
+
+// Eigenvalues of the 3-point second difference with Dirichlet zeros at -1 and n:
+// (2 cos(pi k/(n+1)) - 2)/d^2 = -4 sin^2(pi k / (2(n+1))) / d^2.
+void dst_eigs(int n, double d, std::vector<float>& out) {
+    out.resize(n);
+    for (int k = 1; k <= n; ++k) {
+        const double sn = std::sin(M_PI * k / (2.0 * (n + 1)));
+        out[k - 1] = (float)(-4.0 * sn * sn / (d * d));
+    }
+}
+
+const char* kErrStr[] = {"ok", "null pointer", "bad shape", "CUDA error", "non-finite value",
+                         "device wait timed out", "bad argument", "unsupported"};
+
+}  // namespace
+
+struct StepGraph {
+    cudaGraphExec_t exec = nullptr;
+    const float* q = nullptr;
+    double dt = 0.0;
+    int scheme = -1;
+};
+
+struct qg_plan {
+    int n_members = 0;
+    qg_options opts{};
+    std::vector<qg_member_desc> desc;
+    std::vector<MemberDev> mh;  // host copy of member constants (device pointers filled)
+    MemberDev* md = nullptr;    // device
+    int max_nl = 1;
+    int64_t state_size = 0, xplane = 0, yplane = 0, total_layers = 0;
+    std::vector<int64_t> member_off;
+    // tiles
+    StencilTile* st_tiles = nullptr;
+    int n_st = 0;
+    GemmTile* gx_tiles = nullptr;  // passes with A in x-row planes (G1, G4)
+    GemmTile* gy_tiles = nullptr;  // passes with A in y-row planes (G2, G3)
+    int n_gx = 0, n_gy = 0;
+    // device memory
+    std::vector<void*> allocs;
+    float *XA = nullptr, *XB = nullptr, *XC = nullptr, *XQ = nullptr, *YA = nullptr, *YB = nullptr;
+    float *S1 = nullptr, *S2 = nullptr;
+    float* params = nullptr;  // plan-owned copy of the params (graph-stable)
+    int* flags = nullptr;
+    double* diag_acc = nullptr;
+    int op_fmt = FMT_F32;
+    // graphs
+    cudaStream_t cap = nullptr;
+    StepGraph graph;
+    // profiling
+    bool profiling = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev[QG_K_COUNT];
+    size_t ev_used[QG_K_COUNT] = {0, 0, 0, 0};
+    int device = 0;
+};
+
+namespace {
+
+template <typename T>
+cudaError_t dalloc(qg_plan* p, T** ptr, size_t bytes) {
+    void* v = nullptr;
+    cudaError_t e = cudaMalloc(&v, std::max<size_t>(bytes, 16));
+    if (e != cudaSuccess) return e;
+    cudaMemsetAsync(v, 0, std::max<size_t>(bytes, 16));
+    p->allocs.push_back(v);
+    *ptr = static_cast<T*>(v);
+    return cudaSuccess;
+}
+
+template <typename T>
+cudaError_t upload(qg_plan* p, T** dst, const std::vector<T>& src) {
+    cudaError_t e = dalloc(p, dst, src.size() * sizeof(T));
+    if (e != cudaSuccess) return e;
+    return cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+// Run `launch` bracketed by profiling events of class k when profiling is on.
+template <typename F>
+cudaError_t timed(qg_plan* p, int k, cudaStream_t s, F&& launch) {
+    if (!p->profiling) return launch();
+    auto& v = p->ev[k];
+    if (p->ev_used[k] == v.size()) {
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        v.emplace_back(a, b);
+    }
+    auto& pr = v[p->ev_used[k]++];
+    cudaEventRecord(pr.first, s);
+    cudaError_t e = launch();
+    cudaEventRecord(pr.second, s);
+    return e;
+}
+
+GemmArgs gemm_args(qg_plan* p, int pass, const void* A, void* C, int a_fmt, int c_fmt, int acc) {
+    GemmArgs g{};
+    g.members = p->md;
+    g.xplane = p->xplane;
+    g.yplane = p->yplane;
+    g.tiles = (pass == G1_FWD_X || pass == G4_INV_X) ? p->gx_tiles : p->gy_tiles;
+    g.pass = pass;
+    g.A = A;
+    g.C = C;
+    g.a_fmt = a_fmt;
+    g.c_fmt = c_fmt;
+    g.accumulate = acc;
+    return g;
+}
+
+cudaError_t run_gemm(qg_plan* p, const GemmArgs& g, cudaStream_t s) {
+    const int nt = (g.pass == G1_FWD_X || g.pass == G4_INV_X) ? p->n_gx : p->n_gy;
+    return timed(p, QG_K_GEMM, s, [&] {
+        if (p->opts.dst_precision == QG_DST_FP32) return launch_gemm_simt(g, nt, s);
+        return launch_gemm_tc(g, nt, p->opts.dst_precision, s);
+    });
+}
+
+// psi_hat (XC) from the modal operand already in XA (and XQ for refinement).
+cudaError_t run_dst_solve(qg_plan* p, cudaStream_t s) {
+    const int f = p->op_fmt;
+    cudaError_t e;
+    // the last pass writes FP32 psi_hat; intermediate planes use the operand format
+    if ((e = run_gemm(p, gemm_args(p, G1_FWD_X, p->XA, p->YA, f, f, 0), s))) return e;
+    if ((e = run_gemm(p, gemm_args(p, G2_FWD_Y, p->YA, p->YB, f, f, 0), s))) return e;
+    if ((e = run_gemm(p, gemm_args(p, G3_INV_Y, p->YB, p->XB, f, f, 0), s))) return e;
+    if ((e = run_gemm(p, gemm_args(p, G4_INV_X, p->XB, p->XC, f, FMT_F32, 0), s))) return e;
+    for (int r = 0; r < p->opts.refine_sweeps; ++r) {
+        e = timed(p, QG_K_OTHER, s, [&] {
+            return launch_residual(p->md, p->st_tiles, p->n_st, p->XQ, p->XC, p->XA, f, p->xplane, s);
+        });
+        if (e) return e;
+        if ((e = run_gemm(p, gemm_args(p, G1_FWD_X, p->XA, p->YA, f, f, 0), s))) return e;
+        if ((e = run_gemm(p, gemm_args(p, G2_FWD_Y, p->YA, p->YB, f, f, 0), s))) return e;
+        if ((e = run_gemm(p, gemm_args(p, G3_INV_Y, p->YB, p->XB, f, f, 0), s))) return e;
+        if ((e = run_gemm(p, gemm_args(p, G4_INV_X, p->XB, p->XC, f, FMT_F32, 1), s))) return e;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t run_prep(qg_plan* p, const float* q, float* q_inplace, int apply_bc, cudaStream_t s) {
+    return timed(p, QG_K_PREP, s, [&] {
+        return launch_prep(p->md, p->st_tiles, p->n_st, q, q_inplace, apply_bc, p->XA, p->op_fmt,
+                           p->XQ, p->xplane, s);
+    });
+}
+
+struct Stage {
+    float a, b;
+};
+
+int scheme_stages(int scheme, Stage* st) {
+    switch (scheme) {
+        case QG_SCHEME_HEUN:
+            st[0] = {0.f, 1.f};
+            st[1] = {0.5f, 0.5f};
+            return 2;
+        case QG_SCHEME_SSPRK3:
+            st[0] = {0.f, 1.f};
+            st[1] = {0.75f, 0.25f};
+            st[2] = {1.f / 3.f, 2.f / 3.f};
+            return 3;
+        default:
+            return 0;
+    }
+}
+
+// One time step on q (caller packing, ring already BC'd, XA holding Cl2m q).
+cudaError_t run_one_step(qg_plan* p, float* q, const float* params, float dt, int scheme,
+                         cudaStream_t s) {
+    Stage st[4];
+    const int ns = scheme_stages(scheme, st);
+    float* stage_buf[3] = {q, p->S1, p->S2};
+    cudaError_t e;
+    for (int k = 0; k < ns; ++k) {
+        if ((e = run_dst_solve(p, s))) return e;
+        StencilArgs a{};
+        a.members = p->md;
+        a.tiles = p->st_tiles;
+        a.q = stage_buf[k];
+        a.q_internal = k > 0;
+        a.psi_hat = p->XC;
+        a.params = params;
+        a.apply_bc = 1;
+        a.dq = nullptr;
+        a.y0 = q;
+        const bool fin = (k == ns - 1);
+        a.final_stage = fin;
+        a.y_next = fin ? q : stage_buf[k + 1];
+        a.y_next_internal = !fin;
+        a.a = st[k].a;
+        a.b = st[k].b;
+        a.dt = dt;
+        a.xa = p->XA;
+        a.xa_fmt = p->op_fmt;
+        a.xq = p->XQ;
+        a.flags = p->flags;
+        e = timed(p, QG_K_STENCIL, s, [&] { return launch_stencil(a, p->n_st, p->max_nl, p->xplane, s); });
+        if (e) return e;
+    }
+    return cudaSuccess;
+}
+
+int cuda_err(cudaError_t e) { return e == cudaSuccess ? QG_OK : QG_ERR_CUDA; }
+
+}  // namespace
+
+// =======================================================================================
+// C ABI
+// =======================================================================================
+extern "C" {
+
+const char* qg_strerror(int code) {
+    if (code < 0 || code >= (int)(sizeof(kErrStr) / sizeof(kErrStr[0]))) return "unknown error";
+    return kErrStr[code];
+}
+
+int qg_plan_create(const qg_member_desc* members, int n_members, const qg_options* opts,
+                   qg_plan** out) {
+    if (!members || !out) return QG_ERR_NULL;
+    *out = nullptr;
+    if (n_members < 1) return QG_ERR_SHAPE;
+    qg_options o{};
+    o.dst_precision = QG_DST_FP32;
+    o.refine_sweeps = 0;
+    o.use_graphs = 1;
+    if (opts) o = *opts;
+    if (o.dst_precision < QG_DST_FP32 || o.dst_precision > QG_DST_BF16X3) return QG_ERR_ARG;
+    if (o.refine_sweeps < 0 || o.refine_sweeps > 1) return QG_ERR_ARG;
+    for (int i = 0; i < n_members; ++i) {
+        const qg_member_desc& d = members[i];
+        if (d.nx < 1 || d.ny < 1 || d.n_layers < 1 || d.n_layers > QG_MAX_LAYERS) return QG_ERR_SHAPE;
+        if ((int64_t)(d.nx + 2) * (d.ny + 2) > (1LL << 28)) return QG_ERR_SHAPE;
+        if (d.barotropic && d.n_layers != 1) return QG_ERR_SHAPE;
+        if (!(d.Lx > 0) || !(d.Ly > 0)) return QG_ERR_ARG;
+        if (d.wind_profile != QG_WIND_DOUBLEGYRE && d.wind_profile != QG_WIND_SINGLE) return QG_ERR_ARG;
+        if (d.eigs_mode != QG_EIGS_CONSISTENT && d.eigs_mode != QG_EIGS_REFERENCE) return QG_ERR_ARG;
+        if (!d.has_modes && !d.barotropic)
+            for (int l = 0; l < d.n_layers; ++l)
+                if (!(d.H[l] > 0) || !(d.g_prime[l] > 0)) return QG_ERR_ARG;
+    }
+    qg_plan* p = new (std::nothrow) qg_plan();
+    if (!p) return QG_ERR_CUDA;
+    p->n_members = n_members;
+    p->opts = o;
+    p->desc.assign(members, members + n_members);
+    cudaGetDevice(&p->device);
+    stencil_init();
+    if (o.dst_precision != QG_DST_FP32) {
+        if (gemm_tc_init() != cudaSuccess) {
+            delete p;
+            return QG_ERR_UNSUPPORTED;
+        }
+        p->op_fmt = (o.dst_precision == QG_DST_BF16X3) ? FMT_BF16X2 : FMT_F32;
+    }
+    cudaError_t e = cudaSuccess;
+    // geometry and offsets
+    p->mh.resize(n_members);
+    int64_t off_state = 0, off_x = 0, off_y = 0, off_layer = 0;
+    std::vector<StencilTile> st;
+    std::vector<GemmTile> gx, gy;
+    const bool tc = o.dst_precision != QG_DST_FP32;
+    const int BMg = tc ? 128 : kSimtBM;
+    const int BNg = tc ? gemm_tc_tile_n(o.dst_precision) : kSimtBN;
+    for (int i = 0; i < n_members; ++i) {
+        const qg_member_desc& d = members[i];
+        MemberDev& M = p->mh[i];
+        std::memset(&M, 0, sizeof(M));
+        M.nl = d.n_layers;
+        M.Ny = d.ny + 2;
+        M.Nx = d.nx + 2;
+        M.Px = round_up(M.Nx, 32);
+        M.Py = round_up(M.Ny, 32);
+        M.barotropic = d.barotropic;
+        const double dx = d.Lx / d.nx, dy = d.Ly / d.ny;
+        M.dx = (float)dx;
+        M.dy = (float)dy;
+        M.inv_dx2 = (float)(1.0 / (dx * dx));
+        M.inv_dy2 = (float)(1.0 / (dy * dy));
+        M.inv_12dxdy = (float)(1.0 / (12.0 * dx * dy));
+        M.beta_12dx = (float)(d.beta / (12.0 * dx));
+        M.invH0 = d.barotropic ? 1.f : (float)(1.0 / d.H[0]);
+        double Cl2m[64], Cm2l[64], lam[8];
+        const int n = d.n_layers;
+        if (d.barotropic) {
+            Cl2m[0] = Cm2l[0] = 1.0;
+            lam[0] = 0.0;
+        } else if (d.has_modes) {
+            for (int k = 0; k < n * n; ++k) {
+                Cl2m[k] = d.Cl2m[k];
+                Cm2l[k] = d.Cm2l[k];
+            }
+            for (int k = 0; k < n; ++k) lam[k] = d.lambdas[k];
+        } else {
+            vertical_modes(d, Cl2m, Cm2l, lam);
+        }
+        for (int r = 0; r < n; ++r) {
+            for (int c = 0; c < n; ++c) {
+                M.Cl2m[r * kMaxLayers + c] = (float)Cl2m[r * n + c];
+                M.Cm2l[r * kMaxLayers + c] = (float)Cm2l[r * n + c];
+            }
+            M.lam[r] = (float)lam[r];
+        }
+        p->desc[i].has_modes = 1;  // remember what the plan uses
+        for (int k = 0; k < n * n; ++k) {
+            p->desc[i].Cl2m[k] = Cl2m[k];
+            p->desc[i].Cm2l[k] = Cm2l[k];
+        }
+        for (int k = 0; k < n; ++k) p->desc[i].lambdas[k] = lam[k];
+        M.off_state = off_state;
+        M.off_x = off_x;
+        M.off_y = off_y;
+        M.off_layer = off_layer;
+        p->member_off.push_back(off_state);
+        off_state += (int64_t)n * M.Ny * M.Nx;
+        off_x += (int64_t)n * M.Ny * M.Px;
+        off_y += (int64_t)n * M.Nx * M.Py;
+        off_layer += n;
+        p->max_nl = std::max(p->max_nl, n);
+        // constant fields
+        std::vector<float> by(M.Ny), F(M.Ny), ex, ey, Sx, Sy;
+        for (int j = 0; j < M.Ny; ++j) {
+            const double y = j * dy;
+            by[j] = (float)(d.beta * (y - d.Ly / 2.0));
+            F[j] = (float)(d.wind_profile == QG_WIND_SINGLE ? std::sin(M_PI * y / d.Ly)
+                                                             : -std::sin(2.0 * M_PI * y / d.Ly));
+        }
+        dst_eigs(M.Nx, dx, ex);
+        dst_eigs(M.Ny, dy, ey);
+        dst_matrix(M.Nx, M.Px, Sx);
+        dst_matrix(M.Ny, M.Py, Sy);
+        float *dby, *dF, *dex, *dey, *dSx, *dSy;
+        if ((e = upload(p, &dby, by)) || (e = upload(p, &dF, F)) || (e = upload(p, &dex, ex)) ||
+            (e = upload(p, &dey, ey)) || (e = upload(p, &dSx, Sx)) || (e = upload(p, &dSy, Sy)))
+            break;
+        M.by = dby;
+        M.F = dF;
+        M.ex = dex;
+        M.ey = dey;
+        M.Sx = dSx;
+        M.Sy = dSy;
+        if (o.dst_precision == QG_DST_BF16X3) {
+            // bf16 hi/lo split of the DST matrices (hi plane then lo plane)
+            auto split = [&](const std::vector<float>& S, uint16_t** dst) {
+                std::vector<uint16_t> h(2 * S.size());
+                for (size_t k = 0; k < S.size(); ++k) {
+                    auto bf = [](float f) {
+                        uint32_t u;
+                        std::memcpy(&u, &f, 4);
+                        u += 0x7fffu + ((u >> 16) & 1u);  // round to nearest even
+                        return (uint16_t)(u >> 16);
+                    };
+                    const uint16_t hi = bf(S[k]);
+                    uint32_t hu = (uint32_t)hi << 16;
+                    float hf;
+                    std::memcpy(&hf, &hu, 4);
+                    h[k] = hi;
+                    h[S.size() + k] = bf(S[k] - hf);
+                }
+                return upload(p, dst, h);
+            };
+            uint16_t *bx, *byy;
+            if ((e = split(Sx, &bx)) || (e = split(Sy, &byy))) break;
+            M.Sx_bf = bx;
+            M.Sy_bf = byy;
+        }
+        // tiles
+        for (int ty = 0; ty < (M.Ny + kStencilTY - 1) / kStencilTY; ++ty)
+            for (int tx = 0; tx < (M.Nx + kStencilTX - 1) / kStencilTX; ++tx) st.push_back({i, ty, tx});
+        for (int mt = 0; mt < (n * M.Ny + BMg - 1) / BMg; ++mt)
+            for (int nt = 0; nt < (M.Nx + BNg - 1) / BNg; ++nt) gx.push_back({i, mt, nt});
+        for (int mt = 0; mt < (n * M.Nx + BMg - 1) / BMg; ++mt)
+            for (int nt = 0; nt < (M.Ny + BNg - 1) / BNg; ++nt) gy.push_back({i, mt, nt});
+    }
+    if (e == cudaSuccess) {
+        p->state_size = off_state;
+        p->xplane = off_x;
+        p->yplane = off_y;
+        p->total_layers = off_layer;
+        std::vector<MemberDev> mv(p->mh);
+        e = upload(p, &p->md, mv);
+    }
+    if (e == cudaSuccess) {
+        p->n_st = (int)st.size();
+        p->n_gx = (int)gx.size();
+        p->n_gy = (int)gy.size();
+        if (!(e = upload(p, &p->st_tiles, st)) && !(e = upload(p, &p->gx_tiles, gx)))
+            e = upload(p, &p->gy_tiles, gy);
+    }
+    if (e == cudaSuccess) {
+        const size_t xb = (size_t)p->xplane * 4, yb = (size_t)p->yplane * 4;
+        if (!(e = dalloc(p, &p->XA, xb)) && !(e = dalloc(p, &p->XB, xb)) && !(e = dalloc(p, &p->XC, xb)) &&
+            !(e = dalloc(p, &p->YA, yb)) && !(e = dalloc(p, &p->YB, yb)) && !(e = dalloc(p, &p->S1, xb)) &&
+            !(e = dalloc(p, &p->S2, xb)) && !(e = dalloc(p, &p->params, (size_t)n_members * QG_NPARAMS * 4)) &&
+            !(e = dalloc(p, &p->flags, 16)))
+            e = dalloc(p, &p->diag_acc, (size_t)2 * p->total_layers * sizeof(double));
+        if (!e && o.refine_sweeps > 0) e = dalloc(p, &p->XQ, xb);
+    }
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        qg_plan_destroy(p);
+        return QG_ERR_CUDA;
+    }
+    *out = p;
+    return QG_OK;
+}
+
+void qg_plan_destroy(qg_plan* p) {
+    if (!p) return;
+    cudaDeviceSynchronize();
+    if (p->graph.exec) cudaGraphExecDestroy(p->graph.exec);
+    for (auto& v : p->ev)
+        for (auto& pr : v) {
+            cudaEventDestroy(pr.first);
+            cudaEventDestroy(pr.second);
+        }
+    if (p->cap) cudaStreamDestroy(p->cap);
+    for (void* a : p->allocs) cudaFree(a);
+    delete p;
+}
+
+int64_t qg_plan_state_size(const qg_plan* p) { return p ? p->state_size : -1; }
+
+int64_t qg_plan_member_offset(const qg_plan* p, int m) {
+    if (!p || m < 0 || m >= p->n_members) return -1;
+    return p->member_off[m];
+}
+
+int qg_plan_member_modes(const qg_plan* p, int m, double* lambdas, double* Cl2m, double* Cm2l) {
+    if (!p) return QG_ERR_NULL;
+    if (m < 0 || m >= p->n_members) return QG_ERR_ARG;
+    const qg_member_desc& d = p->desc[m];
+    const int n = d.n_layers;
+    if (lambdas) std::memcpy(lambdas, d.lambdas, sizeof(double) * n);
+    if (Cl2m) std::memcpy(Cl2m, d.Cl2m, sizeof(double) * n * n);
+    if (Cm2l) std::memcpy(Cm2l, d.Cm2l, sizeof(double) * n * n);
+    return QG_OK;
+}
+
+int qg_invert(qg_plan* p, const float* q, float* psi, void* stream) {
+    if (!p || !q || !psi) return QG_ERR_NULL;
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = run_prep(p, q, nullptr, 0, s);
+    if (!e) e = run_dst_solve(p, s);
+    if (!e)
+        e = timed(p, QG_K_OTHER, s, [&] { return launch_mode_to_layer(p->md, p->st_tiles, p->n_st, p->XC, psi, s); });
+    return cuda_err(e);
+}
+
+int qg_rhs(qg_plan* p, const float* q, float* dq, const float* params, int flags, void* stream) {
+    if (!p || !q || !dq || !params) return QG_ERR_NULL;
+    if (flags & ~QG_RHS_APPLY_BC) return QG_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int bc = (flags & QG_RHS_APPLY_BC) ? 1 : 0;
+    cudaError_t e = run_prep(p, q, nullptr, bc, s);
+    if (!e) e = run_dst_solve(p, s);
+    if (!e) {
+        StencilArgs a{};
+        a.members = p->md;
+        a.tiles = p->st_tiles;
+        a.q = q;
+        a.q_internal = 0;
+        a.psi_hat = p->XC;
+        a.params = params;
+        a.apply_bc = bc;
+        a.dq = dq;
+        a.flags = p->flags;
+        e = timed(p, QG_K_STENCIL, s, [&] { return launch_stencil(a, p->n_st, p->max_nl, p->xplane, s); });
+    }
+    return cuda_err(e);
+}
+
+int qg_step(qg_plan* p, float* q, const float* params, double dt, int n_steps, int scheme,
+            void* stream) {
+    if (!p || !q || !params) return QG_ERR_NULL;
+    if (n_steps < 0) return QG_ERR_ARG;
+    Stage st[4];
+    if (scheme_stages(scheme, st) == 0) return QG_ERR_ARG;
+    if (!(dt == dt)) return QG_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = cudaMemcpyAsync(p->params, params, sizeof(float) * p->n_members * QG_NPARAMS,
+                                    cudaMemcpyDeviceToDevice, s);
+    if (!e) e = run_prep(p, q, q, 1, s);  // integrate(): BC on the initial state
+    if (e) return cuda_err(e);
+    if (n_steps == 0) return QG_OK;
+    const bool use_graph = p->opts.use_graphs && !p->profiling;
+    if (!use_graph) {
+        for (int k = 0; k < n_steps && !e; ++k) e = run_one_step(p, q, p->params, (float)dt, scheme, s);
+        return cuda_err(e);
+    }
+    StepGraph& g = p->graph;
+    if (!g.exec || g.q != q || g.dt != dt || g.scheme != scheme) {
+        if (g.exec) {
+            cudaGraphExecDestroy(g.exec);
+            g.exec = nullptr;
+        }
+        cudaGraph_t graph = nullptr;
+        e = cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal);
+        if (!e) {
+            cudaError_t e1 = run_one_step(p, q, p->params, (float)dt, scheme, p->cap);
+            e = cudaStreamEndCapture(p->cap, &graph);
+            if (!e) e = e1;
+        }
+        if (!e) e = cudaGraphInstantiate(&g.exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (e) {
+            g.exec = nullptr;
+            return cuda_err(e);
+        }
+        g.q = q;
+        g.dt = dt;
+        g.scheme = scheme;
+    }
+    for (int k = 0; k < n_steps && !e; ++k) e = cudaGraphLaunch(g.exec, s);
+    return cuda_err(e);
+}
+
+int qg_diagnose(qg_plan* p, const float* q, float* ke, float* ens, void* stream) {
+    if (!p || !q || !ke || !ens) return QG_ERR_NULL;
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = run_prep(p, q, nullptr, 0, s);
+    if (!e) e = run_dst_solve(p, s);
+    if (!e) e = cudaMemsetAsync(p->diag_acc, 0, sizeof(double) * 2 * p->total_layers, s);
+    if (!e)
+        e = timed(p, QG_K_OTHER, s, [&] {
+            return launch_diag_acc(p->md, p->st_tiles, p->n_st, q, p->XC, p->diag_acc, s);
+        });
+    if (!e) e = launch_diag_finish(p->diag_acc, p->total_layers, ke, ens, s);
+    return cuda_err(e);
+}
+
+int qg_status(qg_plan* p, int* flags, void* stream) {
+    if (!p) return QG_ERR_NULL;
+    cudaStream_t s = (cudaStream_t)stream;
+    int h = 0;
+    cudaError_t e = cudaMemcpyAsync(&h, p->flags, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (!e) e = cudaStreamSynchronize(s);
+    if (!e) e = cudaMemsetAsync(p->flags, 0, sizeof(int), s);
+    if (!e) e = cudaStreamSynchronize(s);
+    if (e) return QG_ERR_CUDA;
+    if (flags) *flags = h;
+    if (h & 2) return QG_ERR_TIMEOUT;
+    if (h & 1) return QG_ERR_NONFINITE;
+    return QG_OK;
+}
+
+int qg_set_profiling(qg_plan* p, int enable) {
+    if (!p) return QG_ERR_NULL;
+    cudaDeviceSynchronize();
+    p->profiling = enable != 0;
+    for (auto& u : p->ev_used) u = 0;
+    return QG_OK;
+}
+
+int qg_kernel_stats(qg_plan* p, int k, double* total_ms, int64_t* launches) {
+    if (!p || !total_ms || !launches) return QG_ERR_NULL;
+    if (k < 0 || k >= QG_K_COUNT) return QG_ERR_ARG;
+    double t = 0.0;
+    for (size_t i = 0; i < p->ev_used[k]; ++i) {
+        cudaEventSynchronize(p->ev[k][i].second);
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, p->ev[k][i].first, p->ev[k][i].second) == cudaSuccess) t += ms;
+    }
+    *total_ms = t;
+    *launches = (int64_t)p->ev_used[k];
+    return QG_OK;
+}
+
+}  // extern "C"

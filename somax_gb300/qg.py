@@ -1,0 +1,554 @@
+"""Drop-in QG model classes whose hot path runs in libqgcore (hand-written sm_103a kernels).
+
+Mirrors the public API of ``somax/_src/models/qg/baroclinic.py`` (``BaroclinicQG``),
+``somax/_src/models/qg/barotropic.py`` (``BarotropicQG``) and the ``SomaxModel`` contract
+(``somax/_src/core/model.py``): ``create``, ``vector_field``, ``apply_boundary_conditions``,
+``integrate``, ``diagnose``, ``_invert_pv``; plus ``step`` for in-place stepping.  Arrays are
+float32 CUDA tensors laid out as in the reference, ``(nl, Ny, Nx)`` (``(Ny, Nx)`` for the
+barotropic model), ``Ny = ny + 2``, ``Nx = nx + 2``.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import math
+from typing import Sequence
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import K, MemberDesc, Options, check
+from .transforms import ModalTransform, StratificationProfile
+
+PRECISIONS = {"fp32": K["QG_DST_FP32"], "tf32": K["QG_DST_TF32"], "bf16x3": K["QG_DST_BF16X3"]}
+SCHEMES = {"euler": K["QG_SCHEME_EULER"], "heun": K["QG_SCHEME_HEUN"], "ssprk3": K["QG_SCHEME_SSPRK3"],
+           "tsit5": K["QG_SCHEME_TSIT5"]}
+
+
+# ---------------------------------------------------------------------------------------
+# Solver / SaveAt stand-ins for the diffrax objects integrate() accepts (core/model.py:75-88)
+# ---------------------------------------------------------------------------------------
+class _Solver:
+    name = ""
+
+    def __repr__(self):
+        return f"{type(self).__name__}()"
+
+
+class Euler(_Solver):
+    name = "euler"
+
+
+class Heun(_Solver):
+    name = "heun"
+
+
+class SSPRK3(_Solver):
+    name = "ssprk3"
+
+
+class Tsit5(_Solver):
+    name = "tsit5"
+
+
+@dataclasses.dataclass
+class SaveAt:
+    t1: bool = False
+    ts: Sequence[float] | None = None
+
+
+@dataclasses.dataclass
+class Solution:
+    ts: torch.Tensor
+    ys: object
+
+
+def _solver_name(s) -> str:
+    if s is None:
+        return "tsit5"
+    if isinstance(s, str):
+        if s not in SCHEMES:
+            raise ValueError(f"unknown solver {s!r}")
+        return s
+    if isinstance(s, _Solver):
+        return s.name
+    raise TypeError(f"unsupported solver {s!r}")
+
+
+# ---------------------------------------------------------------------------------------
+# State / params / diagnostics (core/types.py; baroclinic.py:23-88)
+# ---------------------------------------------------------------------------------------
+@dataclasses.dataclass
+class State:
+    q: torch.Tensor
+
+
+class BaroclinicQGState(State):
+    pass
+
+
+class BarotropicQGState(State):
+    pass
+
+
+@dataclasses.dataclass
+class QGParams:
+    """Differentiable parameters (``baroclinic.py:37-48``) plus the biharmonic extension."""
+
+    lateral_viscosity: torch.Tensor
+    bottom_drag: torch.Tensor
+    wind_amplitude: torch.Tensor
+    biharmonic_viscosity: torch.Tensor
+
+    def vector(self, device) -> torch.Tensor:
+        return torch.stack([torch.as_tensor(v, dtype=torch.float32, device=device).reshape(())
+                            for v in (self.lateral_viscosity, self.bottom_drag, self.wind_amplitude,
+                                      self.biharmonic_viscosity)])
+
+
+BaroclinicQGParams = QGParams
+BarotropicQGParams = QGParams
+
+
+@dataclasses.dataclass
+class QGDiagnostics:
+    psi: torch.Tensor
+    u: torch.Tensor
+    v: torch.Tensor
+    kinetic_energy: torch.Tensor
+    total_kinetic_energy: torch.Tensor
+    enstrophy: torch.Tensor
+    total_enstrophy: torch.Tensor
+    relative_vorticity: torch.Tensor
+    rossby_radii: np.ndarray | None
+
+
+BaroclinicQGDiagnostics = QGDiagnostics
+BarotropicQGDiagnostics = QGDiagnostics
+
+
+@dataclasses.dataclass(frozen=True)
+class Grid:
+    """Arakawa C-grid with one ghost ring (finitevolx ``ArakawaCGrid2D.from_interior``)."""
+
+    nx: int
+    ny: int
+    Lx: float
+    Ly: float
+
+    @property
+    def Nx(self):
+        return self.nx + 2
+
+    @property
+    def Ny(self):
+        return self.ny + 2
+
+    @property
+    def dx(self):
+        return self.Lx / self.nx
+
+    @property
+    def dy(self):
+        return self.Ly / self.ny
+
+
+# ---------------------------------------------------------------------------------------
+# Plan: one libqgcore plan for one or more members
+# ---------------------------------------------------------------------------------------
+def _stream_handle(device) -> C.c_void_p:
+    return C.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+class Plan:
+    """Owns a ``qg_plan`` (device constants + workspace) on one CUDA device."""
+
+    def __init__(self, members: Sequence["MemberSpec"], precision="fp32", refine=0, use_graphs=True,
+                 device=None):
+        if not torch.cuda.is_available():
+            raise RuntimeError("somax_gb300 needs a CUDA device (no CPU fallback)")
+        self.device = torch.device(device or "cuda", torch.cuda.current_device()) if device is None \
+            else torch.device(device)
+        L = _lib.lib()
+        arr = (MemberDesc * len(members))()
+        for i, m in enumerate(members):
+            m.fill(arr[i])
+        opts = Options(PRECISIONS[precision], int(refine), int(bool(use_graphs)))
+        handle = C.c_void_p()
+        with torch.cuda.device(self.device):
+            check(L.qg_plan_create(arr, len(members), C.byref(opts), C.byref(handle)), "qg_plan_create")
+        self._h = handle
+        self._L = L
+        self.members = list(members)
+        self.precision = precision
+        self.state_size = int(L.qg_plan_state_size(handle))
+        self.offsets = [int(L.qg_plan_member_offset(handle, i)) for i in range(len(members))]
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                self._L.qg_plan_destroy(h)
+            except Exception:  # pragma: no cover
+                pass
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def member_modes(self, i: int):
+        n = self.members[i].n_layers
+        lam = (C.c_double * n)()
+        a = (C.c_double * (n * n))()
+        b = (C.c_double * (n * n))()
+        check(self._L.qg_plan_member_modes(self._h, i, lam, a, b), "qg_plan_member_modes")
+        return np.array(lam), np.array(a).reshape(n, n), np.array(b).reshape(n, n)
+
+    def _check_field(self, t: torch.Tensor, name: str):
+        if not isinstance(t, torch.Tensor) or t.device.type != "cuda" or t.dtype != torch.float32:
+            raise TypeError(f"{name} must be a float32 CUDA tensor")
+        if not t.is_contiguous() or t.numel() != self.state_size:
+            raise ValueError(f"{name} must be contiguous with {self.state_size} elements, got {tuple(t.shape)}")
+
+    def invert(self, q: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        self._check_field(q, "q")
+        out = torch.empty_like(q) if out is None else out
+        self._check_field(out, "psi")
+        check(self._L.qg_invert(self._h, C.c_void_p(q.data_ptr()), C.c_void_p(out.data_ptr()),
+                                _stream_handle(q.device)), "qg_invert")
+        return out
+
+    def rhs(self, q: torch.Tensor, params: torch.Tensor, apply_bc=False, out=None) -> torch.Tensor:
+        self._check_field(q, "q")
+        out = torch.empty_like(q) if out is None else out
+        self._check_field(out, "dq")
+        params = params.detach().to(device=q.device, dtype=torch.float32).contiguous()
+        if params.numel() != 4 * len(self.members):
+            raise ValueError("params must hold 4 values per member")
+        flags = K["QG_RHS_APPLY_BC"] if apply_bc else 0
+        check(self._L.qg_rhs(self._h, C.c_void_p(q.data_ptr()), C.c_void_p(out.data_ptr()),
+                             C.c_void_p(params.data_ptr()), flags, _stream_handle(q.device)), "qg_rhs")
+        return out
+
+    def step(self, q: torch.Tensor, params: torch.Tensor, dt: float, n_steps: int, scheme: str) -> torch.Tensor:
+        """Advance q in place (integrate() semantics: ring zeroed first, BC on every stage)."""
+        self._check_field(q, "q")
+        params = params.detach().to(device=q.device, dtype=torch.float32).contiguous()
+        if params.numel() != 4 * len(self.members):
+            raise ValueError("params must hold 4 values per member")
+        check(self._L.qg_step(self._h, C.c_void_p(q.data_ptr()), C.c_void_p(params.data_ptr()),
+                              float(dt), int(n_steps), SCHEMES[scheme], _stream_handle(q.device)), "qg_step")
+        return q
+
+    def diagnose(self, q: torch.Tensor):
+        self._check_field(q, "q")
+        nlt = sum(m.n_layers for m in self.members)
+        ke = torch.empty(nlt, device=q.device, dtype=torch.float32)
+        en = torch.empty(nlt, device=q.device, dtype=torch.float32)
+        check(self._L.qg_diagnose(self._h, C.c_void_p(q.data_ptr()), C.c_void_p(ke.data_ptr()),
+                                  C.c_void_p(en.data_ptr()), _stream_handle(q.device)), "qg_diagnose")
+        return ke, en
+
+    def status(self, device=None) -> int:
+        flags = C.c_int(0)
+        code = self._L.qg_status(self._h, C.byref(flags), _stream_handle(device or self.device))
+        if code not in (0, K["QG_ERR_NONFINITE"], K["QG_ERR_TIMEOUT"]):
+            check(code, "qg_status")
+        return code
+
+    def set_profiling(self, on: bool):
+        check(self._L.qg_set_profiling(self._h, int(on)), "qg_set_profiling")
+
+    def kernel_stats(self, kclass: int):
+        t = C.c_double()
+        n = C.c_int64()
+        check(self._L.qg_kernel_stats(self._h, kclass, C.byref(t), C.byref(n)), "qg_kernel_stats")
+        return t.value, n.value
+
+
+@dataclasses.dataclass
+class MemberSpec:
+    """One member of a plan (fills ``qg_member_desc``)."""
+
+    nx: int
+    ny: int
+    Lx: float
+    Ly: float
+    f0: float
+    beta: float
+    H: Sequence[float]
+    g_prime: Sequence[float]
+    barotropic: bool = False
+    wind_profile: str = "doublegyre"
+    eigs: str = "consistent"
+    modal: ModalTransform | None = None
+
+    @property
+    def n_layers(self) -> int:
+        return 1 if self.barotropic else len(self.H)
+
+    @property
+    def cells(self) -> int:
+        return self.n_layers * (self.nx + 2) * (self.ny + 2)
+
+    def fill(self, d: MemberDesc) -> None:
+        n = self.n_layers
+        d.nx, d.ny, d.n_layers, d.barotropic = self.nx, self.ny, n, int(self.barotropic)
+        d.Lx, d.Ly, d.f0, d.beta = self.Lx, self.Ly, self.f0, self.beta
+        for k in range(n):
+            d.H[k] = float(self.H[k]) if not self.barotropic else 1.0
+            d.g_prime[k] = float(self.g_prime[k]) if not self.barotropic else 1.0
+        d.wind_profile = K["QG_WIND_SINGLE"] if self.wind_profile == "single" else K["QG_WIND_DOUBLEGYRE"]
+        d.eigs_mode = K["QG_EIGS_REFERENCE"] if self.eigs == "reference" else K["QG_EIGS_CONSISTENT"]
+        if self.modal is not None and not self.barotropic:
+            d.has_modes = 1
+            lam = self.f0**2 * np.asarray(self.modal.eigenvalues, float)
+            for r in range(n):
+                d.lambdas[r] = float(lam[r])
+                for c in range(n):
+                    d.Cl2m[r * n + c] = float(self.modal.Cl2m[r, c])
+                    d.Cm2l[r * n + c] = float(self.modal.Cm2l[r, c])
+
+
+# ---------------------------------------------------------------------------------------
+# Models
+# ---------------------------------------------------------------------------------------
+class SomaxModel:
+    """The model contract of ``core/model.py:12-95``."""
+
+    def vector_field(self, t, state, args=None):  # pragma: no cover - abstract
+        raise NotImplementedError
+
+    def apply_boundary_conditions(self, state):  # pragma: no cover - abstract
+        raise NotImplementedError
+
+
+def _zero_ring(q: torch.Tensor) -> torch.Tensor:
+    out = q.clone()
+    out[..., 0, :] = 0
+    out[..., -1, :] = 0
+    out[..., :, 0] = 0
+    out[..., :, -1] = 0
+    return out
+
+
+class _QGBase(SomaxModel):
+    state_cls = State
+    barotropic = False
+
+    def __init__(self, spec: MemberSpec, params: QGParams, precision="fp32", refine=0, use_graphs=True,
+                 strat=None, modal=None):
+        self.spec = spec
+        self.params = params
+        self.precision = precision
+        self.refine = refine
+        self.use_graphs = use_graphs
+        self.strat = strat
+        self.modal = modal
+        self.grid = Grid(spec.nx, spec.ny, spec.Lx, spec.Ly)
+        self._plans: dict = {}
+
+    # the plan is created lazily on the device of the first field it sees
+    def plan(self, device=None) -> Plan:
+        device = torch.device(device if device is not None else "cuda")
+        if device.index is None:
+            device = torch.device("cuda", torch.cuda.current_device())
+        key = device.index
+        if key not in self._plans:
+            self._plans[key] = Plan([self.spec], self.precision, self.refine, self.use_graphs, device)
+        return self._plans[key]
+
+    @property
+    def shape(self):
+        g = self.grid
+        return (g.Ny, g.Nx) if self.barotropic else (self.spec.n_layers, g.Ny, g.Nx)
+
+    def _field(self, q: torch.Tensor) -> torch.Tensor:
+        if tuple(q.shape) != self.shape:
+            raise ValueError(f"q must have shape {self.shape}, got {tuple(q.shape)}")
+        if q.device.type != "cuda":
+            raise TypeError("q must live on a CUDA device")
+        return q.to(torch.float32).contiguous()
+
+    def _param_vector(self, device) -> torch.Tensor:
+        return self.params.vector(device)
+
+    # -- reference API -------------------------------------------------------------------
+    def _invert_pv(self, q: torch.Tensor) -> torch.Tensor:
+        q = self._field(q)
+        return self.plan(q.device).invert(q)
+
+    def vector_field(self, t, state, args=None):
+        """dq/dt for ``state.q`` as given (no BC applied, like the reference)."""
+        q = self._field(state.q)
+        dq = self.plan(q.device).rhs(q, self._param_vector(q.device), apply_bc=False)
+        return self.state_cls(q=dq)
+
+    def apply_boundary_conditions(self, state):
+        return self.state_cls(q=_zero_ring(state.q))
+
+    def step(self, state, dt: float, n_steps: int = 1, solver="ssprk3", out: torch.Tensor | None = None):
+        """Advance ``n_steps`` constant steps on the GPU; returns a new state.
+
+        A state held in host memory is copied to the current CUDA device, stepped there and
+        copied back (into ``out`` if given; pinned memory makes both copies asynchronous)."""
+        q_in = state.q
+        host = q_in.device.type == "cpu"
+        if host:
+            if tuple(q_in.shape) != self.shape:
+                raise ValueError(f"q must have shape {self.shape}, got {tuple(q_in.shape)}")
+            dev = torch.device("cuda", torch.cuda.current_device())
+            q = q_in.to(device=dev, dtype=torch.float32, non_blocking=True).contiguous()
+        else:
+            q = self._field(q_in).clone()
+        scheme = _solver_name(solver)
+        if scheme in ("heun", "ssprk3"):
+            self.plan(q.device).step(q, self._param_vector(q.device), dt, n_steps, scheme)
+        else:
+            q = self._host_rk(q, dt, n_steps, scheme)
+        if host:
+            if out is None:
+                out = torch.empty(q.shape, dtype=torch.float32, pin_memory=True)
+            out.copy_(q, non_blocking=True)
+            return self.state_cls(q=out)
+        return self.state_cls(q=q)
+
+    def _host_rk(self, q, dt, n_steps, scheme):
+        # Tableau schemes not yet fused into qg_step: stage loop over the fused RHS kernel.
+        from .tableaus import rk_tableau
+
+        plan = self.plan(q.device)
+        pv = self._param_vector(q.device)
+        a, b = rk_tableau(scheme)
+        y = _zero_ring(q)
+        for _ in range(n_steps):
+            ks = []
+            for s in range(len(b)):
+                ys = y
+                if s:
+                    acc = torch.zeros_like(y)
+                    for j, aj in enumerate(a[s]):
+                        if aj:
+                            acc.add_(ks[j], alpha=aj)
+                    ys = y + dt * acc
+                ks.append(plan.rhs(ys, pv, apply_bc=True))
+            acc = torch.zeros_like(y)
+            for j, bj in enumerate(b):
+                if bj:
+                    acc.add_(ks[j], alpha=bj)
+            y = y + dt * acc
+        return y
+
+    def integrate(self, state0, t0: float, t1: float, dt: float, solver=None, saveat=None, **kw):
+        """``SomaxModel.integrate`` with constant steps (``core/model.py:53-88``)."""
+        if kw.get("stepsize_controller") not in (None, "constant"):
+            raise ValueError("only constant step sizes are supported")
+        scheme = _solver_name(solver)
+        saveat = saveat or SaveAt(t1=True)
+        n_total = int(round((t1 - t0) / dt))
+        if abs(n_total * dt - (t1 - t0)) > 1e-9 * max(1.0, abs(t1 - t0)):
+            raise ValueError("(t1 - t0) must be a whole number of steps")
+        if saveat.ts is not None:
+            targets = [int(round((float(t) - t0) / dt)) for t in saveat.ts]
+        else:
+            targets = [n_total]
+        state = self.apply_boundary_conditions(state0)
+        ys, done = [], 0
+        q = state.q
+        for tgt in targets:
+            if tgt < done:
+                raise ValueError("saveat.ts must be increasing")
+            if tgt > done:
+                q = self.step(self.state_cls(q=q), dt, tgt - done, scheme).q
+                done = tgt
+            ys.append(q.clone())
+        ts = torch.tensor([t0 + k * dt for k in targets], dtype=torch.float64)
+        return Solution(ts=ts, ys=self.state_cls(q=torch.stack(ys)))
+
+    def diagnose(self, state) -> QGDiagnostics:
+        q = self._field(state.q)
+        plan = self.plan(q.device)
+        psi = plan.invert(q)
+        ke, en = plan.diagnose(q)
+        g = self.grid
+        p3 = psi.reshape((-1, g.Ny, g.Nx))
+        u = torch.zeros_like(p3)
+        v = torch.zeros_like(p3)
+        u[:, 1:-1, 1:-1] = -(p3[:, 2:, 1:-1] - p3[:, 1:-1, 1:-1]) / g.dy
+        v[:, 1:-1, 1:-1] = (p3[:, 1:-1, 2:] - p3[:, 1:-1, 1:-1]) / g.dx
+        zeta = torch.zeros_like(p3)
+        c = p3[:, 1:-1, 1:-1]
+        zeta[:, 1:-1, 1:-1] = (p3[:, 1:-1, 2:] - 2 * c + p3[:, 1:-1, :-2]) / g.dx**2 + (
+            p3[:, 2:, 1:-1] - 2 * c + p3[:, :-2, 1:-1]) / g.dy**2
+        shp = psi.shape
+        radii = None if self.modal is None else self.modal.rossby_radii
+        if self.barotropic:
+            ke, en = ke[0], en[0]
+        return QGDiagnostics(psi=psi, u=u.reshape(shp), v=v.reshape(shp), kinetic_energy=ke,
+                             total_kinetic_energy=ke.sum(), enstrophy=en, total_enstrophy=en.sum(),
+                             relative_vorticity=zeta.reshape(shp), rossby_radii=radii)
+
+
+class BaroclinicQG(_QGBase):
+    """Multilayer QG on an Arakawa C-grid (``baroclinic.py:91-332``)."""
+
+    state_cls = BaroclinicQGState
+
+    @property
+    def helmholtz_lambdas(self) -> np.ndarray:
+        return self.spec.f0**2 * np.asarray(self.modal.eigenvalues)
+
+    @property
+    def beta_y(self) -> np.ndarray:
+        g = self.grid
+        y = np.arange(g.Ny) * g.dy
+        return np.broadcast_to((self.spec.beta * (y - g.Ly / 2.0))[:, None], (g.Ny, g.Nx))
+
+    @staticmethod
+    def create(nx=64, ny=64, Lx=4e6, Ly=4e6, f0=9.375e-5, beta=1.754e-11, n_layers=3,
+               H=(400.0, 1100.0, 2600.0), g_prime=(9.81, 0.025, 0.0125), stratification=None,
+               lateral_viscosity=0.0, bottom_drag=0.0, wind_amplitude=0.0, wind_profile="doublegyre",
+               poisson_bc="dst", biharmonic_viscosity=0.0, precision="fp32", refine=0, eigs="consistent",
+               use_graphs=True) -> "BaroclinicQG":
+        """``BaroclinicQG.create`` (``baroclinic.py:230-332``) with the same keyword arguments,
+        plus ``biharmonic_viscosity`` (extension), ``precision`` of the DST-I GEMMs
+        ("fp32", "tf32", "bf16x3"), ``refine`` sweeps and the ``eigs`` mode."""
+        if poisson_bc != "dst":
+            raise ValueError("only the Dirichlet DST-I inversion (poisson_bc='dst') is implemented")
+        if stratification is not None:
+            strat = stratification
+        else:
+            if len(H) != n_layers or len(g_prime) != n_layers:
+                raise ValueError(f"n_layers ({n_layers}), len(H) ({len(H)}), and len(g_prime) "
+                                 f"({len(g_prime)}) must all be equal")
+            strat = StratificationProfile.from_layers(H=list(H), g_prime=list(g_prime))
+        modal = ModalTransform.from_stratification(strat, f0, eigs)
+        spec = MemberSpec(nx, ny, Lx, Ly, f0, beta, list(strat.H), list(strat.g_prime), False, wind_profile,
+                          eigs, modal)
+        params = QGParams(*(torch.tensor(float(v)) for v in (lateral_viscosity, bottom_drag, wind_amplitude,
+                                                             biharmonic_viscosity)))
+        return BaroclinicQG(spec, params, precision, refine, use_graphs, strat, modal)
+
+    @property
+    def n_layers(self):
+        return self.spec.n_layers
+
+
+class BarotropicQG(_QGBase):
+    """Barotropic QG (``barotropic.py:79-248``): Poisson inversion, psi ring kept."""
+
+    state_cls = BarotropicQGState
+    barotropic = True
+
+    @staticmethod
+    def create(nx=64, ny=64, Lx=1e6, Ly=1e6, f0=1e-4, beta=1.6e-11, lateral_viscosity=0.0,
+               bottom_drag=0.0, wind_amplitude=0.0, wind_profile="doublegyre", biharmonic_viscosity=0.0,
+               precision="fp32", refine=0, use_graphs=True) -> "BarotropicQG":
+        """``BarotropicQG.create`` (``barotropic.py:186-248``)."""
+        spec = MemberSpec(nx, ny, Lx, Ly, f0, beta, [1.0], [1.0], True, wind_profile)
+        params = QGParams(*(torch.tensor(float(v)) for v in (lateral_viscosity, bottom_drag, wind_amplitude,
+                                                             biharmonic_viscosity)))
+        return BarotropicQG(spec, params, precision, refine, use_graphs)

@@ -1,0 +1,119 @@
+"""Seeded synthetic workloads of the QG time step (double-gyre basins).
+
+Shapes and parameters of the five benchmark configurations; the initial PV is a seeded
+Gaussian random field with an isotropic k^-3 spectrum (no dataset is involved).  Wind
+amplitudes follow the reference factory's convention: ``wind_amplitude = tau0 * 2 pi /
+(rho0 * Ly)`` with the ``-sin(2 pi y / Ly)`` double-gyre pattern
+(``somax/_src/models/gfd_testcases.py:250-251``, ``baroclinic.py:316-318``).
+"""
+
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+import scipy.fft as sfft
+
+RHO0 = 1000.0
+L_BASIN = 5.12e6
+F0 = 9.375e-5
+BETA = 1.754e-11
+
+
+def wind_amplitude(tau0: float, Ly: float = L_BASIN, rho0: float = RHO0) -> float:
+    """Wind-stress curl amplitude of a tau0 (N/m^2) double gyre."""
+    return tau0 * 2.0 * math.pi / (rho0 * Ly)
+
+
+@dataclasses.dataclass
+class QGConfig:
+    name: str
+    n: int                       # interior cells per side
+    H: tuple
+    g_prime: tuple
+    dt: float
+    scheme: str
+    lateral_viscosity: float = 0.0
+    biharmonic_viscosity: float = 0.0
+    bottom_drag: float = 1e-7
+    tau0: float = 0.08
+    L: float = L_BASIN
+
+    @property
+    def nl(self) -> int:
+        return len(self.H)
+
+    @property
+    def steps_per_day(self) -> float:
+        return 86400.0 / self.dt
+
+    def model_kwargs(self) -> dict:
+        return dict(nx=self.n, ny=self.n, Lx=self.L, Ly=self.L, f0=F0, beta=BETA, n_layers=self.nl,
+                    H=tuple(self.H), g_prime=tuple(self.g_prime), lateral_viscosity=self.lateral_viscosity,
+                    bottom_drag=self.bottom_drag, wind_amplitude=wind_amplitude(self.tau0, self.L),
+                    biharmonic_viscosity=self.biharmonic_viscosity)
+
+
+# Barotropic double gyre with a 50 km deformation radius: a 1-layer model with
+# g' = (f0 Rd)^2 / H so that f0^2 / (g' H) = 1 / Rd^2.
+RD_C1 = 5.0e4
+C1 = QGConfig("barotropic_64", 64, (4000.0,), ((F0 * RD_C1) ** 2 / 4000.0,), 4000.0, "heun",
+              lateral_viscosity=100.0)
+C2 = QGConfig("baroclinic3_128", 128, (400.0, 1100.0, 2600.0), (9.81, 0.025, 0.0125), 1200.0, "ssprk3",
+              biharmonic_viscosity=2e9)
+C3_512 = dataclasses.replace(C2, name="baroclinic3_512", n=512)
+C3_1024 = dataclasses.replace(C2, name="baroclinic3_1024", n=1024)
+C5 = dataclasses.replace(C2, name="baroclinic3_256", n=256)
+# Five layers, H geometric from 200 m to 2000 m; reduced gravities chosen to decrease with
+# depth (the configuration leaves them open).
+H5 = tuple(float(200.0 * 10 ** (k / 4)) for k in range(5))
+G5 = (9.81, 0.030, 0.020, 0.0125, 0.008)
+C4_MIX = (
+    (96, dataclasses.replace(C1, name="ens_barotropic_64", dt=1200.0, scheme="ssprk3")),
+    (96, dataclasses.replace(C2, name="ens_baroclinic3_128")),
+    (48, dataclasses.replace(C2, name="ens_baroclinic3_256", n=256)),
+    (16, dataclasses.replace(C2, name="ens_baroclinic5_256", n=256, H=H5, g_prime=G5)),
+)
+CONFIGS = {c.name: c for c in (C1, C2, C3_512, C3_1024, C5)}
+
+
+def kminus3_field(n: int, seed: int, nl: int = 1) -> np.ndarray:
+    """(nl, n+2, n+2) float64 fields, zero ring, unit RMS interior, with power spectrum
+    proportional to k^-3 over the interior DST-I wavenumbers."""
+    rng = np.random.default_rng(seed)
+    k = np.arange(1, n + 1, dtype=np.float64)
+    kk = np.sqrt(k[:, None] ** 2 + k[None, :] ** 2)
+    amp = kk ** -1.5
+    out = np.zeros((nl, n + 2, n + 2))
+    for l in range(nl):
+        c = rng.standard_normal((n, n)) * amp
+        f = sfft.idstn(c, type=1, norm="ortho")
+        out[l, 1:-1, 1:-1] = f / np.sqrt(np.mean(f * f))
+    return out
+
+
+def initial_pv(cfg: QGConfig, seed: int = 0, rms_vorticity: float = 1e-6) -> np.ndarray:
+    """Seeded k^-3 PV with RMS relative vorticity ``rms_vorticity`` in the top layer.
+
+    The relative vorticity of a PV field q is lap(psi) with (lap - lambda) psi = q; its RMS
+    is evaluated spectrally on the interior (Dirichlet) modes with the barotropic-mode
+    lambda.  Deeper layers are scaled by H[0] / H[k] (thicker layers carry weaker PV
+    anomalies).
+    """
+    n = cfg.n
+    f = kminus3_field(n, seed, cfg.nl)
+    d = cfg.L / n
+    k = np.arange(1, n + 1)
+    e = (2 * np.cos(np.pi * k / (n + 1)) - 2) / d**2
+    E = e[:, None] + e[None, :]
+    if cfg.nl == 1:
+        lam = F0**2 / (cfg.g_prime[0] * cfg.H[0])
+    else:
+        lam = 0.0
+    c = sfft.dstn(f[0, 1:-1, 1:-1], type=1, norm="ortho")
+    zeta = sfft.idstn(c * E / (E - lam), type=1, norm="ortho")
+    scale = rms_vorticity / np.sqrt(np.mean(zeta**2))
+    for l in range(cfg.nl):
+        f[l] *= scale * cfg.H[0] / cfg.H[l]
+    return f

@@ -1,0 +1,244 @@
+"""Parity of the CUDA path (through the C ABI) with the float64 oracle.
+
+Tolerances (relative L2 against float64):
+  * PV inversion psi and single-step RHS: RTOL_INV / RTOL_RHS (FP32 arithmetic; the RHS
+    differences amplify the inversion's rounding by the stencil's cancellation)
+  * state after 1 and 10 steps: RTOL_STEP = 1e-5, the benchmark spec's bound on q after 10 steps
+"""
+
+import numpy as np
+import pytest
+import torch
+
+import somax_gb300 as sg
+from oracle import qg as O
+from somax_gb300 import testcases as tc
+
+pytestmark = pytest.mark.gpu
+
+RTOL_INV = 2e-6
+RTOL_RHS = 2e-5
+RTOL_STEP = 1e-5
+
+
+def rel(a, b):
+    a = a.detach().cpu().double().numpy() if isinstance(a, torch.Tensor) else a
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def pair(nx, ny, nl, barotropic=False, nu=0.0, kappa=0.0, tau=0.0, nu4=0.0, L=(2e6, 1.6e6), precision="fp32",
+         refine=0, eigs="consistent"):
+    H = (400.0, 1100.0, 2600.0, 900.0, 1500.0, 700.0, 300.0, 2000.0)[:nl]
+    g = (9.81, 0.025, 0.0125, 0.01, 0.008, 0.006, 0.004, 0.003)[:nl]
+    if barotropic:
+        m = sg.BarotropicQG.create(nx=nx, ny=ny, Lx=L[0], Ly=L[1], lateral_viscosity=nu, bottom_drag=kappa,
+                                   wind_amplitude=tau, biharmonic_viscosity=nu4, precision=precision, refine=refine)
+        o = O.barotropic_model(nx=nx, ny=ny, Lx=L[0], Ly=L[1], lateral_viscosity=nu, bottom_drag=kappa,
+                               wind_amplitude=tau, biharmonic_viscosity=nu4)
+    else:
+        m = sg.BaroclinicQG.create(nx=nx, ny=ny, Lx=L[0], Ly=L[1], n_layers=nl, H=H, g_prime=g,
+                                   lateral_viscosity=nu, bottom_drag=kappa, wind_amplitude=tau,
+                                   biharmonic_viscosity=nu4, precision=precision, refine=refine, eigs=eigs)
+        o = O.baroclinic_model(nx=nx, ny=ny, Lx=L[0], Ly=L[1], H=H, g_prime=g, lateral_viscosity=nu,
+                               bottom_drag=kappa, wind_amplitude=tau, biharmonic_viscosity=nu4, eigs=eigs)
+    return m, o
+
+
+def field(shape, seed, ring=True, scale=1e-6):
+    rng = np.random.default_rng(seed)
+    n = shape[-1] - 2
+    base = tc.kminus3_field(max(shape[-2], shape[-1]) - 2, seed, int(np.prod(shape[:-2]) or 1))
+    q = base[:, : shape[-2], : shape[-1]].reshape(shape) * scale
+    q = q + 0.1 * scale * rng.standard_normal(shape)  # small-scale content too
+    if not ring:
+        q = O.zero_boundaries(q)
+    return q
+
+
+def cuda(x):
+    return torch.tensor(x, dtype=torch.float32, device="cuda")
+
+
+SHAPES = [(3, 5, 1), (5, 3, 2), (17, 13, 3), (30, 30, 3), (20, 26, 5), (40, 33, 8)]
+
+
+@pytest.mark.parametrize("nx,ny,nl", SHAPES)
+def test_invert(nx, ny, nl):
+    m, o = pair(nx, ny, nl)
+    q = field((nl, ny + 2, nx + 2), 1)
+    psi = m._invert_pv(cuda(q))
+    ref = O.invert_pv(o, q)
+    assert rel(psi, ref) < RTOL_INV
+    # the ring of psi is zero (baroclinic.py:158)
+    p = psi.cpu().numpy()
+    assert np.all(p[:, 0] == 0) and np.all(p[:, :, 0] == 0) and np.all(p[:, -1] == 0) and np.all(p[:, :, -1] == 0)
+
+
+@pytest.mark.parametrize("nx,ny", [(3, 5), (17, 13), (64, 64)])
+def test_invert_barotropic_keeps_ring(nx, ny):
+    m, o = pair(nx, ny, 1, barotropic=True)
+    q = field((ny + 2, nx + 2), 2)
+    psi = m._invert_pv(cuda(q))
+    assert rel(psi, O.invert_pv(o, q)) < RTOL_INV
+
+
+@pytest.mark.parametrize("nx,ny,nl", SHAPES)
+@pytest.mark.parametrize("ring", [True, False])
+def test_rhs(nx, ny, nl, ring):
+    m, o = pair(nx, ny, nl, nu=80.0, kappa=1e-7, tau=1e-10, nu4=1e9)
+    q = field((nl, ny + 2, nx + 2), 3, ring=ring)
+    dq = m.vector_field(0.0, sg.BaroclinicQGState(q=cuda(q))).q
+    assert rel(dq, O.vector_field(o, q)) < RTOL_RHS
+
+
+@pytest.mark.parametrize("nx,ny", [(5, 3), (31, 17), (64, 64)])
+def test_rhs_barotropic(nx, ny):
+    m, o = pair(nx, ny, 1, barotropic=True, nu=80.0, kappa=1e-7, tau=1e-10, L=(1e6, 1e6))
+    q = field((ny + 2, nx + 2), 4)
+    dq = m.vector_field(0.0, sg.BarotropicQGState(q=cuda(q))).q
+    assert rel(dq, O.vector_field(o, q)) < RTOL_RHS
+
+
+def test_zero_pv_zero_tendency_and_wind_top_only():  # test_qg_baroclinic.py:79-112
+    m, _ = pair(16, 16, 2)
+    z = torch.zeros((2, 18, 18), device="cuda")
+    assert float(m.vector_field(0.0, sg.BaroclinicQGState(q=z)).q.abs().max()) < 1e-12
+    m, _ = pair(16, 16, 2, tau=1e-10)
+    dq = m.vector_field(0.0, sg.BaroclinicQGState(q=z)).q
+    assert float(dq[0].abs().max()) > 0 and float(dq[1].abs().max()) < 1e-15
+
+
+def test_apply_bc_flag_equals_zeroed_input():
+    m, o = pair(20, 20, 3, nu=50.0, tau=1e-10)
+    q = field((3, 22, 22), 5)
+    plan = m.plan()
+    pv = m._param_vector(torch.device("cuda"))
+    a = plan.rhs(cuda(q), pv, apply_bc=True)
+    b = plan.rhs(cuda(O.zero_boundaries(q)), pv, apply_bc=False)
+    assert torch.equal(a, b)
+
+
+@pytest.mark.parametrize("scheme", ["heun", "ssprk3"])
+@pytest.mark.parametrize("nx,ny,nl", [(17, 13, 3), (30, 30, 1), (24, 24, 5)])
+def test_step(scheme, nx, ny, nl):
+    m, o = pair(nx, ny, nl, nu=100.0, kappa=1e-7, tau=1e-10, nu4=1e9, L=(1e6, 1e6))
+    q = field((nl, ny + 2, nx + 2), 6)
+    for n in (1, 3):
+        got = m.step(sg.BaroclinicQGState(q=cuda(q)), 1200.0, n, scheme).q
+        ref = O.integrate(o, q, 1200.0, n, scheme)
+        assert rel(got, ref) < RTOL_STEP
+        g = got.cpu().double().numpy()
+        assert rel(g[:, 1:-1, 1:-1], ref[:, 1:-1, 1:-1]) < RTOL_STEP
+
+
+def test_step_graph_and_eager_agree():
+    m, _ = pair(30, 30, 3, nu=100.0, tau=1e-10)
+    q = cuda(field((3, 32, 32), 7))
+    a = m.step(sg.BaroclinicQGState(q=q), 1200.0, 4, "ssprk3").q
+    m2 = sg.BaroclinicQG.create(nx=30, ny=30, Lx=2e6, Ly=1.6e6, n_layers=3, lateral_viscosity=100.0,
+                                wind_amplitude=1e-10, use_graphs=False)
+    b = m2.step(sg.BaroclinicQGState(q=q), 1200.0, 4, "ssprk3").q
+    assert torch.equal(a, b)
+
+
+def _config_pair(cfg):
+    kw = cfg.model_kwargs()
+    m = sg.BaroclinicQG.create(**kw)
+    o = O.baroclinic_model(nx=cfg.n, ny=cfg.n, Lx=cfg.L, Ly=cfg.L, f0=kw["f0"], beta=kw["beta"], H=cfg.H,
+                           g_prime=cfg.g_prime, lateral_viscosity=cfg.lateral_viscosity,
+                           bottom_drag=cfg.bottom_drag, wind_amplitude=kw["wind_amplitude"],
+                           biharmonic_viscosity=cfg.biharmonic_viscosity)
+    return m, o
+
+
+def test_config1_barotropic_64_heun():
+    # 64^2, 1-layer Helmholtz (Rd 50 km), Heun dt = 4000 s: 1 step and 100 steps
+    cfg = tc.C1
+    m, o = _config_pair(cfg)
+    q0 = tc.initial_pv(cfg, seed=0)
+    dq = m.vector_field(0.0, sg.BaroclinicQGState(q=cuda(q0))).q
+    assert rel(dq, O.vector_field(o, q0)) < RTOL_RHS
+    q1 = m.step(sg.BaroclinicQGState(q=cuda(q0)), cfg.dt, 1, cfg.scheme).q
+    assert rel(q1, O.integrate(o, q0, cfg.dt, 1, cfg.scheme)) < RTOL_STEP
+    q100 = m.step(sg.BaroclinicQGState(q=cuda(q0)), cfg.dt, 100, cfg.scheme).q
+    r100 = O.integrate(o, q0, cfg.dt, 100, cfg.scheme)
+    assert rel(q100[:, 1:-1, 1:-1], r100[:, 1:-1, 1:-1]) < 1e-4
+
+
+def test_config2_baroclinic3_128_ssprk3():
+    # 3-layer 128^2, SSP-RK3 dt = 1200 s: single-step RHS and 10-step state
+    cfg = tc.C2
+    m, o = _config_pair(cfg)
+    q0 = tc.initial_pv(cfg, seed=0)
+    dq = m.vector_field(0.0, sg.BaroclinicQGState(q=cuda(q0))).q
+    assert rel(dq, O.vector_field(o, q0)) < RTOL_RHS
+    q10 = m.step(sg.BaroclinicQGState(q=cuda(q0)), cfg.dt, 10, cfg.scheme).q
+    r10 = O.integrate(o, q0, cfg.dt, 10, cfg.scheme)
+    assert rel(q10[:, 1:-1, 1:-1], r10[:, 1:-1, 1:-1]) < RTOL_STEP
+
+
+def test_integrate_api_and_saveat():
+    m, o = pair(16, 16, 2, nu=50.0, tau=1e-10, L=(1e6, 1e6))
+    z = torch.zeros((2, 18, 18), device="cuda")
+    sol = m.integrate(sg.BaroclinicQGState(q=z), 0.0, 3600.0, 100.0, solver=sg.SSPRK3(),
+                      saveat=sg.SaveAt(ts=[1200.0, 3600.0]))
+    assert sol.ys.q.shape == (2, 2, 18, 18)
+    ref = O.integrate(o, np.zeros((2, 18, 18)), 100.0, 36, "ssprk3")
+    assert rel(sol.ys.q[-1], ref) < RTOL_STEP
+    assert float(sol.ys.q[-1][0, 2:-2, 2:-2].abs().max()) > 1e-10  # wind develops flow
+
+
+def test_integrate_tsit5_default():
+    m, o = pair(16, 16, 2, nu=50.0, tau=1e-10, L=(1e6, 1e6))
+    q = field((2, 18, 18), 8)
+    sol = m.integrate(sg.BaroclinicQGState(q=cuda(q)), 0.0, 1000.0, 100.0)
+    assert rel(sol.ys.q[0], O.integrate(o, q, 100.0, 10, "tsit5")) < RTOL_STEP
+
+
+def test_diagnose():
+    m, o = pair(20, 24, 3)
+    q = field((3, 26, 22), 9, ring=False)
+    d = m.diagnose(sg.BaroclinicQGState(q=cuda(q)))
+    r = O.diagnose(o, q)
+    np.testing.assert_allclose(d.kinetic_energy.cpu().numpy(), r["kinetic_energy"], rtol=1e-5)
+    np.testing.assert_allclose(d.enstrophy.cpu().numpy(), r["enstrophy"], rtol=1e-5)
+    assert rel(d.u, r["u"]) < 1e-5 and rel(d.v, r["v"]) < 1e-5
+
+
+def test_nonfinite_flag():
+    m, _ = pair(16, 16, 2, nu=50.0)
+    q = torch.zeros((2, 18, 18), device="cuda")
+    q[0, 5, 5] = float("nan")
+    plan = m.plan()
+    assert plan.status() == 0
+    m.vector_field(0.0, sg.BaroclinicQGState(q=q))
+    assert plan.status() == sg.qg._lib.K["QG_ERR_NONFINITE"]
+    assert plan.status() == 0  # cleared
+
+
+def test_modes_match_plan():
+    m, o = pair(8, 8, 3)
+    lam, Cl2m, Cm2l = m.plan().member_modes(0)
+    np.testing.assert_allclose(lam, o.helmholtz_lambdas, rtol=1e-12)
+    np.testing.assert_allclose(Cm2l @ Cl2m, np.eye(3), atol=1e-12)
+
+
+def test_plan_computes_modes_itself():
+    # a plan built from H, g' alone (C callers) agrees with the host transform
+    H, g = (400.0, 1100.0, 2600.0), (9.81, 0.025, 0.0125)
+    for eigs in ("consistent", "reference"):
+        spec = sg.MemberSpec(10, 10, 1e6, 1e6, 9.375e-5, 1.754e-11, H, g, eigs=eigs)
+        plan = sg.Plan([spec])
+        lam, Cl2m, Cm2l = plan.member_modes(0)
+        om = O.vertical_modes(H, g, 9.375e-5, eigs)
+        np.testing.assert_allclose(lam, 9.375e-5**2 * om.eigenvalues, rtol=1e-10)
+        x = np.diag([1.0, 2.0, 3.0])
+        np.testing.assert_allclose(Cm2l @ x @ Cl2m, om.Cm2l @ x @ om.Cl2m, rtol=1e-9, atol=1e-12)
+
+
+def test_wrong_shapes_raise():
+    m, _ = pair(8, 8, 2)
+    with pytest.raises(ValueError):
+        m.vector_field(0.0, sg.BaroclinicQGState(q=torch.zeros((2, 9, 10), device="cuda")))
+    with pytest.raises(TypeError):
+        m.vector_field(0.0, sg.BaroclinicQGState(q=torch.zeros((2, 10, 10))))
