@@ -69,6 +69,9 @@ extern "C" {
 
 /* flags for qg_rhs */
 #define QG_RHS_APPLY_BC 1 /* zero the ghost ring of q first (core/model.py:47-49) */
+/* flags for qg_step */
+#define QG_STEP_APPLY_BC 1 /* zero the ring of the initial state in place (integrate() on a new
+                              state0); without it the call continues an integration */
 
 /* params layout: per member, QG_NPARAMS floats in device memory */
 #define QG_NPARAMS 4
@@ -125,11 +128,13 @@ int qg_invert(qg_plan* plan, const float* q, float* psi, void* stream);
 int qg_rhs(qg_plan* plan, const float* q, float* dq, const float* params, int flags,
            void* stream);
 
-/* Advance q in place by n_steps steps of size dt with the given scheme.  Like
-   SomaxModel.integrate, the ghost ring of q is zeroed first and the BC is applied to every
-   stage input; the returned state's ring is the stepped (not re-zeroed) ring. */
+/* Advance q in place by n_steps steps of size dt with the given scheme.  The BC is applied
+   to every stage input (core/model.py:47-49); with QG_STEP_APPLY_BC the ghost ring of q is
+   zeroed first, as SomaxModel.integrate does to state0 (model.py:74).  The returned state's
+   ring is the stepped (not re-zeroed) ring, so consecutive calls without the flag give the
+   same result as one call over all their steps. */
 int qg_step(qg_plan* plan, float* q, const float* params, double dt, int n_steps, int scheme,
-            void* stream);
+            int flags, void* stream);
 
 /* Kinetic energy and enstrophy per layer: ke, ens each sum(n_layers) floats (device). */
 int qg_diagnose(qg_plan* plan, const float* q, float* ke, float* ens, void* stream);

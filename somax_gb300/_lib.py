@@ -76,7 +76,7 @@ def lib() -> C.CDLL:
         "qg_plan_member_modes": (C.c_int, [vp, C.c_int, vp, vp, vp]),
         "qg_invert": (C.c_int, [vp, vp, vp, vp]),
         "qg_rhs": (C.c_int, [vp, vp, vp, vp, C.c_int, vp]),
-        "qg_step": (C.c_int, [vp, vp, vp, C.c_double, C.c_int, C.c_int, vp]),
+        "qg_step": (C.c_int, [vp, vp, vp, C.c_double, C.c_int, C.c_int, C.c_int, vp]),
         "qg_diagnose": (C.c_int, [vp, vp, vp, vp, vp]),
         "qg_status": (C.c_int, [vp, C.POINTER(C.c_int), vp]),
         "qg_strerror": (C.c_char_p, [C.c_int]),

@@ -601,16 +601,18 @@ int qg_rhs(qg_plan* p, const float* q, float* dq, const float* params, int flags
 }
 
 int qg_step(qg_plan* p, float* q, const float* params, double dt, int n_steps, int scheme,
-            void* stream) {
+            int flags, void* stream) {
     if (!p || !q || !params) return QG_ERR_NULL;
-    if (n_steps < 0) return QG_ERR_ARG;
+    if (n_steps < 0 || (flags & ~QG_STEP_APPLY_BC)) return QG_ERR_ARG;
     Stage st[4];
     if (scheme_stages(scheme, st) == 0) return QG_ERR_ARG;
     if (!(dt == dt)) return QG_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = cudaMemcpyAsync(p->params, params, sizeof(float) * p->n_members * QG_NPARAMS,
                                     cudaMemcpyDeviceToDevice, s);
-    if (!e) e = run_prep(p, q, q, 1, s);  // integrate(): BC on the initial state
+    // stage inputs always read q with a zero ring; the ring itself is zeroed in place only for
+    // a new integration (integrate() applies the BC to state0)
+    if (!e) e = run_prep(p, q, (flags & QG_STEP_APPLY_BC) ? q : nullptr, 1, s);
     if (e) return cuda_err(e);
     if (n_steps == 0) return QG_OK;
     const bool use_graph = p->opts.use_graphs && !p->profiling;

@@ -233,14 +233,17 @@ class Plan:
                              C.c_void_p(params.data_ptr()), flags, _stream_handle(q.device)), "qg_rhs")
         return out
 
-    def step(self, q: torch.Tensor, params: torch.Tensor, dt: float, n_steps: int, scheme: str) -> torch.Tensor:
-        """Advance q in place (integrate() semantics: ring zeroed first, BC on every stage)."""
+    def step(self, q: torch.Tensor, params: torch.Tensor, dt: float, n_steps: int, scheme: str,
+             apply_bc: bool = True) -> torch.Tensor:
+        """Advance q in place: BC on every stage input; ``apply_bc`` zeroes the ring of the
+        initial state first (a new integrate()), otherwise the call continues one."""
         self._check_field(q, "q")
         params = params.detach().to(device=q.device, dtype=torch.float32).contiguous()
         if params.numel() != 4 * len(self.members):
             raise ValueError("params must hold 4 values per member")
         check(self._L.qg_step(self._h, C.c_void_p(q.data_ptr()), C.c_void_p(params.data_ptr()),
-                              float(dt), int(n_steps), SCHEMES[scheme], _stream_handle(q.device)), "qg_step")
+                              float(dt), int(n_steps), SCHEMES[scheme], K["QG_STEP_APPLY_BC"] if apply_bc else 0,
+                              _stream_handle(q.device)), "qg_step")
         return q
 
     def diagnose(self, q: torch.Tensor):
@@ -390,11 +393,14 @@ class _QGBase(SomaxModel):
     def apply_boundary_conditions(self, state):
         return self.state_cls(q=_zero_ring(state.q))
 
-    def step(self, state, dt: float, n_steps: int = 1, solver="ssprk3", out: torch.Tensor | None = None):
+    def step(self, state, dt: float, n_steps: int = 1, solver="ssprk3", out: torch.Tensor | None = None,
+             apply_bc: bool = True):
         """Advance ``n_steps`` constant steps on the GPU; returns a new state.
 
-        A state held in host memory is copied to the current CUDA device, stepped there and
-        copied back (into ``out`` if given; pinned memory makes both copies asynchronous)."""
+        Like ``integrate``, the ring of the initial state is zeroed first (``apply_bc``) and
+        the BC is applied to every stage input.  A state held in host memory is copied to the
+        current CUDA device, stepped there and copied back (into ``out`` if given; pinned
+        memory makes both copies asynchronous)."""
         q_in = state.q
         host = q_in.device.type == "cpu"
         if host:
@@ -406,9 +412,9 @@ class _QGBase(SomaxModel):
             q = self._field(q_in).clone()
         scheme = _solver_name(solver)
         if scheme in ("heun", "ssprk3"):
-            self.plan(q.device).step(q, self._param_vector(q.device), dt, n_steps, scheme)
+            self.plan(q.device).step(q, self._param_vector(q.device), dt, n_steps, scheme, apply_bc)
         else:
-            q = self._host_rk(q, dt, n_steps, scheme)
+            q = self._host_rk(q, dt, n_steps, scheme, apply_bc)
         if host:
             if out is None:
                 out = torch.empty(q.shape, dtype=torch.float32, pin_memory=True)
@@ -416,14 +422,14 @@ class _QGBase(SomaxModel):
             return self.state_cls(q=out)
         return self.state_cls(q=q)
 
-    def _host_rk(self, q, dt, n_steps, scheme):
+    def _host_rk(self, q, dt, n_steps, scheme, apply_bc=True):
         # Tableau schemes not yet fused into qg_step: stage loop over the fused RHS kernel.
         from .tableaus import rk_tableau
 
         plan = self.plan(q.device)
         pv = self._param_vector(q.device)
         a, b = rk_tableau(scheme)
-        y = _zero_ring(q)
+        y = _zero_ring(q) if apply_bc else q
         for _ in range(n_steps):
             ks = []
             for s in range(len(b)):
@@ -462,7 +468,8 @@ class _QGBase(SomaxModel):
             if tgt < done:
                 raise ValueError("saveat.ts must be increasing")
             if tgt > done:
-                q = self.step(self.state_cls(q=q), dt, tgt - done, scheme).q
+                # one continuous integration: only the first chunk starts from a BC'd state
+                q = self.step(self.state_cls(q=q), dt, tgt - done, scheme, apply_bc=False).q
                 done = tgt
             ys.append(q.clone())
         ts = torch.tensor([t0 + k * dt for k in targets], dtype=torch.float64)

@@ -60,6 +60,6 @@ def test_plan_create_validates_before_cuda(L):
 def test_entry_points_reject_null(L):
     assert L.qg_invert(None, None, None, None) == _lib.K["QG_ERR_NULL"]
     assert L.qg_rhs(None, None, None, None, 0, None) == _lib.K["QG_ERR_NULL"]
-    assert L.qg_step(None, None, None, 1.0, 1, 2, None) == _lib.K["QG_ERR_NULL"]
+    assert L.qg_step(None, None, None, 1.0, 1, 2, 0, None) == _lib.K["QG_ERR_NULL"]
     assert L.qg_status(None, None, None) == _lib.K["QG_ERR_NULL"]
     assert L.qg_plan_state_size(None) == -1
