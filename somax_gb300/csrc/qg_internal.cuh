@@ -116,6 +116,11 @@ struct GemmArgs {
 cudaError_t launch_gemm_simt(const GemmArgs& g, int ntiles, cudaStream_t s);
 cudaError_t launch_gemm_tc(const GemmArgs& g, int ntiles, int precision, cudaStream_t s);
 
+// host helpers shared by the plan and the plan-free entry points
+int validate_member(const qg_member_desc& d);
+void member_constants(const qg_member_desc& d, MemberDev& M, double* Cl2m, double* Cm2l, double* lam);
+int round_up(int v, int m);
+
 constexpr int kStencilTX = 32;
 constexpr int kStencilTY = 16;
 constexpr int kSimtBM = 64;

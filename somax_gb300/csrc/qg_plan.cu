@@ -76,6 +76,10 @@ void jacobi_eigh(int n, const double* Ain, double* w, double* V) {
     std::memcpy(V, Vs, sizeof(double) * n * n);
 }
 
+}  // namespace
+
+namespace qg {
+
 // Layered QG coupling A = diag(1/H) M with M symmetric tridiagonal (the stretching
 // operator of finitevolx build_coupling_matrix, transforms.py:192).  Its right
 // eigenvectors are R = diag(H^-1/2) V with V the eigenvectors of the symmetric
@@ -115,6 +119,63 @@ void vertical_modes(const qg_member_desc& d, double* Cl2m, double* Cm2l, double*
 }
 
 int round_up(int v, int m) { return (v + m - 1) / m * m; }
+
+int validate_member(const qg_member_desc& d) {
+    if (d.nx < 1 || d.ny < 1 || d.n_layers < 1 || d.n_layers > QG_MAX_LAYERS) return QG_ERR_SHAPE;
+    if ((int64_t)(d.nx + 2) * (d.ny + 2) > (1LL << 28)) return QG_ERR_SHAPE;
+    if (d.barotropic && d.n_layers != 1) return QG_ERR_SHAPE;
+    if (!(d.Lx > 0) || !(d.Ly > 0)) return QG_ERR_ARG;
+    if (d.wind_profile != QG_WIND_DOUBLEGYRE && d.wind_profile != QG_WIND_SINGLE) return QG_ERR_ARG;
+    if (d.eigs_mode != QG_EIGS_CONSISTENT && d.eigs_mode != QG_EIGS_REFERENCE) return QG_ERR_ARG;
+    if (!d.has_modes && !d.barotropic)
+        for (int l = 0; l < d.n_layers; ++l)
+            if (!(d.H[l] > 0) || !(d.g_prime[l] > 0)) return QG_ERR_ARG;
+    return QG_OK;
+}
+
+// Geometry, finite-difference constants and modal matrices of one member (the device
+// pointers and offsets are left zero for the caller to fill).
+void member_constants(const qg_member_desc& d, MemberDev& M, double* Cl2m, double* Cm2l, double* lam) {
+    std::memset(&M, 0, sizeof(M));
+    M.nl = d.n_layers;
+    M.Ny = d.ny + 2;
+    M.Nx = d.nx + 2;
+    M.Px = round_up(M.Nx, 32);
+    M.Py = round_up(M.Ny, 32);
+    M.barotropic = d.barotropic;
+    const double dx = d.Lx / d.nx, dy = d.Ly / d.ny;
+    M.dx = (float)dx;
+    M.dy = (float)dy;
+    M.inv_dx2 = (float)(1.0 / (dx * dx));
+    M.inv_dy2 = (float)(1.0 / (dy * dy));
+    M.inv_12dxdy = (float)(1.0 / (12.0 * dx * dy));
+    M.beta_12dx = (float)(d.beta / (12.0 * dx));
+    M.invH0 = d.barotropic ? 1.f : (float)(1.0 / d.H[0]);
+    const int n = d.n_layers;
+    if (d.barotropic) {
+        Cl2m[0] = Cm2l[0] = 1.0;
+        lam[0] = 0.0;
+    } else if (d.has_modes) {
+        for (int k = 0; k < n * n; ++k) {
+            Cl2m[k] = d.Cl2m[k];
+            Cm2l[k] = d.Cm2l[k];
+        }
+        for (int k = 0; k < n; ++k) lam[k] = d.lambdas[k];
+    } else {
+        vertical_modes(d, Cl2m, Cm2l, lam);
+    }
+    for (int r = 0; r < n; ++r) {
+        for (int c = 0; c < n; ++c) {
+            M.Cl2m[r * kMaxLayers + c] = (float)Cl2m[r * n + c];
+            M.Cm2l[r * kMaxLayers + c] = (float)Cm2l[r * n + c];
+        }
+        M.lam[r] = (float)lam[r];
+    }
+}
+
+}  // namespace qg
+
+namespace {
 
 // Orthonormal DST-I matrix (n x n, pitch ld): sqrt(2/(n+1)) sin(pi (i+1)(j+1)/(n+1)),
 // the argument reduced modulo 2(n+1) for accuracy.
@@ -357,16 +418,8 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
     if (o.dst_precision < QG_DST_FP32 || o.dst_precision > QG_DST_BF16X3) return QG_ERR_ARG;
     if (o.refine_sweeps < 0 || o.refine_sweeps > 1) return QG_ERR_ARG;
     for (int i = 0; i < n_members; ++i) {
-        const qg_member_desc& d = members[i];
-        if (d.nx < 1 || d.ny < 1 || d.n_layers < 1 || d.n_layers > QG_MAX_LAYERS) return QG_ERR_SHAPE;
-        if ((int64_t)(d.nx + 2) * (d.ny + 2) > (1LL << 28)) return QG_ERR_SHAPE;
-        if (d.barotropic && d.n_layers != 1) return QG_ERR_SHAPE;
-        if (!(d.Lx > 0) || !(d.Ly > 0)) return QG_ERR_ARG;
-        if (d.wind_profile != QG_WIND_DOUBLEGYRE && d.wind_profile != QG_WIND_SINGLE) return QG_ERR_ARG;
-        if (d.eigs_mode != QG_EIGS_CONSISTENT && d.eigs_mode != QG_EIGS_REFERENCE) return QG_ERR_ARG;
-        if (!d.has_modes && !d.barotropic)
-            for (int l = 0; l < d.n_layers; ++l)
-                if (!(d.H[l] > 0) || !(d.g_prime[l] > 0)) return QG_ERR_ARG;
+        const int v = validate_member(members[i]);
+        if (v != QG_OK) return v;
     }
     qg_plan* p = new (std::nothrow) qg_plan();
     if (!p) return QG_ERR_CUDA;
@@ -394,42 +447,10 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
     for (int i = 0; i < n_members; ++i) {
         const qg_member_desc& d = members[i];
         MemberDev& M = p->mh[i];
-        std::memset(&M, 0, sizeof(M));
-        M.nl = d.n_layers;
-        M.Ny = d.ny + 2;
-        M.Nx = d.nx + 2;
-        M.Px = round_up(M.Nx, 32);
-        M.Py = round_up(M.Ny, 32);
-        M.barotropic = d.barotropic;
-        const double dx = d.Lx / d.nx, dy = d.Ly / d.ny;
-        M.dx = (float)dx;
-        M.dy = (float)dy;
-        M.inv_dx2 = (float)(1.0 / (dx * dx));
-        M.inv_dy2 = (float)(1.0 / (dy * dy));
-        M.inv_12dxdy = (float)(1.0 / (12.0 * dx * dy));
-        M.beta_12dx = (float)(d.beta / (12.0 * dx));
-        M.invH0 = d.barotropic ? 1.f : (float)(1.0 / d.H[0]);
         double Cl2m[64], Cm2l[64], lam[8];
+        member_constants(d, M, Cl2m, Cm2l, lam);
         const int n = d.n_layers;
-        if (d.barotropic) {
-            Cl2m[0] = Cm2l[0] = 1.0;
-            lam[0] = 0.0;
-        } else if (d.has_modes) {
-            for (int k = 0; k < n * n; ++k) {
-                Cl2m[k] = d.Cl2m[k];
-                Cm2l[k] = d.Cm2l[k];
-            }
-            for (int k = 0; k < n; ++k) lam[k] = d.lambdas[k];
-        } else {
-            vertical_modes(d, Cl2m, Cm2l, lam);
-        }
-        for (int r = 0; r < n; ++r) {
-            for (int c = 0; c < n; ++c) {
-                M.Cl2m[r * kMaxLayers + c] = (float)Cl2m[r * n + c];
-                M.Cm2l[r * kMaxLayers + c] = (float)Cm2l[r * n + c];
-            }
-            M.lam[r] = (float)lam[r];
-        }
+        const double dx = d.Lx / d.nx, dy = d.Ly / d.ny;
         p->desc[i].has_modes = 1;  // remember what the plan uses
         for (int k = 0; k < n * n; ++k) {
             p->desc[i].Cl2m[k] = Cl2m[k];
