@@ -47,6 +47,7 @@ extern "C" {
 #define QG_ERR_TIMEOUT 5      /* a bounded device-side wait gave up */
 #define QG_ERR_ARG 6          /* bad enum / option value */
 #define QG_ERR_UNSUPPORTED 7  /* option not available on this device */
+#define QG_ERR_TOO_LARGE 8    /* member exceeds the fixed scratch of qg_invert_static */
 
 /* dst_precision: arithmetic of the DST-I GEMMs of the PV inversion */
 #define QG_DST_FP32 0    /* plain FP32 on the CUDA cores (the baseline path) */
@@ -138,6 +139,17 @@ int qg_step(qg_plan* plan, float* q, const float* params, double dt, int n_steps
 
 /* Kinetic energy and enstrophy per layer: ke, ens each sum(n_layers) floats (device). */
 int qg_diagnose(qg_plan* plan, const float* q, float* ke, float* ens, void* stream);
+
+/* qg_invert for one member without a plan and without allocating device memory.
+   No counterpart in the reference: this is for callers that may not allocate at the time
+   they invert (code inside a framework's compiled program or memory pool, loops with an
+   allocation ban).  Scratch is one fixed file-scope device array of about 14.9 MB that
+   every GPU loading the library holds until exit.  Limits: nx, ny <= 512 and n_layers *
+   (ny+2) * round_up(nx+2, 32) <= 2^20 (and the same with x and y swapped); larger members
+   return QG_ERR_TOO_LARGE.  All calls on a device share that scratch, so calls that
+   overlap on the GPU race; serialise them.  The first call on each device looks up the
+   scratch address (cudaGetSymbolAddress); make it before any stream capture. */
+int qg_invert_static(const qg_member_desc* member, const float* q, float* psi, void* stream);
 
 /* Device-side status: synchronises the stream, returns QG_OK or QG_ERR_NONFINITE /
    QG_ERR_TIMEOUT, writes the raw flag word to *flags (may be NULL) and clears it. */

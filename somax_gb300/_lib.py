@@ -75,6 +75,7 @@ def lib() -> C.CDLL:
         "qg_plan_member_offset": (i64, [vp, C.c_int]),
         "qg_plan_member_modes": (C.c_int, [vp, C.c_int, vp, vp, vp]),
         "qg_invert": (C.c_int, [vp, vp, vp, vp]),
+        "qg_invert_static": (C.c_int, [C.POINTER(MemberDesc), vp, vp, vp]),
         "qg_rhs": (C.c_int, [vp, vp, vp, vp, C.c_int, vp]),
         "qg_step": (C.c_int, [vp, vp, vp, C.c_double, C.c_int, C.c_int, C.c_int, vp]),
         "qg_diagnose": (C.c_int, [vp, vp, vp, vp, vp]),

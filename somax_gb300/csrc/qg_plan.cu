@@ -201,7 +201,8 @@ void dst_eigs(int n, double d, std::vector<float>& out) {
 }
 
 const char* kErrStr[] = {"ok", "null pointer", "bad shape", "CUDA error", "non-finite value",
-                         "device wait timed out", "bad argument", "unsupported"};
+                         "device wait timed out", "bad argument", "unsupported",
+                         "member exceeds the static scratch limit"};
 
 }  // namespace
 
