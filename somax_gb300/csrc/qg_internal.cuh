@@ -111,8 +111,13 @@ struct GemmArgs {
     const void* A;   // plane base (internal packing)
     void* C;         // plane base
     int a_fmt, c_fmt;
-    int accumulate;  // C += result (refinement of psi_hat)
+    int accumulate;       // C += result (refinement of psi_hat)
+    const void* tc_maps;  // tensor-core path: TMA descriptors, 4 per member (one per pass)
+    int* flags;           // device status word (bit 1: a bounded wait timed out)
 };
+constexpr int kTcMapsBytes = 512;  // 4 CUtensorMap per (member, pass)
+cudaError_t gemm_tc_encode(const MemberDev& M, int pass, const void* a_plane, int64_t a_plane_elems, int prec,
+                           void* out);
 cudaError_t launch_gemm_simt(const GemmArgs& g, int ntiles, cudaStream_t s);
 cudaError_t launch_gemm_tc(const GemmArgs& g, int ntiles, int precision, cudaStream_t s);
 

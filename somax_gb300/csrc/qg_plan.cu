@@ -236,6 +236,7 @@ struct qg_plan {
     int* flags = nullptr;
     double* diag_acc = nullptr;
     int op_fmt = FMT_F32;
+    void* tc_maps = nullptr;  // TMA descriptors of the tensor-core GEMMs
     // graphs
     cudaStream_t cap = nullptr;
     StepGraph graph;
@@ -296,6 +297,8 @@ GemmArgs gemm_args(qg_plan* p, int pass, const void* A, void* C, int a_fmt, int 
     g.a_fmt = a_fmt;
     g.c_fmt = c_fmt;
     g.accumulate = acc;
+    g.tc_maps = p->tc_maps;
+    g.flags = p->flags;
     return g;
 }
 
@@ -546,6 +549,17 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
             !(e = dalloc(p, &p->flags, 16)))
             e = dalloc(p, &p->diag_acc, (size_t)2 * p->total_layers * sizeof(double));
         if (!e && o.refine_sweeps > 0) e = dalloc(p, &p->XQ, xb);
+    }
+    if (e == cudaSuccess && tc) {
+        // one set of TMA descriptors per (member, pass); the planes never move
+        std::vector<uint8_t> maps((size_t)n_members * 4 * kTcMapsBytes);
+        const void* in_plane[4] = {p->XA, p->YA, p->YB, p->XB};
+        const int64_t in_elems[4] = {p->xplane, p->yplane, p->yplane, p->xplane};
+        for (int i = 0; i < n_members && !e; ++i)
+            for (int pass = 0; pass < 4 && !e; ++pass)
+                e = gemm_tc_encode(p->mh[i], pass, in_plane[pass], in_elems[pass], o.dst_precision,
+                                   maps.data() + ((size_t)i * 4 + pass) * kTcMapsBytes);
+        if (!e) e = upload(p, (uint8_t**)&p->tc_maps, maps);
     }
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();

@@ -242,3 +242,41 @@ def test_wrong_shapes_raise():
         m.vector_field(0.0, sg.BaroclinicQGState(q=torch.zeros((2, 9, 10), device="cuda")))
     with pytest.raises(TypeError):
         m.vector_field(0.0, sg.BaroclinicQGState(q=torch.zeros((2, 10, 10))))
+
+
+# ---- tensor-core DST GEMMs ---------------------------------------------------------------
+# Measured bounds (relative L2 vs float64): BF16x3 inverts to ~1e-5 (1e-7 after one FP32
+# refinement sweep).  TF32 inverts to ~3e-3: its rounded DST matrix perturbs the operator
+# and the Helmholtz condition number amplifies that, so refinement only recovers ~1e-5 on
+# small grids; TF32 meets the 10-step q bound only with refinement and at <= 128^2.
+TC_INV = {("bf16x3", 0): 3e-5, ("bf16x3", 1): 1e-6, ("tf32", 0): 6e-3, ("tf32", 1): 2e-4}
+TC_Q10 = {("bf16x3", 0): RTOL_STEP, ("bf16x3", 1): RTOL_STEP, ("tf32", 1): RTOL_STEP}
+
+
+@pytest.mark.parametrize("precision,refine", sorted(TC_INV))
+@pytest.mark.parametrize("nx,ny,nl", [(3, 5, 1), (17, 13, 3), (40, 33, 8), (128, 128, 3), (200, 130, 2)])
+def test_invert_tensor_cores(precision, refine, nx, ny, nl):
+    m, o = pair(nx, ny, nl, precision=precision, refine=refine, L=(5.12e6, 4e6))
+    q = field((nl, ny + 2, nx + 2), 11, ring=False)
+    psi = m._invert_pv(cuda(q))
+    assert rel(psi, O.invert_pv(o, q)) < TC_INV[(precision, refine)]
+    assert m.plan().status() == 0
+
+
+@pytest.mark.parametrize("precision,refine", sorted(TC_Q10))
+def test_config2_tensor_cores_10_steps(precision, refine):
+    cfg = tc.C2
+    kw = cfg.model_kwargs()
+    m = sg.BaroclinicQG.create(**kw, precision=precision, refine=refine)
+    _, o = _config_pair(cfg)
+    q0 = tc.initial_pv(cfg, seed=0)
+    q10 = m.step(sg.BaroclinicQGState(q=cuda(q0)), cfg.dt, 10, cfg.scheme).q
+    r10 = O.integrate(o, q0, cfg.dt, 10, cfg.scheme)
+    assert rel(q10[:, 1:-1, 1:-1], r10[:, 1:-1, 1:-1]) < TC_Q10[(precision, refine)]
+
+
+def test_tensor_core_rhs_barotropic():
+    m, o = pair(64, 64, 1, barotropic=True, nu=80.0, kappa=1e-7, tau=1e-10, L=(1e6, 1e6), precision="bf16x3")
+    q = field((66, 66), 12)
+    dq = m.vector_field(0.0, sg.BarotropicQGState(q=cuda(q))).q
+    assert rel(dq, O.vector_field(o, q)) < 1e-4
