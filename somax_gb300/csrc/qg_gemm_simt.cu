@@ -1,6 +1,7 @@
 // Plain FP32 DST-I GEMMs on the CUDA cores: the baseline ("plain FP32 single-member path")
 // against which the tensor-core inversion is measured, and the fallback-free reference for
 // the tcgen05 kernels' numerics.  C = A * S with S the symmetric orthonormal DST-I matrix.
+#include "qg_device.cuh"
 #include "qg_internal.cuh"
 
 namespace qg {
@@ -40,6 +41,8 @@ __global__ void __launch_bounds__(NT) k_gemm_simt(GemmArgs ga) {
     const GemmTile t = ga.tiles[blockIdx.x];
     const MemberDev& M = ga.members[t.member];
     const PassGeom g = pass_geom(M, PASS, ga.A, ga.C);
+    pdl_wait();
+    pdl_launch_dependents();
     const int nl = M.nl;
     const int Mtot = nl * g.Mb;
     const int m0 = t.mt * BM, n0 = t.nt * BN;
@@ -114,15 +117,14 @@ __global__ void __launch_bounds__(NT) k_gemm_simt(GemmArgs ga) {
 
 }  // namespace
 
-cudaError_t launch_gemm_simt(const GemmArgs& g, int ntiles, cudaStream_t s) {
+cudaError_t launch_gemm_simt(const GemmArgs& g, int ntiles, cudaStream_t s, bool pdl) {
     switch (g.pass) {
-        case G1_FWD_X: k_gemm_simt<G1_FWD_X><<<ntiles, NT, 0, s>>>(g); break;
-        case G2_FWD_Y: k_gemm_simt<G2_FWD_Y><<<ntiles, NT, 0, s>>>(g); break;
-        case G3_INV_Y: k_gemm_simt<G3_INV_Y><<<ntiles, NT, 0, s>>>(g); break;
-        case G4_INV_X: k_gemm_simt<G4_INV_X><<<ntiles, NT, 0, s>>>(g); break;
+        case G1_FWD_X: return launch_k(k_gemm_simt<G1_FWD_X>, ntiles, NT, 0, s, pdl, g);
+        case G2_FWD_Y: return launch_k(k_gemm_simt<G2_FWD_Y>, ntiles, NT, 0, s, pdl, g);
+        case G3_INV_Y: return launch_k(k_gemm_simt<G3_INV_Y>, ntiles, NT, 0, s, pdl, g);
+        case G4_INV_X: return launch_k(k_gemm_simt<G4_INV_X>, ntiles, NT, 0, s, pdl, g);
         default: return cudaErrorInvalidValue;
     }
-    return cudaGetLastError();
 }
 
 }  // namespace qg

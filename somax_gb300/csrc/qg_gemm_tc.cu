@@ -19,6 +19,7 @@
 
 #include <cstring>
 
+#include "qg_device.cuh"
 #include "qg_internal.cuh"
 
 namespace qg {
@@ -28,7 +29,6 @@ namespace {
 constexpr int BM = 128;
 constexpr int BN = 128;
 constexpr int NTHREADS = 192;
-constexpr long long kTimeoutCycles = 4000000000LL;  // ~2 s at 2 GHz
 
 struct TcMaps {
     CUtensorMap a[2];  // A hi (or f32), A lo
@@ -66,50 +66,7 @@ __host__ __device__ constexpr int stage_bytes() { return Cfg<PREC>::NA * tile_a_
 template <int PREC>
 __host__ __device__ constexpr int smem_bytes() { return Cfg<PREC>::STAGES * stage_bytes<PREC>() + 1024; }
 
-// ---- PTX wrappers --------------------------------------------------------------------
-__device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t n) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(b)), "r"(n) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(b)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try(uint64_t* b, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(su32(b)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// Bounded wait: false after ~2 s or when another role already gave up.
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile int* abort) {
-    const long long t0 = clock64();
-    while (!mbar_try(b, parity)) {
-        if (*abort) return false;
-        if (clock64() - t0 > kTimeoutCycles) {
-            *abort = 1;
-            return false;
-        }
-    }
-    return true;
-}
-// Bounded wait used while draining after an abort: ignores the abort flag.
-__device__ __forceinline__ bool mbar_drain(uint64_t* b, uint32_t parity) {
-    const long long t0 = clock64();
-    while (!mbar_try(b, parity))
-        if (clock64() - t0 > kTimeoutCycles) return false;
-    return true;
-}
-__device__ __forceinline__ void tma_load(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-            su32(dst)),
-        "l"((uint64_t)map), "r"(x), "r"(y), "r"(su32(bar))
-        : "memory");
-}
+// ---- tcgen05 wrappers ----------------------------------------------------------------
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
@@ -203,11 +160,17 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_gemm_tc(GemmArgs ga, const TcMa
                      "r"(BN));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
+    if (threadIdx.x == 32) {
+        for (int a = 0; a < C::NA; ++a) tma_prefetch_desc(&tm->a[a]);
+        for (int b = 0; b < C::NB; ++b) tma_prefetch_desc(&tm->b[b]);
+    }
     fence_before();
     __syncthreads();
     fence_after();
     const uint32_t tmem = tmem_slot;
     volatile int* abort = &abort_flag;
+    pdl_wait();
+    pdl_launch_dependents();
 
     if (warp == 0) {
         if (lane == 0) {
@@ -218,9 +181,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_gemm_tc(GemmArgs ga, const TcMa
                 uint8_t* st = smem + s * stage_bytes<PREC>();
                 mbar_expect_tx(&full_bar[s], stage_bytes<PREC>());
                 const int kx = kb * C::BK;
-                for (int a = 0; a < C::NA; ++a) tma_load(st + a * tile_a_bytes<PREC>(), &tm->a[a], &full_bar[s], kx, m0);
+                for (int a = 0; a < C::NA; ++a) tma_load_2d(st + a * tile_a_bytes<PREC>(), &tm->a[a], &full_bar[s], kx, m0);
                 for (int b = 0; b < C::NB; ++b)
-                    tma_load(st + C::NA * tile_a_bytes<PREC>() + b * tile_b_bytes<PREC>(), &tm->b[b], &full_bar[s], kx, n0);
+                    tma_load_2d(st + C::NA * tile_a_bytes<PREC>() + b * tile_b_bytes<PREC>(), &tm->b[b], &full_bar[s], kx, n0);
                 n_issued = kb + 1;
             }
         }
@@ -327,8 +290,6 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_gemm_tc(GemmArgs ga, const TcMa
     if (threadIdx.x == 0 && abort_flag && ga.flags) atomicOr(ga.flags, 2);
 }
 
-PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
-
 template <int PREC>
 cudaError_t set_attrs() {
     cudaError_t e = cudaSuccess;
@@ -341,34 +302,27 @@ cudaError_t set_attrs() {
 }
 
 template <int PREC>
-cudaError_t launch(const GemmArgs& g, int ntiles, cudaStream_t s) {
+cudaError_t launch(const GemmArgs& g, int ntiles, cudaStream_t s, bool pdl) {
     const TcMaps* maps = static_cast<const TcMaps*>(g.tc_maps);
     const int sm = smem_bytes<PREC>();
     switch (g.pass) {
-        case G1_FWD_X: k_gemm_tc<PREC, G1_FWD_X><<<ntiles, NTHREADS, sm, s>>>(g, maps); break;
-        case G2_FWD_Y: k_gemm_tc<PREC, G2_FWD_Y><<<ntiles, NTHREADS, sm, s>>>(g, maps); break;
-        case G3_INV_Y: k_gemm_tc<PREC, G3_INV_Y><<<ntiles, NTHREADS, sm, s>>>(g, maps); break;
-        case G4_INV_X: k_gemm_tc<PREC, G4_INV_X><<<ntiles, NTHREADS, sm, s>>>(g, maps); break;
+        case G1_FWD_X: return launch_k(k_gemm_tc<PREC, G1_FWD_X>, ntiles, NTHREADS, sm, s, pdl, g, maps);
+        case G2_FWD_Y: return launch_k(k_gemm_tc<PREC, G2_FWD_Y>, ntiles, NTHREADS, sm, s, pdl, g, maps);
+        case G3_INV_Y: return launch_k(k_gemm_tc<PREC, G3_INV_Y>, ntiles, NTHREADS, sm, s, pdl, g, maps);
+        case G4_INV_X: return launch_k(k_gemm_tc<PREC, G4_INV_X>, ntiles, NTHREADS, sm, s, pdl, g, maps);
         default: return cudaErrorInvalidValue;
     }
-    return cudaGetLastError();
 }
 
 // 2-D tensor map over `rows` rows of `cols` valid elements with a row pitch of `pitch`
-// elements; columns >= cols and rows >= rows read as zero.
+// elements; columns >= cols and rows >= rows read as zero.  128-byte rows, 128-byte swizzle.
 cudaError_t encode(CUtensorMap* m, const void* base, int cols, int rows, int pitch, int prec, int box_rows) {
     const bool bf = prec == QG_DST_BF16X3;
     const int es = bf ? 2 : 4;
-    if (((uintptr_t)base & 15) || ((int64_t)pitch * es) % 16) return cudaErrorInvalidValue;
-    cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)pitch * es};
-    cuuint32_t box[2] = {(cuuint32_t)(128 / es), (cuuint32_t)box_rows};
-    cuuint32_t estr[2] = {1, 1};
-    CUresult r = g_encode(m, bf ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
-                          const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                          CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+    const uint64_t dims[2] = {(uint64_t)cols, (uint64_t)rows};
+    const uint64_t strides[1] = {(uint64_t)pitch * es};
+    const uint32_t box[2] = {(uint32_t)(128 / es), (uint32_t)box_rows};
+    return tmap_encode(m, bf ? 1 : 0, 2, base, dims, strides, box, 1);
 }
 
 }  // namespace
@@ -380,13 +334,6 @@ cudaError_t gemm_tc_init() {
     if (!e) e = cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
     if (e) return e;
     if (major != 10 || minor != 3) return cudaErrorNotSupported;  // built for sm_103a only
-    if (!g_encode) {
-        void* fn = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
-        if (e || q != cudaDriverEntryPointSuccess || !fn) return cudaErrorNotSupported;
-        g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
-    }
     if (!e) e = set_attrs<QG_DST_TF32>();
     if (!e) e = set_attrs<QG_DST_BF16X3>();
     return e;
@@ -416,10 +363,10 @@ cudaError_t gemm_tc_encode(const MemberDev& M, int pass, const void* a_plane, in
     return e;
 }
 
-cudaError_t launch_gemm_tc(const GemmArgs& g, int ntiles, int precision, cudaStream_t s) {
+cudaError_t launch_gemm_tc(const GemmArgs& g, int ntiles, int precision, cudaStream_t s, bool pdl) {
     if (!g.tc_maps) return cudaErrorInvalidValue;
-    if (precision == QG_DST_TF32) return launch<QG_DST_TF32>(g, ntiles, s);
-    if (precision == QG_DST_BF16X3) return launch<QG_DST_BF16X3>(g, ntiles, s);
+    if (precision == QG_DST_TF32) return launch<QG_DST_TF32>(g, ntiles, s, pdl);
+    if (precision == QG_DST_BF16X3) return launch<QG_DST_BF16X3>(g, ntiles, s, pdl);
     return cudaErrorInvalidValue;
 }
 

@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <utility>
+
 #include "../../include/qgcore.h"
 
 namespace qg {
@@ -63,20 +65,56 @@ enum PlaneFmt : int {
     FMT_BF16X2 = 1,  // bf16 hi plane followed by bf16 lo plane (same byte size as f32)
 };
 
+// Programmatic-dependent-launch-capable launch: with `pdl` the kernel may start while its
+// predecessor in the stream finishes; every kernel calls griddepcontrol.wait before it
+// touches memory a predecessor writes.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_k(void (*kernel)(KArgs...), int grid, int block, size_t smem, cudaStream_t s, bool pdl,
+                     Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
+struct PrepArgs {
+    const MemberDev* members;
+    const StencilTile* tiles;
+    const float* q;        // caller packing
+    float* copy;           // internal x-row plane to receive q (may be null)
+    int zero_ring_copy;    // zero the ring in the copy
+    int bc_operand;        // operand built from q with a zero ring
+    void* xa;              // Cl2m q in the GEMM operand format (may be null)
+    int xa_fmt;
+    float* xq;             // FP32 Cl2m q for the refinement residual (may be null)
+    int64_t xplane;
+};
+
+// TMA descriptors of one member for the stencil: the three stage planes and psi_hat,
+// 3-D boxes (x, y, layer) over the padded x-row planes.
+constexpr int kStencilMapsBytes = 4 * 128;
+cudaError_t stencil_encode_maps(const MemberDev& M, const float* const planes[4], void* out);
+
 struct StencilArgs {
     const MemberDev* members;
     const StencilTile* tiles;
-    const float* q;        // stage input (layer space), caller packing or internal packing
-    int q_internal;        // 1: q uses the internal x-row packing (off_x, pitch Px)
-    const float* psi_hat;  // modal psi, x-row planes
+    const void* maps;      // StencilMaps per member
+    int q_sel;             // which stage plane holds the input q (0..2)
     const float* params;   // n_members * QG_NPARAMS
     int apply_bc;          // zero the ring of q on read
+    int64_t xplane;
     // rhs mode
     float* dq;             // caller packing; null in step mode
-    // step mode: y_next = a * y0 + b * (y_s + dt * dq)
-    const float* y0;       // caller packing (state); read pointwise
-    float* y_next;         // destination (caller packing if final, internal otherwise)
-    int y_next_internal;
+    // step mode: y_next = a * y0 + b * (y_s + dt * dq), internal planes
+    const float* y0;
+    float* y_next;
     int final_stage;
     float a, b, dt;
     void* xa;              // next-stage GEMM operand (modal q, x-row planes); may be null
@@ -86,14 +124,13 @@ struct StencilArgs {
 };
 
 // launchers (return cudaError_t of the launch)
-cudaError_t launch_prep(const MemberDev* members, const StencilTile* tiles, int ntiles,
-                        const float* q, float* q_bc_inplace, int apply_bc, void* xa, int xa_fmt,
-                        float* xq, int64_t xplane, cudaStream_t s);
-cudaError_t launch_stencil(const StencilArgs& a, int ntiles, int max_nl, int64_t xplane,
-                           cudaStream_t s);
+cudaError_t launch_prep(const PrepArgs& a, int ntiles, cudaStream_t s, bool pdl);
+cudaError_t launch_unpack(const MemberDev* members, const StencilTile* tiles, int ntiles, const float* src,
+                          float* q, cudaStream_t s, bool pdl);
+cudaError_t launch_stencil(const StencilArgs& a, int ntiles, int max_nl, cudaStream_t s, bool pdl);
 size_t stencil_smem_bytes(int max_nl);
 cudaError_t launch_mode_to_layer(const MemberDev* members, const StencilTile* tiles, int ntiles,
-                                 const float* psi_hat, float* psi, cudaStream_t s);
+                                 const float* psi_hat, float* psi, cudaStream_t s, bool pdl);
 cudaError_t launch_diag_acc(const MemberDev* members, const StencilTile* tiles, int ntiles,
                             const float* q, const float* psi_hat, double* acc, cudaStream_t s);
 cudaError_t launch_diag_finish(const double* acc, int64_t n_layers, float* ke, float* ens,
@@ -101,7 +138,11 @@ cudaError_t launch_diag_finish(const double* acc, int64_t n_layers, float* ke, f
 void stencil_init();
 cudaError_t launch_residual(const MemberDev* members, const StencilTile* tiles, int ntiles,
                             const float* qm, const float* psi_hat, void* out, int out_fmt,
-                            int64_t xplane, cudaStream_t s);
+                            int64_t xplane, cudaStream_t s, bool pdl);
+
+// host: cuTensorMapEncodeTiled through the driver entry point (no libcuda link needed)
+cudaError_t tmap_encode(void* map, int bf16, int rank, const void* base, const uint64_t* dims,
+                        const uint64_t* strides_bytes, const uint32_t* box, int swizzle128);
 
 struct GemmArgs {
     const MemberDev* members;
@@ -118,15 +159,15 @@ struct GemmArgs {
 constexpr int kTcMapsBytes = 512;  // 4 CUtensorMap per (member, pass)
 cudaError_t gemm_tc_encode(const MemberDev& M, int pass, const void* a_plane, int64_t a_plane_elems, int prec,
                            void* out);
-cudaError_t launch_gemm_simt(const GemmArgs& g, int ntiles, cudaStream_t s);
-cudaError_t launch_gemm_tc(const GemmArgs& g, int ntiles, int precision, cudaStream_t s);
+cudaError_t launch_gemm_simt(const GemmArgs& g, int ntiles, cudaStream_t s, bool pdl);
+cudaError_t launch_gemm_tc(const GemmArgs& g, int ntiles, int precision, cudaStream_t s, bool pdl);
 
 // host helpers shared by the plan and the plan-free entry points
 int validate_member(const qg_member_desc& d);
 void member_constants(const qg_member_desc& d, MemberDev& M, double* Cl2m, double* Cm2l, double* lam);
 int round_up(int v, int m);
 
-constexpr int kStencilTX = 32;
+constexpr int kStencilTX = 64;
 constexpr int kStencilTY = 16;
 constexpr int kSimtBM = 64;
 constexpr int kSimtBN = 64;

@@ -1,7 +1,9 @@
 // Host side of libqgcore: plan construction (FP64 modal matrices, DST-I matrices and
 // eigenvalues, grids of tiles), the C-ABI entry points and their launch sequences, CUDA
 // graph capture of a whole time step, and per-kernel event timing.
+#include <cuda.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <cmath>
@@ -208,7 +210,6 @@ const char* kErrStr[] = {"ok", "null pointer", "bad shape", "CUDA error", "non-f
 
 struct StepGraph {
     cudaGraphExec_t exec = nullptr;
-    const float* q = nullptr;
     double dt = 0.0;
     int scheme = -1;
 };
@@ -228,15 +229,17 @@ struct qg_plan {
     GemmTile* gx_tiles = nullptr;  // passes with A in x-row planes (G1, G4)
     GemmTile* gy_tiles = nullptr;  // passes with A in y-row planes (G2, G3)
     int n_gx = 0, n_gy = 0;
-    // device memory
+    // device memory: x-row planes XA (modal operand), XB (V^T), XC (psi_hat), XQ (FP32 modal
+    // rhs for refinement), S0 (state), S1/S2 (stage inputs); y-row planes YA (T1^T), YB (U)
     std::vector<void*> allocs;
     float *XA = nullptr, *XB = nullptr, *XC = nullptr, *XQ = nullptr, *YA = nullptr, *YB = nullptr;
-    float *S1 = nullptr, *S2 = nullptr;
+    float *S0 = nullptr, *S1 = nullptr, *S2 = nullptr;
     float* params = nullptr;  // plan-owned copy of the params (graph-stable)
     int* flags = nullptr;
     double* diag_acc = nullptr;
     int op_fmt = FMT_F32;
     void* tc_maps = nullptr;  // TMA descriptors of the tensor-core GEMMs
+    void* st_maps = nullptr;  // TMA descriptors of the stencil halo boxes
     // graphs
     cudaStream_t cap = nullptr;
     StepGraph graph;
@@ -248,6 +251,18 @@ struct qg_plan {
 };
 
 namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+
+cudaError_t tmap_init() {
+    if (g_encode) return cudaSuccess;
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+    if (e || q != cudaDriverEntryPointSuccess || !fn) return cudaErrorNotSupported;
+    g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    return cudaSuccess;
+}
 
 template <typename T>
 cudaError_t dalloc(qg_plan* p, T** ptr, size_t bytes) {
@@ -285,6 +300,10 @@ cudaError_t timed(qg_plan* p, int k, cudaStream_t s, F&& launch) {
     return e;
 }
 
+// Kernels may overlap their prologue with the predecessor (programmatic dependent launch)
+// except while profiling, where events separate every launch.
+bool use_pdl(const qg_plan* p) { return !p->profiling; }
+
 GemmArgs gemm_args(qg_plan* p, int pass, const void* A, void* C, int a_fmt, int c_fmt, int acc) {
     GemmArgs g{};
     g.members = p->md;
@@ -305,8 +324,8 @@ GemmArgs gemm_args(qg_plan* p, int pass, const void* A, void* C, int a_fmt, int 
 cudaError_t run_gemm(qg_plan* p, const GemmArgs& g, cudaStream_t s) {
     const int nt = (g.pass == G1_FWD_X || g.pass == G4_INV_X) ? p->n_gx : p->n_gy;
     return timed(p, QG_K_GEMM, s, [&] {
-        if (p->opts.dst_precision == QG_DST_FP32) return launch_gemm_simt(g, nt, s);
-        return launch_gemm_tc(g, nt, p->opts.dst_precision, s);
+        if (p->opts.dst_precision == QG_DST_FP32) return launch_gemm_simt(g, nt, s, use_pdl(p));
+        return launch_gemm_tc(g, nt, p->opts.dst_precision, s, use_pdl(p));
     });
 }
 
@@ -321,7 +340,7 @@ cudaError_t run_dst_solve(qg_plan* p, cudaStream_t s) {
     if ((e = run_gemm(p, gemm_args(p, G4_INV_X, p->XB, p->XC, f, FMT_F32, 0), s))) return e;
     for (int r = 0; r < p->opts.refine_sweeps; ++r) {
         e = timed(p, QG_K_OTHER, s, [&] {
-            return launch_residual(p->md, p->st_tiles, p->n_st, p->XQ, p->XC, p->XA, f, p->xplane, s);
+            return launch_residual(p->md, p->st_tiles, p->n_st, p->XQ, p->XC, p->XA, f, p->xplane, s, use_pdl(p));
         });
         if (e) return e;
         if ((e = run_gemm(p, gemm_args(p, G1_FWD_X, p->XA, p->YA, f, f, 0), s))) return e;
@@ -332,11 +351,33 @@ cudaError_t run_dst_solve(qg_plan* p, cudaStream_t s) {
     return cudaSuccess;
 }
 
-cudaError_t run_prep(qg_plan* p, const float* q, float* q_inplace, int apply_bc, cudaStream_t s) {
-    return timed(p, QG_K_PREP, s, [&] {
-        return launch_prep(p->md, p->st_tiles, p->n_st, q, q_inplace, apply_bc, p->XA, p->op_fmt,
-                           p->XQ, p->xplane, s);
-    });
+// q (caller packing) -> optional internal copy + the modal GEMM operand.
+cudaError_t run_prep(qg_plan* p, const float* q, float* copy, int zero_ring_copy, int bc_operand,
+                     cudaStream_t s) {
+    PrepArgs a{};
+    a.members = p->md;
+    a.tiles = p->st_tiles;
+    a.q = q;
+    a.copy = copy;
+    a.zero_ring_copy = zero_ring_copy;
+    a.bc_operand = bc_operand;
+    a.xa = p->XA;
+    a.xa_fmt = p->op_fmt;
+    a.xq = p->XQ;
+    a.xplane = p->xplane;
+    return timed(p, QG_K_PREP, s, [&] { return launch_prep(a, p->n_st, s, use_pdl(p)); });
+}
+
+StencilArgs stencil_args(qg_plan* p, const float* params) {
+    StencilArgs a{};
+    a.members = p->md;
+    a.tiles = p->st_tiles;
+    a.maps = p->st_maps;
+    a.params = params;
+    a.xplane = p->xplane;
+    a.xa_fmt = p->op_fmt;
+    a.flags = p->flags;
+    return a;
 }
 
 struct Stage {
@@ -359,37 +400,29 @@ int scheme_stages(int scheme, Stage* st) {
     }
 }
 
-// One time step on q (caller packing, ring already BC'd, XA holding Cl2m q).
-cudaError_t run_one_step(qg_plan* p, float* q, const float* params, float dt, int scheme,
-                         cudaStream_t s) {
+// One time step of the state in S0 (XA holding Cl2m BC(S0)).  Stage k reads stage plane k
+// (S0, S1, S2) and writes stage plane k + 1; the final stage updates S0 in place (it reads S0
+// only pointwise there) and leaves XA ready for the next step.
+cudaError_t run_one_step(qg_plan* p, const float* params, float dt, int scheme, cudaStream_t s) {
     Stage st[4];
     const int ns = scheme_stages(scheme, st);
-    float* stage_buf[3] = {q, p->S1, p->S2};
+    float* stage_buf[3] = {p->S0, p->S1, p->S2};
     cudaError_t e;
     for (int k = 0; k < ns; ++k) {
         if ((e = run_dst_solve(p, s))) return e;
-        StencilArgs a{};
-        a.members = p->md;
-        a.tiles = p->st_tiles;
-        a.q = stage_buf[k];
-        a.q_internal = k > 0;
-        a.psi_hat = p->XC;
-        a.params = params;
+        StencilArgs a = stencil_args(p, params);
+        a.q_sel = k;
         a.apply_bc = 1;
-        a.dq = nullptr;
-        a.y0 = q;
+        a.y0 = p->S0;
         const bool fin = (k == ns - 1);
         a.final_stage = fin;
-        a.y_next = fin ? q : stage_buf[k + 1];
-        a.y_next_internal = !fin;
+        a.y_next = fin ? p->S0 : stage_buf[k + 1];
         a.a = st[k].a;
         a.b = st[k].b;
         a.dt = dt;
         a.xa = p->XA;
-        a.xa_fmt = p->op_fmt;
         a.xq = p->XQ;
-        a.flags = p->flags;
-        e = timed(p, QG_K_STENCIL, s, [&] { return launch_stencil(a, p->n_st, p->max_nl, p->xplane, s); });
+        e = timed(p, QG_K_STENCIL, s, [&] { return launch_stencil(a, p->n_st, p->max_nl, s, use_pdl(p)); });
         if (e) return e;
     }
     return cudaSuccess;
@@ -398,6 +431,33 @@ cudaError_t run_one_step(qg_plan* p, float* q, const float* params, float dt, in
 int cuda_err(cudaError_t e) { return e == cudaSuccess ? QG_OK : QG_ERR_CUDA; }
 
 }  // namespace
+
+namespace qg {
+cudaError_t tmap_encode(void* map, int bf16, int rank, const void* base, const uint64_t* dims,
+                        const uint64_t* strides_bytes, const uint32_t* box, int swizzle128) {
+    if (!g_encode || rank < 1 || rank > 5) return cudaErrorInvalidValue;
+    const int es = bf16 ? 2 : 4;
+    if (((uintptr_t)base & 15) || (box[0] * es) % 16) return cudaErrorInvalidValue;
+    cuuint64_t d[5];
+    cuuint64_t st[4];
+    cuuint32_t b[5], e[5];
+    for (int k = 0; k < rank; ++k) {
+        d[k] = dims[k];
+        b[k] = box[k];
+        e[k] = 1;
+        if (k < rank - 1) {
+            st[k] = strides_bytes[k];
+            if (st[k] % 16) return cudaErrorInvalidValue;
+        }
+    }
+    CUresult r = g_encode(static_cast<CUtensorMap*>(map),
+                          bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, rank,
+                          const_cast<void*>(base), d, st, b, e, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          swizzle128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+}  // namespace qg
 
 // =======================================================================================
 // C ABI
@@ -432,6 +492,10 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
     p->desc.assign(members, members + n_members);
     cudaGetDevice(&p->device);
     stencil_init();
+    if (tmap_init() != cudaSuccess) {
+        delete p;
+        return QG_ERR_UNSUPPORTED;
+    }
     if (o.dst_precision != QG_DST_FP32) {
         if (gemm_tc_init() != cudaSuccess) {
             delete p;
@@ -544,7 +608,8 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
     if (e == cudaSuccess) {
         const size_t xb = (size_t)p->xplane * 4, yb = (size_t)p->yplane * 4;
         if (!(e = dalloc(p, &p->XA, xb)) && !(e = dalloc(p, &p->XB, xb)) && !(e = dalloc(p, &p->XC, xb)) &&
-            !(e = dalloc(p, &p->YA, yb)) && !(e = dalloc(p, &p->YB, yb)) && !(e = dalloc(p, &p->S1, xb)) &&
+            !(e = dalloc(p, &p->YA, yb)) && !(e = dalloc(p, &p->YB, yb)) && !(e = dalloc(p, &p->S0, xb)) &&
+            !(e = dalloc(p, &p->S1, xb)) &&
             !(e = dalloc(p, &p->S2, xb)) && !(e = dalloc(p, &p->params, (size_t)n_members * QG_NPARAMS * 4)) &&
             !(e = dalloc(p, &p->flags, 16)))
             e = dalloc(p, &p->diag_acc, (size_t)2 * p->total_layers * sizeof(double));
@@ -560,6 +625,14 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
                 e = gemm_tc_encode(p->mh[i], pass, in_plane[pass], in_elems[pass], o.dst_precision,
                                    maps.data() + ((size_t)i * 4 + pass) * kTcMapsBytes);
         if (!e) e = upload(p, (uint8_t**)&p->tc_maps, maps);
+    }
+    if (e == cudaSuccess) {
+        // TMA descriptors of the stencil's halo boxes: the three stage planes and psi_hat
+        std::vector<uint8_t> maps((size_t)n_members * kStencilMapsBytes);
+        const float* planes[4] = {p->S0, p->S1, p->S2, p->XC};
+        for (int i = 0; i < n_members && !e; ++i)
+            e = stencil_encode_maps(p->mh[i], planes, maps.data() + (size_t)i * kStencilMapsBytes);
+        if (!e) e = upload(p, (uint8_t**)&p->st_maps, maps);
     }
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
@@ -606,10 +679,12 @@ int qg_plan_member_modes(const qg_plan* p, int m, double* lambdas, double* Cl2m,
 int qg_invert(qg_plan* p, const float* q, float* psi, void* stream) {
     if (!p || !q || !psi) return QG_ERR_NULL;
     cudaStream_t s = (cudaStream_t)stream;
-    cudaError_t e = run_prep(p, q, nullptr, 0, s);
+    cudaError_t e = run_prep(p, q, nullptr, 0, 0, s);
     if (!e) e = run_dst_solve(p, s);
     if (!e)
-        e = timed(p, QG_K_OTHER, s, [&] { return launch_mode_to_layer(p->md, p->st_tiles, p->n_st, p->XC, psi, s); });
+        e = timed(p, QG_K_OTHER, s, [&] {
+            return launch_mode_to_layer(p->md, p->st_tiles, p->n_st, p->XC, psi, s, use_pdl(p));
+        });
     return cuda_err(e);
 }
 
@@ -618,20 +693,15 @@ int qg_rhs(qg_plan* p, const float* q, float* dq, const float* params, int flags
     if (flags & ~QG_RHS_APPLY_BC) return QG_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
     const int bc = (flags & QG_RHS_APPLY_BC) ? 1 : 0;
-    cudaError_t e = run_prep(p, q, nullptr, bc, s);
+    // q is staged into the S1 plane (TMA-able pitch); the stencil applies the BC on read
+    cudaError_t e = run_prep(p, q, p->S1, 0, bc, s);
     if (!e) e = run_dst_solve(p, s);
     if (!e) {
-        StencilArgs a{};
-        a.members = p->md;
-        a.tiles = p->st_tiles;
-        a.q = q;
-        a.q_internal = 0;
-        a.psi_hat = p->XC;
-        a.params = params;
+        StencilArgs a = stencil_args(p, params);
+        a.q_sel = 1;
         a.apply_bc = bc;
         a.dq = dq;
-        a.flags = p->flags;
-        e = timed(p, QG_K_STENCIL, s, [&] { return launch_stencil(a, p->n_st, p->max_nl, p->xplane, s); });
+        e = timed(p, QG_K_STENCIL, s, [&] { return launch_stencil(a, p->n_st, p->max_nl, s, use_pdl(p)); });
     }
     return cuda_err(e);
 }
@@ -646,47 +716,49 @@ int qg_step(qg_plan* p, float* q, const float* params, double dt, int n_steps, i
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = cudaMemcpyAsync(p->params, params, sizeof(float) * p->n_members * QG_NPARAMS,
                                     cudaMemcpyDeviceToDevice, s);
-    // stage inputs always read q with a zero ring; the ring itself is zeroed in place only for
-    // a new integration (integrate() applies the BC to state0)
-    if (!e) e = run_prep(p, q, (flags & QG_STEP_APPLY_BC) ? q : nullptr, 1, s);
+    // the state lives in S0 for the whole call; its ring is zeroed only for a new
+    // integration (integrate() applies the BC to state0), stage inputs always read a zero ring
+    if (!e) e = run_prep(p, q, p->S0, (flags & QG_STEP_APPLY_BC) ? 1 : 0, 1, s);
     if (e) return cuda_err(e);
-    if (n_steps == 0) return QG_OK;
     const bool use_graph = p->opts.use_graphs && !p->profiling;
     if (!use_graph) {
-        for (int k = 0; k < n_steps && !e; ++k) e = run_one_step(p, q, p->params, (float)dt, scheme, s);
-        return cuda_err(e);
+        for (int k = 0; k < n_steps && !e; ++k) e = run_one_step(p, p->params, (float)dt, scheme, s);
+    } else if (n_steps > 0) {
+        StepGraph& g = p->graph;
+        if (!g.exec || g.dt != dt || g.scheme != scheme) {
+            if (g.exec) {
+                cudaGraphExecDestroy(g.exec);
+                g.exec = nullptr;
+            }
+            cudaGraph_t graph = nullptr;
+            e = cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal);
+            if (!e) {
+                cudaError_t e1 = run_one_step(p, p->params, (float)dt, scheme, p->cap);
+                e = cudaStreamEndCapture(p->cap, &graph);
+                if (!e) e = e1;
+            }
+            if (!e) e = cudaGraphInstantiate(&g.exec, graph, 0);
+            if (graph) cudaGraphDestroy(graph);
+            if (e) {
+                g.exec = nullptr;
+                return cuda_err(e);
+            }
+            g.dt = dt;
+            g.scheme = scheme;
+        }
+        for (int k = 0; k < n_steps && !e; ++k) e = cudaGraphLaunch(g.exec, s);
     }
-    StepGraph& g = p->graph;
-    if (!g.exec || g.q != q || g.dt != dt || g.scheme != scheme) {
-        if (g.exec) {
-            cudaGraphExecDestroy(g.exec);
-            g.exec = nullptr;
-        }
-        cudaGraph_t graph = nullptr;
-        e = cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal);
-        if (!e) {
-            cudaError_t e1 = run_one_step(p, q, p->params, (float)dt, scheme, p->cap);
-            e = cudaStreamEndCapture(p->cap, &graph);
-            if (!e) e = e1;
-        }
-        if (!e) e = cudaGraphInstantiate(&g.exec, graph, 0);
-        if (graph) cudaGraphDestroy(graph);
-        if (e) {
-            g.exec = nullptr;
-            return cuda_err(e);
-        }
-        g.q = q;
-        g.dt = dt;
-        g.scheme = scheme;
-    }
-    for (int k = 0; k < n_steps && !e; ++k) e = cudaGraphLaunch(g.exec, s);
+    if (!e)
+        e = timed(p, QG_K_OTHER, s, [&] {
+            return launch_unpack(p->md, p->st_tiles, p->n_st, p->S0, q, s, use_pdl(p));
+        });
     return cuda_err(e);
 }
 
 int qg_diagnose(qg_plan* p, const float* q, float* ke, float* ens, void* stream) {
     if (!p || !q || !ke || !ens) return QG_ERR_NULL;
     cudaStream_t s = (cudaStream_t)stream;
-    cudaError_t e = run_prep(p, q, nullptr, 0, s);
+    cudaError_t e = run_prep(p, q, nullptr, 0, 0, s);
     if (!e) e = run_dst_solve(p, s);
     if (!e) e = cudaMemsetAsync(p->diag_acc, 0, sizeof(double) * 2 * p->total_layers, s);
     if (!e)

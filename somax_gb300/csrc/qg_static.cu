@@ -161,7 +161,16 @@ extern "C" int qg_invert_static(const qg_member_desc* member, const float* q, fl
 
     k_static_setup<<<64, 256, 0, s>>>(M, d.Lx / d.nx, d.Ly / d.ny, base, n_st, st_tx, n_gx, gx_nt, n_gy, gy_nt);
     cudaError_t e = cudaGetLastError();
-    if (!e) e = launch_prep(md, st, n_st, q, nullptr, 0, P0, FMT_F32, nullptr, kStaticPlane, s);
+    if (!e) {
+        PrepArgs pa{};
+        pa.members = md;
+        pa.tiles = st;
+        pa.q = q;
+        pa.xa = P0;
+        pa.xa_fmt = FMT_F32;
+        pa.xplane = kStaticPlane;
+        e = launch_prep(pa, n_st, s, false);
+    }
     auto gemm = [&](int pass, const float* A, float* C, const GemmTile* tl, int nt) {
         GemmArgs g{};
         g.members = md;
@@ -171,12 +180,12 @@ extern "C" int qg_invert_static(const qg_member_desc* member, const float* q, fl
         g.A = A;
         g.C = C;
         g.a_fmt = g.c_fmt = FMT_F32;
-        return launch_gemm_simt(g, nt, s);
+        return launch_gemm_simt(g, nt, s, false);
     };
     if (!e) e = gemm(G1_FWD_X, P0, P1, gx, n_gx);
     if (!e) e = gemm(G2_FWD_Y, P1, P2, gy, n_gy);
     if (!e) e = gemm(G3_INV_Y, P2, P0, gy, n_gy);
     if (!e) e = gemm(G4_INV_X, P0, P1, gx, n_gx);
-    if (!e) e = launch_mode_to_layer(md, st, n_st, P1, psi, s);
+    if (!e) e = launch_mode_to_layer(md, st, n_st, P1, psi, s, false);
     return e == cudaSuccess ? QG_OK : QG_ERR_CUDA;
 }
