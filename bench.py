@@ -162,6 +162,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="baroclinic3_128")
     ap.add_argument("--precision", default="fp32")
+    ap.add_argument("--persistent", type=int, default=1, help="tensor-core precisions: one launch per call")
     ap.add_argument("--ref-sample-steps", type=int, default=12)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -186,7 +187,7 @@ def main():
     if world > 1:
         dist.init_process_group("nccl", device_id=dev)
 
-    model = sg.BaroclinicQG.create(**cfg.model_kwargs(), precision=args.precision)
+    model = sg.BaroclinicQG.create(**cfg.model_kwargs(), precision=args.precision, persistent=bool(args.persistent))
     steps_per_day = int(round(86400.0 / cfg.dt))
     q0 = tc.initial_pv(cfg, seed=rank).astype(np.float32)
     q = torch.tensor(q0, device=dev)

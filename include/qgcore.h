@@ -103,7 +103,9 @@ typedef struct qg_options {
     int dst_precision;  /* QG_DST_* */
     int refine_sweeps;  /* FP32 residual-refinement sweeps of the Helmholtz solve (0 or 1) */
     int use_graphs;     /* 1: qg_step replays a captured CUDA graph per step */
-    int reserved[5];
+    int persistent;     /* 1: qg_step advances all steps in one persistent cooperative launch
+                           (tensor-core precisions without refinement) */
+    int reserved[4];
 } qg_options;
 
 typedef struct qg_plan qg_plan;
@@ -164,7 +166,8 @@ const char* qg_strerror(int code);
 #define QG_K_GEMM 1    /* DST-I GEMMs of the inversion */
 #define QG_K_STENCIL 2 /* fused RHS stencil (+ RK stage update, + next-stage prologue) */
 #define QG_K_OTHER 3   /* mode -> layer epilogue, residual, diagnostics, packing */
-#define QG_K_COUNT 4
+#define QG_K_PERSISTENT 4 /* the persistent step kernel (all phases of all steps) */
+#define QG_K_COUNT 5
 int qg_set_profiling(qg_plan* plan, int enable); /* resets the counters */
 int qg_kernel_stats(qg_plan* plan, int kclass, double* total_ms, int64_t* launches);
 

@@ -5,6 +5,6 @@ include/qgcore.h); this package is the Python host side that mirrors somax's cla
 from .qg import (  # noqa: F401
     SSPRK3, BaroclinicQG, BaroclinicQGDiagnostics, BaroclinicQGParams, BaroclinicQGState,
     BarotropicQG, BarotropicQGDiagnostics, BarotropicQGParams, BarotropicQGState, Euler, Heun,
-    MemberSpec, Plan, QGDiagnostics, QGParams, SaveAt, Solution, SomaxModel, State, Tsit5,
+    MemberSpec, Plan, QGDiagnostics, QGEnsemble, QGParams, SaveAt, Solution, SomaxModel, State, Tsit5,
 )
 from .transforms import ModalTransform, StratificationProfile  # noqa: F401

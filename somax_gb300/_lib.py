@@ -51,7 +51,7 @@ class MemberDesc(C.Structure):
 
 class Options(C.Structure):
     _fields_ = [("dst_precision", C.c_int), ("refine_sweeps", C.c_int), ("use_graphs", C.c_int),
-                ("reserved", C.c_int * 5)]
+                ("persistent", C.c_int), ("reserved", C.c_int * 4)]
 
 
 _lib = None

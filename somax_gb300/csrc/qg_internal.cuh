@@ -156,7 +156,33 @@ struct GemmArgs {
     const void* tc_maps;  // tensor-core path: TMA descriptors, 4 per member (one per pass)
     int* flags;           // device status word (bit 1: a bounded wait timed out)
 };
-constexpr int kTcMapsBytes = 512;  // 4 CUtensorMap per (member, pass)
+constexpr int kTcMapsBytes = 512;
+
+// Arguments of the persistent step kernel (qg_persistent.cu).
+struct PersistArgs {
+    const MemberDev* members;
+    const GemmTile* gx;
+    const GemmTile* gy;
+    const StencilTile* st;
+    int n_gx, n_gy, n_st, max_nl;
+    const void* tc_maps;
+    const void* st_maps;
+    void *XA, *YA, *YB, *XB;  // operand-format planes
+    float* XC;                // psi_hat
+    float* S[3];              // stage planes (S[0] = state)
+    const float* params;
+    int64_t xplane, yplane;
+    size_t slot_bytes;        // one stencil box buffer
+    int op_fmt;
+    int n_stages, n_steps;
+    float sa[4], sb[4], dt;   // Shu-Osher stage coefficients
+    int* flags;
+    unsigned* bar_count;      // grid barrier: arrivals, generation
+    unsigned* bar_gen;
+};
+size_t persistent_smem_bytes(int precision, int max_nl, size_t* slot_bytes);
+cudaError_t persistent_init();
+cudaError_t launch_persistent(const PersistArgs& a, int grid, int precision, cudaStream_t s);  // 4 CUtensorMap per (member, pass)
 cudaError_t gemm_tc_encode(const MemberDev& M, int pass, const void* a_plane, int64_t a_plane_elems, int prec,
                            void* out);
 cudaError_t launch_gemm_simt(const GemmArgs& g, int ntiles, cudaStream_t s, bool pdl);

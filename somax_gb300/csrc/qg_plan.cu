@@ -240,13 +240,15 @@ struct qg_plan {
     int op_fmt = FMT_F32;
     void* tc_maps = nullptr;  // TMA descriptors of the tensor-core GEMMs
     void* st_maps = nullptr;  // TMA descriptors of the stencil halo boxes
+    unsigned* bar = nullptr;  // grid barrier words of the persistent kernel (count, generation)
+    int n_sm = 0;
     // graphs
     cudaStream_t cap = nullptr;
     StepGraph graph;
     // profiling
     bool profiling = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev[QG_K_COUNT];
-    size_t ev_used[QG_K_COUNT] = {0, 0, 0, 0};
+    size_t ev_used[QG_K_COUNT] = {0, 0, 0, 0, 0};
     int device = 0;
 };
 
@@ -478,6 +480,7 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
     o.dst_precision = QG_DST_FP32;
     o.refine_sweeps = 0;
     o.use_graphs = 1;
+    o.persistent = 1;
     if (opts) o = *opts;
     if (o.dst_precision < QG_DST_FP32 || o.dst_precision > QG_DST_BF16X3) return QG_ERR_ARG;
     if (o.refine_sweeps < 0 || o.refine_sweeps > 1) return QG_ERR_ARG;
@@ -497,7 +500,7 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
         return QG_ERR_UNSUPPORTED;
     }
     if (o.dst_precision != QG_DST_FP32) {
-        if (gemm_tc_init() != cudaSuccess) {
+        if (gemm_tc_init() != cudaSuccess || persistent_init() != cudaSuccess) {
             delete p;
             return QG_ERR_UNSUPPORTED;
         }
@@ -611,7 +614,7 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
             !(e = dalloc(p, &p->YA, yb)) && !(e = dalloc(p, &p->YB, yb)) && !(e = dalloc(p, &p->S0, xb)) &&
             !(e = dalloc(p, &p->S1, xb)) &&
             !(e = dalloc(p, &p->S2, xb)) && !(e = dalloc(p, &p->params, (size_t)n_members * QG_NPARAMS * 4)) &&
-            !(e = dalloc(p, &p->flags, 16)))
+            !(e = dalloc(p, &p->flags, 16)) && !(e = dalloc(p, &p->bar, 16)))
             e = dalloc(p, &p->diag_acc, (size_t)2 * p->total_layers * sizeof(double));
         if (!e && o.refine_sweeps > 0) e = dalloc(p, &p->XQ, xb);
     }
@@ -634,6 +637,7 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
             e = stencil_encode_maps(p->mh[i], planes, maps.data() + (size_t)i * kStencilMapsBytes);
         if (!e) e = upload(p, (uint8_t**)&p->st_maps, maps);
     }
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&p->n_sm, cudaDevAttrMultiProcessorCount, p->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
@@ -720,8 +724,46 @@ int qg_step(qg_plan* p, float* q, const float* params, double dt, int n_steps, i
     // integration (integrate() applies the BC to state0), stage inputs always read a zero ring
     if (!e) e = run_prep(p, q, p->S0, (flags & QG_STEP_APPLY_BC) ? 1 : 0, 1, s);
     if (e) return cuda_err(e);
+    const bool persistent = p->opts.persistent && p->opts.dst_precision != QG_DST_FP32 && p->opts.refine_sweeps == 0;
     const bool use_graph = p->opts.use_graphs && !p->profiling;
-    if (!use_graph) {
+    if (persistent && n_steps > 0) {
+        PersistArgs a{};
+        a.members = p->md;
+        a.gx = p->gx_tiles;
+        a.gy = p->gy_tiles;
+        a.st = p->st_tiles;
+        a.n_gx = p->n_gx;
+        a.n_gy = p->n_gy;
+        a.n_st = p->n_st;
+        a.max_nl = p->max_nl;
+        a.tc_maps = p->tc_maps;
+        a.st_maps = p->st_maps;
+        a.XA = p->XA;
+        a.YA = p->YA;
+        a.YB = p->YB;
+        a.XB = p->XB;
+        a.XC = p->XC;
+        a.S[0] = p->S0;
+        a.S[1] = p->S1;
+        a.S[2] = p->S2;
+        a.params = p->params;
+        a.xplane = p->xplane;
+        a.yplane = p->yplane;
+        persistent_smem_bytes(p->opts.dst_precision, p->max_nl, &a.slot_bytes);
+        a.op_fmt = p->op_fmt;
+        a.n_stages = scheme_stages(scheme, st);
+        for (int k = 0; k < a.n_stages; ++k) {
+            a.sa[k] = st[k].a;
+            a.sb[k] = st[k].b;
+        }
+        a.dt = (float)dt;
+        a.n_steps = n_steps;
+        a.flags = p->flags;
+        a.bar_count = p->bar;
+        a.bar_gen = p->bar + 1;
+        const int grid = std::max(1, std::min(p->n_sm, std::max(p->n_st, std::max(p->n_gx, p->n_gy))));
+        e = timed(p, QG_K_PERSISTENT, s, [&] { return launch_persistent(a, grid, p->opts.dst_precision, s); });
+    } else if (!use_graph) {
         for (int k = 0; k < n_steps && !e; ++k) e = run_one_step(p, p->params, (float)dt, scheme, s);
     } else if (n_steps > 0) {
         StepGraph& g = p->graph;

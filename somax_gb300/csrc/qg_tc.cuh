@@ -1,0 +1,214 @@
+// tcgen05 building blocks of the DST-I GEMMs, shared by the one-tile-per-CTA kernels
+// (qg_gemm_tc.cu) and the persistent step kernel (qg_persistent.cu).
+//
+// C = A * S with A rows (layer, r) K-major and S symmetric (so its rows are the K-major B
+// operand).  Operands are 128-byte rows in 128-byte-swizzled shared memory (the layout TMA
+// writes with SWIZZLE_128B); the FP32 accumulator is a 128-lane x BN-column TMEM block.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include "qg_device.cuh"
+#include "qg_internal.cuh"
+
+namespace qg {
+
+constexpr int TC_BM = 128;
+constexpr int TC_BN = 128;
+
+struct TcMaps {
+    CUtensorMap a[2];  // A hi (or f32), A lo
+    CUtensorMap b[2];  // S hi (or f32), S lo
+};
+static_assert(sizeof(TcMaps) == kTcMapsBytes, "TcMaps size");
+
+template <int PREC>
+struct TcCfg;
+template <>
+struct TcCfg<QG_DST_TF32> {
+    static constexpr int BK = 32;  // 32 fp32 = 128-byte rows
+    static constexpr int STAGES = 4;
+    static constexpr int ESIZE = 4;
+    static constexpr int NA = 1, NB = 1;  // operand planes
+    static constexpr int UMMA_K = 8;      // 32 bytes per MMA along K
+    static constexpr uint32_t FMT = 2;    // tf32
+};
+template <>
+struct TcCfg<QG_DST_BF16X3> {
+    static constexpr int BK = 64;  // 64 bf16 = 128-byte rows
+    static constexpr int STAGES = 3;
+    static constexpr int ESIZE = 2;
+    static constexpr int NA = 2, NB = 2;  // hi, lo
+    static constexpr int UMMA_K = 16;
+    static constexpr uint32_t FMT = 1;    // bf16
+};
+
+template <int PREC>
+__host__ __device__ constexpr int tc_tile_a_bytes() { return TC_BM * TcCfg<PREC>::BK * TcCfg<PREC>::ESIZE; }
+template <int PREC>
+__host__ __device__ constexpr int tc_tile_b_bytes() { return TC_BN * TcCfg<PREC>::BK * TcCfg<PREC>::ESIZE; }
+template <int PREC>
+__host__ __device__ constexpr int tc_stage_bytes() {
+    return TcCfg<PREC>::NA * tc_tile_a_bytes<PREC>() + TcCfg<PREC>::NB * tc_tile_b_bytes<PREC>();
+}
+
+// Instruction descriptor: D f32, A/B format FMT, both K-major, N = TC_BN, M = TC_BM.
+template <int PREC>
+__device__ __forceinline__ uint32_t tc_idesc() {
+    return (1u << 4) | (TcCfg<PREC>::FMT << 7) | (TcCfg<PREC>::FMT << 10) | ((uint32_t)(TC_BN >> 3) << 17) |
+           ((uint32_t)(TC_BM >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, 8-row groups 1024
+// bytes apart (SBO), descriptor version 1.
+__device__ __forceinline__ uint64_t tc_sdesc(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;            // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;  // stride byte offset
+    d |= (uint64_t)1 << 46;            // version
+    d |= (uint64_t)2 << 61;            // SWIZZLE_128B
+    return d;
+}
+
+template <uint32_t FMT>
+__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
+    if constexpr (FMT == 2) {
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+            "l"(da), "l"(db), "r"(idesc), "r"(acc));
+    } else {
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+            "l"(da), "l"(db), "r"(idesc), "r"(acc));
+    }
+}
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void tc_alloc(uint32_t* slot, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(slot)), "r"(ncols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+}
+__device__ __forceinline__ void tc_dealloc(uint32_t tmem, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(b)) : "memory");
+}
+
+#define QG_LD32(r, taddr)                                                                                   \
+    asm volatile(                                                                                           \
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"    \
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"                          \
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),  \
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),         \
+          "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),       \
+          "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),       \
+          "=r"(r[29]), "=r"(r[30]), "=r"(r[31])                                                            \
+        : "r"(taddr))
+
+// Geometry of a pass for one member.
+struct TcGeom {
+    int Mb, K, Nn, Mtot, ldo;
+    int64_t cbase, cplane;
+};
+template <int PASS>
+__device__ __forceinline__ TcGeom tc_geom(const MemberDev& M, int64_t xplane, int64_t yplane) {
+    constexpr bool xin = (PASS == G1_FWD_X || PASS == G4_INV_X);
+    constexpr bool xout = (PASS == G3_INV_Y || PASS == G4_INV_X);
+    TcGeom g;
+    g.Mb = xin ? M.Ny : M.Nx;
+    g.K = xin ? M.Nx : M.Ny;
+    g.Nn = g.K;
+    g.Mtot = M.nl * g.Mb;
+    g.ldo = xout ? M.Px : M.Py;
+    g.cbase = xout ? M.off_x : M.off_y;
+    g.cplane = xout ? xplane : yplane;
+    return g;
+}
+
+// Issue the MMAs of one k-block (operands at shared addresses sa / sb) into tmem_d.
+template <int PREC>
+__device__ __forceinline__ void tc_mma_kblock(uint32_t tmem_d, uint32_t sa, uint32_t sb, bool first) {
+    using C = TcCfg<PREC>;
+    const uint32_t idesc = tc_idesc<PREC>();
+#pragma unroll
+    for (int k = 0; k < C::BK / C::UMMA_K; ++k) {
+        const uint32_t koff = k * C::UMMA_K * C::ESIZE;  // 32 bytes per step
+        const uint64_t a0 = tc_sdesc(sa + koff), b0 = tc_sdesc(sb + koff);
+        tc_mma<C::FMT>(tmem_d, a0, b0, idesc, (!first || k > 0) ? 1u : 0u);
+        if constexpr (C::NA == 2) {
+            const uint64_t a1 = tc_sdesc(sa + tc_tile_a_bytes<PREC>() + koff);
+            const uint64_t b1 = tc_sdesc(sb + tc_tile_b_bytes<PREC>() + koff);
+            tc_mma<C::FMT>(tmem_d, a0, b1, idesc, 1u);  // Ahi * Slo
+            tc_mma<C::FMT>(tmem_d, a1, b0, idesc, 1u);  // Alo * Shi
+        }
+    }
+}
+
+__device__ __forceinline__ void tc_store_bf16x2(__nv_bfloat16* p, int64_t plane, int64_t idx, float v) {
+    const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+    p[idx] = hi;
+    p[plane + idx] = __float2bfloat16_rn(v - __bfloat162float(hi));
+}
+
+// Epilogue of one 128 x TC_BN tile by one of four epilogue warps (TMEM lane quarter
+// `quarter`): read the accumulator and apply the pass's store.  All four warps must call it
+// (tcgen05.ld is warp-collective); `valid` false skips the stores.
+template <int PASS>
+__device__ __forceinline__ void tc_epilogue(const MemberDev& M, const TcGeom& g, void* Cv, int c_fmt, int accumulate,
+                                            int m0, int n0, uint32_t tmem_acc, int quarter, int lane, bool valid) {
+    const int m = m0 + quarter * 32 + lane;
+    const int l = m < g.Mtot ? m / g.Mb : 0;
+    const int r = m - l * g.Mb;
+    const float exr = (PASS == G2_FWD_Y && m < g.Mtot) ? M.ex[r] : 0.f;
+    const float laml = M.lam[l];
+    float* Cf = static_cast<float*>(Cv) + g.cbase;
+    __nv_bfloat16* Cb = static_cast<__nv_bfloat16*>(Cv) + g.cbase;
+    for (int c = 0; c < TC_BN / 32; ++c) {
+        uint32_t v[32];
+        const uint32_t taddr = tmem_acc + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(c * 32);
+        QG_LD32(v, taddr);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (!valid || m >= g.Mtot) continue;
+        const int nb = n0 + c * 32;
+        if (nb >= g.Nn) continue;
+        if constexpr (PASS == G1_FWD_X || PASS == G3_INV_Y) {
+            // transposed store out[(l, n)][r]: lanes hold consecutive r -> coalesced
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                if (nb + j >= g.Nn) break;
+                const float x = __uint_as_float(v[j]);
+                const int64_t o = ((int64_t)l * g.Nn + nb + j) * g.ldo + r;
+                if (c_fmt == FMT_F32)
+                    Cf[o] = x;
+                else
+                    tc_store_bf16x2(Cb, g.cplane, o, x);
+            }
+        } else {
+            const int64_t o = (int64_t)m * g.ldo + nb;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                if (nb + j >= g.Nn) break;
+                float x = __uint_as_float(v[j]);
+                if constexpr (PASS == G2_FWD_Y) x = x / (exr + M.ey[nb + j] - laml);
+                if (c_fmt == FMT_F32) {
+                    if (PASS == G4_INV_X && accumulate) x += Cf[o + j];
+                    Cf[o + j] = x;
+                } else {
+                    tc_store_bf16x2(Cb, g.cplane, o + j, x);
+                }
+            }
+        }
+    }
+}
+
+}  // namespace qg

@@ -166,7 +166,7 @@ class Plan:
     """Owns a ``qg_plan`` (device constants + workspace) on one CUDA device."""
 
     def __init__(self, members: Sequence["MemberSpec"], precision="fp32", refine=0, use_graphs=True,
-                 device=None):
+                 device=None, persistent=True):
         if not torch.cuda.is_available():
             raise RuntimeError("somax_gb300 needs a CUDA device (no CPU fallback)")
         self.device = torch.device(device or "cuda", torch.cuda.current_device()) if device is None \
@@ -175,7 +175,7 @@ class Plan:
         arr = (MemberDesc * len(members))()
         for i, m in enumerate(members):
             m.fill(arr[i])
-        opts = Options(PRECISIONS[precision], int(refine), int(bool(use_graphs)))
+        opts = Options(PRECISIONS[precision], int(refine), int(bool(use_graphs)), int(bool(persistent)))
         handle = C.c_void_p()
         with torch.cuda.device(self.device):
             check(L.qg_plan_create(arr, len(members), C.byref(opts), C.byref(handle)), "qg_plan_create")
@@ -343,12 +343,13 @@ class _QGBase(SomaxModel):
     barotropic = False
 
     def __init__(self, spec: MemberSpec, params: QGParams, precision="fp32", refine=0, use_graphs=True,
-                 strat=None, modal=None):
+                 strat=None, modal=None, persistent=True):
         self.spec = spec
         self.params = params
         self.precision = precision
         self.refine = refine
         self.use_graphs = use_graphs
+        self.persistent = persistent
         self.strat = strat
         self.modal = modal
         self.grid = Grid(spec.nx, spec.ny, spec.Lx, spec.Ly)
@@ -361,7 +362,7 @@ class _QGBase(SomaxModel):
             device = torch.device("cuda", torch.cuda.current_device())
         key = device.index
         if key not in self._plans:
-            self._plans[key] = Plan([self.spec], self.precision, self.refine, self.use_graphs, device)
+            self._plans[key] = Plan([self.spec], self.precision, self.refine, self.use_graphs, device, self.persistent)
         return self._plans[key]
 
     @property
@@ -519,10 +520,11 @@ class BaroclinicQG(_QGBase):
                H=(400.0, 1100.0, 2600.0), g_prime=(9.81, 0.025, 0.0125), stratification=None,
                lateral_viscosity=0.0, bottom_drag=0.0, wind_amplitude=0.0, wind_profile="doublegyre",
                poisson_bc="dst", biharmonic_viscosity=0.0, precision="fp32", refine=0, eigs="consistent",
-               use_graphs=True) -> "BaroclinicQG":
+               use_graphs=True, persistent=True) -> "BaroclinicQG":
         """``BaroclinicQG.create`` (``baroclinic.py:230-332``) with the same keyword arguments,
         plus ``biharmonic_viscosity`` (extension), ``precision`` of the DST-I GEMMs
-        ("fp32", "tf32", "bf16x3"), ``refine`` sweeps and the ``eigs`` mode."""
+        ("fp32", "tf32", "bf16x3"), ``refine`` sweeps, the ``eigs`` mode and whether ``step`` runs
+        in one ``persistent`` launch (tensor-core precisions)."""
         if poisson_bc != "dst":
             raise ValueError("only the Dirichlet DST-I inversion (poisson_bc='dst') is implemented")
         if stratification is not None:
@@ -537,7 +539,7 @@ class BaroclinicQG(_QGBase):
                           eigs, modal)
         params = QGParams(*(torch.tensor(float(v)) for v in (lateral_viscosity, bottom_drag, wind_amplitude,
                                                              biharmonic_viscosity)))
-        return BaroclinicQG(spec, params, precision, refine, use_graphs, strat, modal)
+        return BaroclinicQG(spec, params, precision, refine, use_graphs, strat, modal, persistent)
 
     @property
     def n_layers(self):
@@ -553,9 +555,56 @@ class BarotropicQG(_QGBase):
     @staticmethod
     def create(nx=64, ny=64, Lx=1e6, Ly=1e6, f0=1e-4, beta=1.6e-11, lateral_viscosity=0.0,
                bottom_drag=0.0, wind_amplitude=0.0, wind_profile="doublegyre", biharmonic_viscosity=0.0,
-               precision="fp32", refine=0, use_graphs=True) -> "BarotropicQG":
+               precision="fp32", refine=0, use_graphs=True, persistent=True) -> "BarotropicQG":
         """``BarotropicQG.create`` (``barotropic.py:186-248``)."""
         spec = MemberSpec(nx, ny, Lx, Ly, f0, beta, [1.0], [1.0], True, wind_profile)
         params = QGParams(*(torch.tensor(float(v)) for v in (lateral_viscosity, bottom_drag, wind_amplitude,
                                                              biharmonic_viscosity)))
-        return BarotropicQG(spec, params, precision, refine, use_graphs)
+        return BarotropicQG(spec, params, precision, refine, use_graphs, persistent=persistent)
+
+
+class QGEnsemble:
+    """Many independent members (any mix of grid sizes, layer counts and parameters) advanced
+    together: one plan, every launch covers all members (the persistent step kernel for the
+    tensor-core precisions).  States are packed member after member in the reference layout."""
+
+    def __init__(self, models: Sequence[_QGBase], precision="bf16x3", refine=0, use_graphs=True, persistent=True,
+                 device=None):
+        if not models:
+            raise ValueError("an ensemble needs at least one member")
+        self.models = list(models)
+        self.plan = Plan([m.spec for m in self.models], precision, refine, use_graphs, device, persistent)
+        self.offsets = self.plan.offsets
+        self.sizes = [int(np.prod(m.shape)) for m in self.models]
+
+    @property
+    def state_size(self) -> int:
+        return self.plan.state_size
+
+    def params(self, device=None) -> torch.Tensor:
+        device = device or self.plan.device
+        return torch.cat([m._param_vector(device) for m in self.models])
+
+    def pack(self, qs: Sequence[torch.Tensor]) -> torch.Tensor:
+        if len(qs) != len(self.models):
+            raise ValueError("one field per member")
+        for q, m in zip(qs, self.models):
+            if tuple(q.shape) != m.shape:
+                raise ValueError(f"member field shape {tuple(q.shape)} != {m.shape}")
+        return torch.cat([q.reshape(-1).to(torch.float32) for q in qs]).contiguous()
+
+    def unpack(self, packed: torch.Tensor) -> list:
+        return [packed[o:o + n].view(m.shape) for o, n, m in zip(self.offsets, self.sizes, self.models)]
+
+    def rhs(self, packed: torch.Tensor, apply_bc=False) -> torch.Tensor:
+        return self.plan.rhs(packed, self.params(packed.device), apply_bc=apply_bc)
+
+    def invert(self, packed: torch.Tensor) -> torch.Tensor:
+        return self.plan.invert(packed)
+
+    def step(self, packed: torch.Tensor, dt: float, n_steps: int = 1, solver="ssprk3", apply_bc=True) -> torch.Tensor:
+        """Advance every member in place by ``n_steps`` steps of ``dt``."""
+        scheme = _solver_name(solver)
+        if scheme not in ("heun", "ssprk3"):
+            raise ValueError("ensembles step with heun or ssprk3")
+        return self.plan.step(packed, self.params(packed.device), dt, n_steps, scheme, apply_bc)
