@@ -126,11 +126,38 @@ def cpu_baseline(cfg, sample_steps: int, threads: int):
     return days_per_s, el
 
 
+def ensemble_cpu_rate(threads: int, sample_steps: int):
+    """member-days/s of the 256-member mix on the host: one member of each class timed for
+    `sample_steps` steps, the ensemble's step time is the count-weighted sum."""
+    from somax_gb300 import testcases as tc
+
+    t_step = 0.0
+    for count, cfg in tc.C4_MIX:
+        _, el = cpu_baseline(cfg, sample_steps, threads)
+        t_step += count * el / sample_steps
+    return 256 * tc.C4_MIX[0][1].dt / 86400.0 / t_step
+
+
 def run_reference(args, cfg):
     rank = _env_int("RANK", 0)
     if rank != 0:
         return
     threads = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    if args.config == "ensemble256":
+        vals = [ensemble_cpu_rate(threads, 2) for _ in range(args.steps)]
+        value = statistics.median(vals)
+        line = {
+            "impl": "reference", "metric": "QG member-days/sec per GB300 (256-member ragged ensemble, SSP-RK3 dt=1200 s)",
+            "value": value, "unit": "member-days/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 / value, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "ensemble256", "sample": "2 steps of one member per class, count-weighted"},
+            "cpu_baseline": {"value": value, "unit": "member-days/s", "cores": threads, "kind": "port",
+                             "sample": "float32 NumPy/SciPy restatement, one member of each class"},
+            "e2e": {"value": value, "unit": "member-days/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line), flush=True)
+        return
     sample = max(1, min(args.ref_sample_steps, int(round(86400 / cfg.dt))))
     for _ in range(args.warmup):
         cpu_baseline(cfg, 1, threads)
@@ -154,6 +181,76 @@ def run_reference(args, cfg):
     print(json.dumps(line), flush=True)
 
 
+class Workload:
+    """One bench step = one model day of every member, on one device."""
+
+    def __init__(self, name, precision, persistent, dev, seed):
+        import torch
+
+        import somax_gb300 as sg
+        from somax_gb300 import testcases as tc
+
+        self.name = name
+        rng = np.random.default_rng(1000 + seed)
+        if name == "ensemble256":
+            cfgs, models, q0s = [], [], []
+            k = 0
+            for count, cfg in tc.C4_MIX:
+                for _ in range(count):
+                    kw = cfg.model_kwargs()
+                    kw["wind_amplitude"] = tc.wind_amplitude(float(rng.uniform(0.05, 0.12)), cfg.L)
+                    models.append(sg.BaroclinicQG.create(**kw, precision=precision, persistent=persistent))
+                    q0s.append(tc.initial_pv(cfg, seed=10000 * seed + k).astype(np.float32))
+                    cfgs.append(cfg)
+                    k += 1
+            self.ens = sg.QGEnsemble(models, precision=precision, persistent=persistent, device=dev)
+            self.plan = self.ens.plan
+            self.params = self.ens.params(dev)
+            self.q0 = np.concatenate([q.reshape(-1) for q in q0s])
+            self.members = [(c.n + 2, c.nl) for c in cfgs]
+            self.dt, self.scheme = cfgs[0].dt, cfgs[0].scheme
+            self.unit = "member-days/s"
+            self.metric = "QG member-days/sec per GB300 (256-member ragged ensemble, SSP-RK3 dt=1200 s)"
+            self.describe = ("ensemble256: 96 x 1-layer 64^2 (Rd 50 km) + 96 x 3-layer 128^2 + 48 x 3-layer 256^2 + "
+                             "16 x 5-layer 256^2 double gyres, tau0 ~ U(0.05, 0.12) N/m^2, ssprk3 dt=1200s")
+            self.model = None
+        else:
+            cfg = tc.CONFIGS[name]
+            self.model = sg.BaroclinicQG.create(**cfg.model_kwargs(), precision=precision, persistent=persistent)
+            self.plan = self.model.plan(dev)
+            self.params = self.model._param_vector(dev)
+            self.q0 = tc.initial_pv(cfg, seed=seed).astype(np.float32)
+            self.members = [(cfg.n + 2, cfg.nl)]
+            self.dt, self.scheme = cfg.dt, cfg.scheme
+            self.unit = "model-days/s"
+            self.metric = METRIC if name == "baroclinic3_128" else f"QG model-days/sec per GB300 ({name})"
+            self.describe = (f"{name}: {cfg.nl}-layer {cfg.n}x{cfg.n} double gyre (Lx=Ly=5120 km), "
+                             f"{cfg.scheme} dt={cfg.dt:g}s")
+            self.ens = None
+        self.n_members = len(self.members)
+        self.steps_per_day = int(round(86400.0 / self.dt))
+        self.q = torch.tensor(self.q0, device=dev).reshape(-1)
+
+    def device_step(self):
+        self.plan.step(self.q, self.params, self.dt, self.steps_per_day, self.scheme)
+
+    def host_step(self, qh, out):
+        """The public API with host buffers: H2D, one model day, D2H."""
+        import somax_gb300 as sg
+
+        if self.ens is not None:
+            self.ens.step_host(qh, out, self.dt, self.steps_per_day, self.scheme)
+        else:
+            self.model.step(sg.BaroclinicQGState(q=qh.view(self.model.shape)), self.dt, self.steps_per_day,
+                            self.scheme, out=out.view(self.model.shape))
+
+    def cells(self):
+        return sum(nl * N * N for N, nl in self.members)
+
+    def gemm_flops_per_pass(self):
+        return sum(2.0 * nl * N ** 3 for N, nl in self.members)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -169,15 +266,12 @@ def main():
 
     from somax_gb300 import testcases as tc
 
-    cfg = tc.CONFIGS[args.config]
     if args.impl == "reference":
-        run_reference(args, cfg)
+        run_reference(args, tc.CONFIGS.get(args.config))
         return
 
     import torch
     import torch.distributed as dist
-
-    import somax_gb300 as sg
 
     world = _env_int("WORLD_SIZE", 1)
     rank = _env_int("RANK", 0)
@@ -187,19 +281,12 @@ def main():
     if world > 1:
         dist.init_process_group("nccl", device_id=dev)
 
-    model = sg.BaroclinicQG.create(**cfg.model_kwargs(), precision=args.precision, persistent=bool(args.persistent))
-    steps_per_day = int(round(86400.0 / cfg.dt))
-    q0 = tc.initial_pv(cfg, seed=rank).astype(np.float32)
-    q = torch.tensor(q0, device=dev)
-    plan = model.plan(dev)
-    pv = model._param_vector(dev)
+    W = Workload(args.config, args.precision, bool(args.persistent), dev, rank)
+    plan = W.plan
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
 
-    def device_step(qt):
-        plan.step(qt, pv, cfg.dt, steps_per_day, cfg.scheme)
-
     for _ in range(args.warmup):
-        device_step(q)
+        W.device_step()
     torch.cuda.synchronize()
 
     # ---- timed region: device-resident state ------------------------------------------
@@ -211,7 +298,7 @@ def main():
         for k in range(args.steps):
             flush.fill_(float(k))  # evict L2 between timed steps (outside the events)
             ev[k][0].record()
-            device_step(q)
+            W.device_step()
             ev[k][1].record()
         torch.cuda.synchronize()
     if world > 1:
@@ -222,80 +309,85 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
     dev_ms = float(t.item())
     ms_per_step = dev_ms / args.steps
-    value = world * args.steps / (dev_ms / 1000.0)
+    value = world * W.n_members * args.steps / (dev_ms / 1000.0)
     status = plan.status(dev)
 
     # ---- e2e: public API with pinned host buffers --------------------------------------
-    qh = torch.tensor(q0).pin_memory()
+    qh = torch.tensor(W.q0).reshape(-1).pin_memory()
     out = torch.empty_like(qh).pin_memory()
-    model.step(sg.BaroclinicQGState(q=qh), cfg.dt, steps_per_day, cfg.scheme, out=out)  # warm
+    W.host_step(qh, out)  # warm
     torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        model.step(sg.BaroclinicQGState(q=qh), cfg.dt, steps_per_day, cfg.scheme, out=out)
+        W.host_step(qh, out)
         torch.cuda.current_stream(dev).synchronize()
     e2e_s = time.perf_counter() - t0
     t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
     if world > 1:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    e2e_value = world * args.steps / float(t.item())
+    e2e_value = world * W.n_members * args.steps / float(t.item())
     qbytes = qh.numel() * 4
 
-    # ---- profiled pass: per-kernel-class event timing -----------------------------------
+    # ---- launches per bench step (graph / persistent replay counts every kernel) ---------
+    launches_per_day = plan.launches_per_call(W.steps_per_day, W.scheme)
+
+    # ---- profiled pass: per-kernel-class event timing (multi-launch path) ----------------
     plan.set_profiling(True)
-    device_step(q)
+    W.device_step()
     torch.cuda.synchronize()
-    stats = {k: plan.kernel_stats(k) for k in range(4)}
+    stats = {k: plan.kernel_stats(k) for k in range(5)}
     plan.set_profiling(False)
-    launches_per_day = sum(n for _, n in stats.values()) - stats[0][1]  # prep runs once per call
-    kern = {0: "prep", 1: "dst_gemm", 2: "rhs_stencil", 3: "other"}
+    kern = {0: "prep", 1: "dst_gemm", 2: "rhs_stencil", 3: "other", 4: "persistent"}
     dom = max(stats, key=lambda k: stats[k][0])
-    N = cfg.n + 2
-    nl = cfg.nl
-    cells = nl * N * N
     pk = peaks()
-    stages = {"heun": 2, "ssprk3": 3}[cfg.scheme]
-    if dom == 1:  # GEMM: 2 M N K flops per pass, M = nl N, N = K = N
-        flop = 2.0 * nl * N * N * N
+    stages = {"heun": 2, "ssprk3": 3}[W.scheme]
+    if dom == 1:
         avg_s = stats[1][0] / 1000.0 / stats[1][1]
-        achieved = flop / avg_s / 1e12
-        roof = {"bound": "tensor", "kernel": "dst_gemm", "achieved": achieved, "peak": pk["bf16_tflops"],
-                "unit": "TFLOP/s", "frac": achieved / pk["bf16_tflops"], "traffic": None,
-                "peak_src": pk["src"], "note": "GEMM passes are latency-bound at 130^2 (L2-resident)"}
+        achieved = W.gemm_flops_per_pass() / avg_s / 1e12
+        peak = pk["bf16_tflops"]
+        roof = {"bound": "tensor", "kernel": "dst_gemm", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": None, "peak_src": pk["src"],
+                "note": "achieved counts the algorithmic 2MNK of one DST pass (BF16x3 issues three products)"}
     else:
         # stencil in step mode: read y_s, psi_hat, y0 (stages > 0), write y_next and the
         # next-stage modal operand: (5 * stages - 1) / stages * 4 bytes per cell per layer
         bpc = 4.0 * (5 * stages - 1) / stages
-        avg_s = stats[dom][0] / 1000.0 / stats[dom][1]
-        achieved = bpc * cells / avg_s / 1e9
+        avg_s = stats[dom][0] / 1000.0 / max(stats[dom][1], 1)
+        achieved = bpc * W.cells() / avg_s / 1e9
         roof = {"bound": "hbm", "kernel": kern[dom], "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / pk["hbm_gbs"], "traffic": None, "peak_src": pk["src"]}
-    roof["kernel_ms"] = {kern[k]: {"total_ms": v[0], "launches": v[1]} for k, v in stats.items()}
+    roof["kernel_ms"] = {kern[k]: {"total_ms": v[0], "launches": v[1]} for k, v in stats.items() if v[1]}
 
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "metric": W.metric, "value": value, "unit": W.unit, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"{cfg.name}: {nl}-layer {cfg.n}x{cfg.n} double gyre (Lx=Ly=5120 km), "
-                               f"{cfg.scheme} dt={cfg.dt:g}s, {steps_per_day} steps = 1 model day per bench step",
-                   "precision": args.precision, "l2": "flushed between timed steps (256 MB write)",
-                   "replicas": "independent basin per rank" if world > 1 else "single basin",
+        "config": {"workload": W.describe + f", {W.steps_per_day} steps = 1 model day per bench step",
+                   "precision": args.precision, "persistent": bool(args.persistent),
+                   "l2": "flushed between timed steps (256 MB write)",
+                   "replicas": "independent basins per rank" if world > 1 else "one device",
                    "status": status},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": qbytes, "d2h_bytes_per_step": qbytes,
-                "api": "BaroclinicQG.step(state with pinned host q) -> qg_step"},
+        "e2e": {"value": e2e_value, "unit": W.unit, "h2d_bytes_per_step": qbytes, "d2h_bytes_per_step": qbytes,
+                "api": "BaroclinicQG.step / QGEnsemble.step_host with pinned host q -> qg_step"},
         "roofline": roof,
         "gpu_launches": launches_per_day * args.steps,
         "clocks": clk.summary(),
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = len(os.sched_getaffinity(0))
-        sample = 6
-        v, el = cpu_baseline(cfg, sample, threads)
-        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": f"{sample} {cfg.scheme} steps of {cfg.name}, float32 NumPy/SciPy "
-                                          f"restatement ({el:.2f} s)"}
+        if W.model is not None:
+            sample = 6
+            cfg = tc.CONFIGS[args.config]
+            v, el = cpu_baseline(cfg, sample, threads)
+            line["cpu_baseline"] = {"value": v, "unit": W.unit, "cores": threads, "kind": "port",
+                                    "sample": f"{sample} {cfg.scheme} steps of {cfg.name}, float32 NumPy/SciPy "
+                                              f"restatement ({el:.2f} s)"}
+        else:
+            v = ensemble_cpu_rate(threads, 1)
+            line["cpu_baseline"] = {"value": v, "unit": W.unit, "cores": threads, "kind": "port",
+                                    "sample": "1 step of one member per class, count-weighted, float32 NumPy/SciPy"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -24,7 +24,9 @@ namespace {
 constexpr int NTHREADS = 192;
 
 template <int PREC>
-__host__ __device__ constexpr int smem_bytes() { return TcCfg<PREC>::STAGES * tc_stage_bytes<PREC>() + 1024; }
+__host__ __device__ constexpr int smem_bytes() {
+    return TcCfg<PREC>::STAGES * tc_stage_bytes<PREC>() + TC_EPI_SMEM + 1024;
+}
 
 template <int PREC, int PASS>
 __global__ void __launch_bounds__(NTHREADS, 1) k_gemm_tc(GemmArgs ga, const TcMaps* __restrict__ maps) {
@@ -103,7 +105,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_gemm_tc(GemmArgs ga, const TcMa
         // the MMAs in flight before TMEM is read and freed
         const bool have = mbar_drain(&acc_bar, 0) && !*abort;
         tc_fence_after();
-        tc_epilogue<PASS>(M, g, ga.C, ga.c_fmt, ga.accumulate, m0, n0, tmem, warp & 3, lane, have);
+        float* stage = reinterpret_cast<float*>(smem + C::STAGES * tc_stage_bytes<PREC>()) + (warp - 2) * TC_STAGE_FLOATS;
+        tc_epilogue<PASS>(M, g, ga.C, ga.c_fmt, ga.accumulate, m0, n0, tmem, warp & 3, lane, have, stage);
     }
     tc_fence_before();
     __syncthreads();

@@ -95,12 +95,13 @@ struct PrepArgs {
     int xa_fmt;
     float* xq;             // FP32 Cl2m q for the refinement residual (may be null)
     int64_t xplane;
+    int tile_x, tile_y;    // cells per tile of the tile list
 };
 
 // TMA descriptors of one member for the stencil: the three stage planes and psi_hat,
 // 3-D boxes (x, y, layer) over the padded x-row planes.
 constexpr int kStencilMapsBytes = 4 * 128;
-cudaError_t stencil_encode_maps(const MemberDev& M, const float* const planes[4], void* out);
+cudaError_t stencil_encode_maps(const MemberDev& M, const float* const planes[4], int large, void* out);
 
 struct StencilArgs {
     const MemberDev* members;
@@ -125,18 +126,18 @@ struct StencilArgs {
 
 // launchers (return cudaError_t of the launch)
 cudaError_t launch_prep(const PrepArgs& a, int ntiles, cudaStream_t s, bool pdl);
-cudaError_t launch_unpack(const MemberDev* members, const StencilTile* tiles, int ntiles, const float* src,
-                          float* q, cudaStream_t s, bool pdl);
-cudaError_t launch_stencil(const StencilArgs& a, int ntiles, int max_nl, cudaStream_t s, bool pdl);
-size_t stencil_smem_bytes(int max_nl);
-cudaError_t launch_mode_to_layer(const MemberDev* members, const StencilTile* tiles, int ntiles,
+cudaError_t launch_unpack(const MemberDev* members, const StencilTile* tiles, int ntiles, int large,
+                          const float* src, float* q, cudaStream_t s, bool pdl);
+cudaError_t launch_stencil(const StencilArgs& a, int ntiles, int max_nl, int large, cudaStream_t s, bool pdl);
+size_t stencil_smem_bytes(int max_nl, int large);
+cudaError_t launch_mode_to_layer(const MemberDev* members, const StencilTile* tiles, int ntiles, int large,
                                  const float* psi_hat, float* psi, cudaStream_t s, bool pdl);
-cudaError_t launch_diag_acc(const MemberDev* members, const StencilTile* tiles, int ntiles,
+cudaError_t launch_diag_acc(const MemberDev* members, const StencilTile* tiles, int ntiles, int large,
                             const float* q, const float* psi_hat, double* acc, cudaStream_t s);
 cudaError_t launch_diag_finish(const double* acc, int64_t n_layers, float* ke, float* ens,
                                cudaStream_t s);
 void stencil_init();
-cudaError_t launch_residual(const MemberDev* members, const StencilTile* tiles, int ntiles,
+cudaError_t launch_residual(const MemberDev* members, const StencilTile* tiles, int ntiles, int large,
                             const float* qm, const float* psi_hat, void* out, int out_fmt,
                             int64_t xplane, cudaStream_t s, bool pdl);
 
@@ -172,7 +173,10 @@ struct PersistArgs {
     float* S[3];              // stage planes (S[0] = state)
     const float* params;
     int64_t xplane, yplane;
-    size_t slot_bytes;        // one stencil box buffer
+    size_t slot_bytes;        // one stencil box buffer (q and psi boxes)
+    size_t lap_offset;        // shared-memory offset of the lap(q) buffer
+    int st_nbuf;              // stencil box buffers (2: next tile loads during compute)
+    int st_large;             // stencil tile shape: 0 = 32 x 8, 1 = 64 x 16
     int op_fmt;
     int n_stages, n_steps;
     float sa[4], sb[4], dt;   // Shu-Osher stage coefficients
@@ -180,7 +184,7 @@ struct PersistArgs {
     unsigned* bar_count;      // grid barrier: arrivals, generation
     unsigned* bar_gen;
 };
-size_t persistent_smem_bytes(int precision, int max_nl, size_t* slot_bytes);
+size_t persistent_smem_bytes(int precision, int max_nl, int large, PersistArgs* a);
 cudaError_t persistent_init();
 cudaError_t launch_persistent(const PersistArgs& a, int grid, int precision, cudaStream_t s);  // 4 CUtensorMap per (member, pass)
 cudaError_t gemm_tc_encode(const MemberDev& M, int pass, const void* a_plane, int64_t a_plane_elems, int prec,
@@ -193,8 +197,8 @@ int validate_member(const qg_member_desc& d);
 void member_constants(const qg_member_desc& d, MemberDev& M, double* Cl2m, double* Cm2l, double* lam);
 int round_up(int v, int m);
 
-constexpr int kStencilTX = 64;
-constexpr int kStencilTY = 16;
+// stencil tile shapes (cells): small grids use 32 x 8, large ones 64 x 16
+constexpr int kTileSX = 32, kTileSY = 8, kTileLX = 64, kTileLY = 16;
 constexpr int kSimtBM = 64;
 constexpr int kSimtBN = 64;
 

@@ -149,8 +149,9 @@ __device__ void gemm_phase(const PersistArgs& a, uint8_t* smem, Shared& sh, uint
             const bool have = mbar_wait(&sh.tfull[buf], use & 1, abort);
             if (!have) break;
             tc_fence_after();
+            float* stage = reinterpret_cast<float*>(smem + C::STAGES * tc_stage_bytes<PREC>()) + (warp - 4) * TC_STAGE_FLOATS;
             tc_epilogue<PASS>(M, g, Cv, c_fmt, 0, tl.mt * TC_BM, tl.nt * TC_BN, tmem + buf * TC_BN, warp & 3, lane,
-                              true);
+                              true, stage);
             tc_fence_before();
             mbar_arrive(&sh.tempty[buf]);
             ++c.epi_tiles;
@@ -158,9 +159,10 @@ __device__ void gemm_phase(const PersistArgs& a, uint8_t* smem, Shared& sh, uint
     }
 }
 
-// Stencil phase of stage `k`: tiles round-robin, double-buffered TMA boxes.
-__device__ void stencil_phase(const PersistArgs& a, int k, uint8_t* smem, size_t slot_bytes, Shared& sh,
-                              Counters& c) {
+// Stencil phase of stage `k`: tiles round-robin; with two box buffers the next tile's TMA
+// copies run while the current tile is computed.
+template <class T>
+__device__ void stencil_phase(const PersistArgs& a, int k, uint8_t* smem, Shared& sh, Counters& c) {
     using namespace st;
     const StencilMaps* maps = static_cast<const StencilMaps*>(a.st_maps);
     const bool fin = (k == a.n_stages - 1);
@@ -182,45 +184,50 @@ __device__ void stencil_phase(const PersistArgs& a, int k, uint8_t* smem, size_t
     sa.xa_fmt = a.op_fmt;
     sa.xq = nullptr;
     sa.flags = a.flags;
+    float* sl = reinterpret_cast<float*>(smem + a.lap_offset);
+    const int nbuf = a.st_nbuf;
 
     auto issue = [&](int t, int b) {
         const StencilTile tl = a.st[t];
         const int nl = a.members[tl.member].nl;
-        float* sq = reinterpret_cast<float*>(smem + b * slot_bytes);
-        float* sp = sq + nl * BOX;
-        proxy_fence_shared();  // generic reads of this buffer finished before TMA rewrites it
-        mbar_expect_tx(&sh.sbar[b], (uint32_t)(2 * nl * BOX * sizeof(float)));
-        tma_load_3d(sq, &maps[tl.member].q[k], &sh.sbar[b], tl.tx * TX - 4, tl.ty * TY - 2, 0);
-        tma_load_3d(sp, &maps[tl.member].psi, &sh.sbar[b], tl.tx * TX - 4, tl.ty * TY - 2, 0);
+        float* sq = reinterpret_cast<float*>(smem + b * a.slot_bytes);
+        proxy_fence_shared();  // generic accesses of this buffer finished before TMA rewrites it
+        tile_issue<T>(&maps[tl.member], k, nl, tl.ty, tl.tx, sq, sq + nl * T::BOX, &sh.sbar[b]);
     };
-    if (threadIdx.x == 0 && (int)blockIdx.x < a.n_st) issue(blockIdx.x, 0);
+    if (nbuf == 2 && threadIdx.x == 0 && (int)blockIdx.x < a.n_st) issue(blockIdx.x, 0);
     bool bad = false;
     for (int u = 0;; ++u) {
         const int t = blockIdx.x + u * gridDim.x;
         if (t >= a.n_st || sh.abort) break;
-        const int b = u & 1;
-        const int tn = t + gridDim.x;
-        if (threadIdx.x == 0 && tn < a.n_st) issue(tn, b ^ 1);
+        const int b = nbuf == 2 ? (u & 1) : 0;
+        if (threadIdx.x == 0) {
+            if (nbuf == 1) {
+                issue(t, 0);
+            } else if (t + (int)gridDim.x < a.n_st) {
+                issue(t + gridDim.x, b ^ 1);
+            }
+        }
         const StencilTile tl = a.st[t];
         load_member(&sh.M, a.members + tl.member);
+        const bool need_lap = a.params[(int64_t)tl.member * QG_NPARAMS + QG_P_NU4] != 0.f;
         __syncthreads();
         const bool have = mbar_wait(&sh.sbar[b], c.st_use[b] & 1, &sh.abort);
         ++c.st_use[b];
-        float* sq = reinterpret_cast<float*>(smem + b * slot_bytes);
-        float* sp = sq + sh.M.nl * BOX;
-        stencil_fix_box(sh.M, sq, sp, tl.ty * TY - 2, tl.tx * TX - 4, 1);
+        float* sq = reinterpret_cast<float*>(smem + b * a.slot_bytes);
+        float* sp = sq + sh.M.nl * T::BOX;
+        stencil_fix_box<T>(sh.M, sq, sp, sl, tl.ty, tl.tx, 1, need_lap);
         __syncthreads();
-        bad |= stencil_compute(sa, sh.M, tl, sq, sp) || !have;
+        bad |= stencil_compute<T>(sa, sh.M, tl, sq, sp, sl) || !have;
         __syncthreads();
     }
     if (bad && a.flags) atomicOr(a.flags, 1);
     // a prefetch issued for a tile beyond an abort is drained before the buffers are reused
     if (sh.abort && threadIdx.x == 0) {
-        for (int b = 0; b < 2; ++b) mbar_drain(&sh.sbar[b], c.st_use[b] & 1);
+        for (int b = 0; b < nbuf; ++b) mbar_drain(&sh.sbar[b], c.st_use[b] & 1);
     }
 }
 
-template <int PREC>
+template <int PREC, class T>
 __global__ void __launch_bounds__(PT, 1) k_persistent(PersistArgs a) {
     using C = TcCfg<PREC>;
     extern __shared__ uint8_t smem_raw[];
@@ -259,7 +266,7 @@ __global__ void __launch_bounds__(PT, 1) k_persistent(PersistArgs a) {
             if (!grid_sync(a.bar_count, a.bar_gen, a.flags, abort)) goto done;
             gemm_phase<PREC, G4_INV_X>(a, smem, sh, tmem, c);
             if (!grid_sync(a.bar_count, a.bar_gen, a.flags, abort)) goto done;
-            stencil_phase(a, k, smem, a.slot_bytes, sh, c);
+            stencil_phase<T>(a, k, smem, sh, c);
             if (!grid_sync(a.bar_count, a.bar_gen, a.flags, abort)) goto done;
         }
     }
@@ -284,19 +291,39 @@ done:
 
 }  // namespace
 
-size_t persistent_smem_bytes(int precision, int max_nl, size_t* slot_bytes) {
-    const size_t slot = ((size_t)2 * max_nl * st::BOX * sizeof(float) + 1023) & ~size_t(1023);
-    const size_t gemm = precision == QG_DST_TF32 ? (size_t)TcCfg<QG_DST_TF32>::STAGES * tc_stage_bytes<QG_DST_TF32>()
-                                                 : (size_t)TcCfg<QG_DST_BF16X3>::STAGES * tc_stage_bytes<QG_DST_BF16X3>();
-    if (slot_bytes) *slot_bytes = slot;
-    return std::max(gemm, 2 * slot) + 1024;
+template <class T>
+size_t stencil_layout(int max_nl, PersistArgs* a) {
+    const size_t budget = 228 * 1024;  // dynamic shared memory left beside the static part
+    const size_t slot = (st::tile_box_bytes<T>(max_nl) + 1023) & ~size_t(1023);
+    const size_t lap = (st::tile_lap_bytes<T>(max_nl) + 1023) & ~size_t(1023);
+    const int nbuf = (2 * slot + lap <= budget) ? 2 : 1;
+    if (a) {
+        a->slot_bytes = slot;
+        a->lap_offset = nbuf * slot;
+        a->st_nbuf = nbuf;
+    }
+    return nbuf * slot + lap;
+}
+
+size_t persistent_smem_bytes(int precision, int max_nl, int large, PersistArgs* a) {
+    const size_t gemm = (precision == QG_DST_TF32 ? (size_t)TcCfg<QG_DST_TF32>::STAGES * tc_stage_bytes<QG_DST_TF32>()
+                                                  : (size_t)TcCfg<QG_DST_BF16X3>::STAGES * tc_stage_bytes<QG_DST_BF16X3>()) +
+                        TC_EPI_SMEM;
+    const size_t sten = large ? stencil_layout<st::TileL>(max_nl, a) : stencil_layout<st::TileS>(max_nl, a);
+    return std::max(gemm, sten) + 1024;
 }
 
 cudaError_t persistent_init() {
-    const int tf = (int)persistent_smem_bytes(QG_DST_TF32, kMaxLayers, nullptr);
-    const int bf = (int)persistent_smem_bytes(QG_DST_BF16X3, kMaxLayers, nullptr);
-    cudaError_t e = cudaFuncSetAttribute(k_persistent<QG_DST_TF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, tf);
-    if (!e) e = cudaFuncSetAttribute(k_persistent<QG_DST_BF16X3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bf);
+    cudaError_t e = cudaSuccess;
+#define QG_PATTR(P, T, L)                                                                                      \
+    if (!e)                                                                                                    \
+        e = cudaFuncSetAttribute(k_persistent<P, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,              \
+                                 (int)persistent_smem_bytes(P, kMaxLayers, L, nullptr));
+    QG_PATTR(QG_DST_TF32, st::TileS, 0)
+    QG_PATTR(QG_DST_TF32, st::TileL, 1)
+    QG_PATTR(QG_DST_BF16X3, st::TileS, 0)
+    QG_PATTR(QG_DST_BF16X3, st::TileL, 1)
+#undef QG_PATTR
     return e;
 }
 
@@ -304,15 +331,19 @@ cudaError_t launch_persistent(const PersistArgs& a, int grid, int precision, cud
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);
     cfg.blockDim = dim3(PT);
-    cfg.dynamicSmemBytes = persistent_smem_bytes(precision, a.max_nl, nullptr);
+    cfg.dynamicSmemBytes = persistent_smem_bytes(precision, a.max_nl, a.st_large, nullptr);
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;  // all CTAs co-resident: the grid barrier needs it
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    if (precision == QG_DST_TF32) return cudaLaunchKernelEx(&cfg, k_persistent<QG_DST_TF32>, a);
-    if (precision == QG_DST_BF16X3) return cudaLaunchKernelEx(&cfg, k_persistent<QG_DST_BF16X3>, a);
+    if (precision == QG_DST_TF32)
+        return a.st_large ? cudaLaunchKernelEx(&cfg, k_persistent<QG_DST_TF32, st::TileL>, a)
+                          : cudaLaunchKernelEx(&cfg, k_persistent<QG_DST_TF32, st::TileS>, a);
+    if (precision == QG_DST_BF16X3)
+        return a.st_large ? cudaLaunchKernelEx(&cfg, k_persistent<QG_DST_BF16X3, st::TileL>, a)
+                          : cudaLaunchKernelEx(&cfg, k_persistent<QG_DST_BF16X3, st::TileS>, a);
     return cudaErrorInvalidValue;
 }
 

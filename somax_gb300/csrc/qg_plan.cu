@@ -242,6 +242,7 @@ struct qg_plan {
     void* st_maps = nullptr;  // TMA descriptors of the stencil halo boxes
     unsigned* bar = nullptr;  // grid barrier words of the persistent kernel (count, generation)
     int n_sm = 0;
+    int st_large = 0;         // stencil tile shape: 0 = 32 x 8, 1 = 64 x 16
     // graphs
     cudaStream_t cap = nullptr;
     StepGraph graph;
@@ -342,7 +343,8 @@ cudaError_t run_dst_solve(qg_plan* p, cudaStream_t s) {
     if ((e = run_gemm(p, gemm_args(p, G4_INV_X, p->XB, p->XC, f, FMT_F32, 0), s))) return e;
     for (int r = 0; r < p->opts.refine_sweeps; ++r) {
         e = timed(p, QG_K_OTHER, s, [&] {
-            return launch_residual(p->md, p->st_tiles, p->n_st, p->XQ, p->XC, p->XA, f, p->xplane, s, use_pdl(p));
+            return launch_residual(p->md, p->st_tiles, p->n_st, p->st_large, p->XQ, p->XC, p->XA, f, p->xplane, s,
+                                   use_pdl(p));
         });
         if (e) return e;
         if ((e = run_gemm(p, gemm_args(p, G1_FWD_X, p->XA, p->YA, f, f, 0), s))) return e;
@@ -367,6 +369,8 @@ cudaError_t run_prep(qg_plan* p, const float* q, float* copy, int zero_ring_copy
     a.xa_fmt = p->op_fmt;
     a.xq = p->XQ;
     a.xplane = p->xplane;
+    a.tile_x = p->st_large ? kTileLX : kTileSX;
+    a.tile_y = p->st_large ? kTileLY : kTileSY;
     return timed(p, QG_K_PREP, s, [&] { return launch_prep(a, p->n_st, s, use_pdl(p)); });
 }
 
@@ -424,7 +428,7 @@ cudaError_t run_one_step(qg_plan* p, const float* params, float dt, int scheme, 
         a.dt = dt;
         a.xa = p->XA;
         a.xq = p->XQ;
-        e = timed(p, QG_K_STENCIL, s, [&] { return launch_stencil(a, p->n_st, p->max_nl, s, use_pdl(p)); });
+        e = timed(p, QG_K_STENCIL, s, [&] { return launch_stencil(a, p->n_st, p->max_nl, p->st_large, s, use_pdl(p)); });
         if (e) return e;
     }
     return cudaSuccess;
@@ -506,7 +510,16 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
         }
         p->op_fmt = (o.dst_precision == QG_DST_BF16X3) ? FMT_BF16X2 : FMT_F32;
     }
-    cudaError_t e = cudaSuccess;
+    cudaError_t e = cudaDeviceGetAttribute(&p->n_sm, cudaDevAttrMultiProcessorCount, p->device);
+    {
+        // stencil tile shape: the large tile once it still gives every SM two tiles per stage
+        int64_t large_tiles = 0;
+        for (int i = 0; i < n_members; ++i)
+            large_tiles += (int64_t)((members[i].ny + 2 + kTileLY - 1) / kTileLY) *
+                           ((members[i].nx + 2 + kTileLX - 1) / kTileLX);
+        p->st_large = large_tiles >= 2 * (int64_t)std::max(p->n_sm, 1);
+    }
+    const int TX = p->st_large ? kTileLX : kTileSX, TY = p->st_large ? kTileLY : kTileSY;
     // geometry and offsets
     p->mh.resize(n_members);
     int64_t off_state = 0, off_x = 0, off_y = 0, off_layer = 0;
@@ -586,8 +599,8 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
             M.Sy_bf = byy;
         }
         // tiles
-        for (int ty = 0; ty < (M.Ny + kStencilTY - 1) / kStencilTY; ++ty)
-            for (int tx = 0; tx < (M.Nx + kStencilTX - 1) / kStencilTX; ++tx) st.push_back({i, ty, tx});
+        for (int ty = 0; ty < (M.Ny + TY - 1) / TY; ++ty)
+            for (int tx = 0; tx < (M.Nx + TX - 1) / TX; ++tx) st.push_back({i, ty, tx});
         for (int mt = 0; mt < (n * M.Ny + BMg - 1) / BMg; ++mt)
             for (int nt = 0; nt < (M.Nx + BNg - 1) / BNg; ++nt) gx.push_back({i, mt, nt});
         for (int mt = 0; mt < (n * M.Nx + BMg - 1) / BMg; ++mt)
@@ -634,10 +647,9 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
         std::vector<uint8_t> maps((size_t)n_members * kStencilMapsBytes);
         const float* planes[4] = {p->S0, p->S1, p->S2, p->XC};
         for (int i = 0; i < n_members && !e; ++i)
-            e = stencil_encode_maps(p->mh[i], planes, maps.data() + (size_t)i * kStencilMapsBytes);
+            e = stencil_encode_maps(p->mh[i], planes, p->st_large, maps.data() + (size_t)i * kStencilMapsBytes);
         if (!e) e = upload(p, (uint8_t**)&p->st_maps, maps);
     }
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&p->n_sm, cudaDevAttrMultiProcessorCount, p->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
@@ -687,7 +699,7 @@ int qg_invert(qg_plan* p, const float* q, float* psi, void* stream) {
     if (!e) e = run_dst_solve(p, s);
     if (!e)
         e = timed(p, QG_K_OTHER, s, [&] {
-            return launch_mode_to_layer(p->md, p->st_tiles, p->n_st, p->XC, psi, s, use_pdl(p));
+            return launch_mode_to_layer(p->md, p->st_tiles, p->n_st, p->st_large, p->XC, psi, s, use_pdl(p));
         });
     return cuda_err(e);
 }
@@ -705,7 +717,7 @@ int qg_rhs(qg_plan* p, const float* q, float* dq, const float* params, int flags
         a.q_sel = 1;
         a.apply_bc = bc;
         a.dq = dq;
-        e = timed(p, QG_K_STENCIL, s, [&] { return launch_stencil(a, p->n_st, p->max_nl, s, use_pdl(p)); });
+        e = timed(p, QG_K_STENCIL, s, [&] { return launch_stencil(a, p->n_st, p->max_nl, p->st_large, s, use_pdl(p)); });
     }
     return cuda_err(e);
 }
@@ -724,7 +736,9 @@ int qg_step(qg_plan* p, float* q, const float* params, double dt, int n_steps, i
     // integration (integrate() applies the BC to state0), stage inputs always read a zero ring
     if (!e) e = run_prep(p, q, p->S0, (flags & QG_STEP_APPLY_BC) ? 1 : 0, 1, s);
     if (e) return cuda_err(e);
-    const bool persistent = p->opts.persistent && p->opts.dst_precision != QG_DST_FP32 && p->opts.refine_sweeps == 0;
+    // while profiling, the multi-launch path runs so that every kernel class gets its events
+    const bool persistent = p->opts.persistent && p->opts.dst_precision != QG_DST_FP32 &&
+                            p->opts.refine_sweeps == 0 && !p->profiling;
     const bool use_graph = p->opts.use_graphs && !p->profiling;
     if (persistent && n_steps > 0) {
         PersistArgs a{};
@@ -749,7 +763,8 @@ int qg_step(qg_plan* p, float* q, const float* params, double dt, int n_steps, i
         a.params = p->params;
         a.xplane = p->xplane;
         a.yplane = p->yplane;
-        persistent_smem_bytes(p->opts.dst_precision, p->max_nl, &a.slot_bytes);
+        a.st_large = p->st_large;
+        persistent_smem_bytes(p->opts.dst_precision, p->max_nl, p->st_large, &a);
         a.op_fmt = p->op_fmt;
         a.n_stages = scheme_stages(scheme, st);
         for (int k = 0; k < a.n_stages; ++k) {
@@ -792,7 +807,7 @@ int qg_step(qg_plan* p, float* q, const float* params, double dt, int n_steps, i
     }
     if (!e)
         e = timed(p, QG_K_OTHER, s, [&] {
-            return launch_unpack(p->md, p->st_tiles, p->n_st, p->S0, q, s, use_pdl(p));
+            return launch_unpack(p->md, p->st_tiles, p->n_st, p->st_large, p->S0, q, s, use_pdl(p));
         });
     return cuda_err(e);
 }
@@ -805,7 +820,7 @@ int qg_diagnose(qg_plan* p, const float* q, float* ke, float* ens, void* stream)
     if (!e) e = cudaMemsetAsync(p->diag_acc, 0, sizeof(double) * 2 * p->total_layers, s);
     if (!e)
         e = timed(p, QG_K_OTHER, s, [&] {
-            return launch_diag_acc(p->md, p->st_tiles, p->n_st, q, p->XC, p->diag_acc, s);
+            return launch_diag_acc(p->md, p->st_tiles, p->n_st, p->st_large, q, p->XC, p->diag_acc, s);
         });
     if (!e) e = launch_diag_finish(p->diag_acc, p->total_layers, ke, ens, s);
     return cuda_err(e);

@@ -130,7 +130,7 @@ extern "C" int qg_invert_static(const qg_member_desc* member, const float* q, fl
     const int Px = round_up(Nx, 32), Py = round_up(Ny, 32);
     if (Nx > kStaticMaxN || Ny > kStaticMaxN) return QG_ERR_TOO_LARGE;
     if ((int64_t)nl * Ny * Px > kStaticPlane || (int64_t)nl * Nx * Py > kStaticPlane) return QG_ERR_TOO_LARGE;
-    const int st_ty = (Ny + kStencilTY - 1) / kStencilTY, st_tx = (Nx + kStencilTX - 1) / kStencilTX;
+    const int st_ty = (Ny + kTileSY - 1) / kTileSY, st_tx = (Nx + kTileSX - 1) / kTileSX;
     const int gx_mt = (nl * Ny + kSimtBM - 1) / kSimtBM, gx_nt = (Nx + kSimtBN - 1) / kSimtBN;
     const int gy_mt = (nl * Nx + kSimtBM - 1) / kSimtBM, gy_nt = (Ny + kSimtBN - 1) / kSimtBN;
     const int n_st = st_ty * st_tx, n_gx = gx_mt * gx_nt, n_gy = gy_mt * gy_nt;
@@ -169,6 +169,8 @@ extern "C" int qg_invert_static(const qg_member_desc* member, const float* q, fl
         pa.xa = P0;
         pa.xa_fmt = FMT_F32;
         pa.xplane = kStaticPlane;
+        pa.tile_x = kTileSX;
+        pa.tile_y = kTileSY;
         e = launch_prep(pa, n_st, s, false);
     }
     auto gemm = [&](int pass, const float* A, float* C, const GemmTile* tl, int nt) {
@@ -186,6 +188,6 @@ extern "C" int qg_invert_static(const qg_member_desc* member, const float* q, fl
     if (!e) e = gemm(G2_FWD_Y, P1, P2, gy, n_gy);
     if (!e) e = gemm(G3_INV_Y, P2, P0, gy, n_gy);
     if (!e) e = gemm(G4_INV_X, P0, P1, gx, n_gx);
-    if (!e) e = launch_mode_to_layer(md, st, n_st, P1, psi, s, false);
+    if (!e) e = launch_mode_to_layer(md, st, n_st, 0, P1, psi, s, false);
     return e == cudaSuccess ? QG_OK : QG_ERR_CUDA;
 }

@@ -24,6 +24,7 @@ using namespace st;
 __global__ void __launch_bounds__(NTHREADS) k_prep(PrepArgs a) {
     __shared__ MemberDev M;
     const StencilTile t = a.tiles[blockIdx.x];
+    const int TX = a.tile_x, TY = a.tile_y;
     load_member(&M, a.members + t.member);
     __syncthreads();
     pdl_wait();
@@ -51,7 +52,7 @@ __global__ void __launch_bounds__(NTHREADS) k_prep(PrepArgs a) {
 
 // Unpack: internal plane -> caller packing (every cell, ring included).
 __global__ void __launch_bounds__(NTHREADS) k_unpack(const MemberDev* __restrict__ members,
-                                                     const StencilTile* __restrict__ tiles,
+                                                     const StencilTile* __restrict__ tiles, int TX, int TY,
                                                      const float* __restrict__ src, float* __restrict__ q) {
     __shared__ MemberDev M;
     const StencilTile t = tiles[blockIdx.x];
@@ -79,6 +80,7 @@ __global__ void __launch_bounds__(NTHREADS) k_unpack(const MemberDev* __restrict
 // outside the array).  Step mode fuses the Shu-Osher stage update
 // y_next = a y0 + b (y_s + dt dq) and the next stage's layer->mode prologue.
 // ---------------------------------------------------------------------------------------
+template <class T>
 __global__ void __launch_bounds__(NTHREADS) k_stencil(StencilArgs a) {
     extern __shared__ uint8_t smem_raw[];
     float* smem = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
@@ -100,18 +102,15 @@ __global__ void __launch_bounds__(NTHREADS) k_stencil(StencilArgs a) {
     pdl_launch_dependents();
 
     const int nl = M.nl;
-    float* sq = smem;              // [nl][BY][BX] q, then BC applied
-    float* sp = smem + nl * BOX;   // [nl][BY][BX] psi_hat, mixed in place to psi
-    const int j0 = t.ty * TY - 2, i0 = t.tx * TX - 4;
-    if (threadIdx.x == 0) {
-        mbar_expect_tx(&bar, (uint32_t)(2 * nl * BOX * sizeof(float)));
-        tma_load_3d(sq, &maps->q[a.q_sel], &bar, i0, j0, 0);
-        tma_load_3d(sp, &maps->psi, &bar, i0, j0, 0);
-    }
+    float* sq = smem;                      // [nl][BY][BX] q, then BC applied
+    float* sp = smem + nl * T::BOX;        // [nl][BY][BX] psi_hat, mixed in place to psi
+    float* sl = smem + 2 * nl * T::BOX;    // [nl][BY][BX] lap(q)
+    if (threadIdx.x == 0) tile_issue<T>(maps, a.q_sel, nl, t.ty, t.tx, sq, sp, &bar);
+    const bool need_lap = a.params[(int64_t)t.member * QG_NPARAMS + QG_P_NU4] != 0.f;
     const bool have = mbar_wait(&bar, 0, &abort_flag);
-    stencil_fix_box(M, sq, sp, j0, i0, a.apply_bc);
+    stencil_fix_box<T>(M, sq, sp, sl, t.ty, t.tx, a.apply_bc, need_lap);
     __syncthreads();
-    const bool bad = stencil_compute(a, M, t, sq, sp) || !have;
+    const bool bad = stencil_compute<T>(a, M, t, sq, sp, sl) || !have;
     if (bad && a.flags) atomicOr(a.flags, have ? 1 : 2);
 }
 
@@ -119,7 +118,7 @@ __global__ void __launch_bounds__(NTHREADS) k_stencil(StencilArgs a) {
 // Mode -> layer epilogue for qg_invert: psi = Cm2l psi_hat, ring zeroed (baroclinic).
 // ---------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(NTHREADS) k_mode_to_layer(const MemberDev* __restrict__ members,
-                                                            const StencilTile* __restrict__ tiles,
+                                                            const StencilTile* __restrict__ tiles, int TX, int TY,
                                                             const float* __restrict__ psi_hat,
                                                             float* __restrict__ psi) {
     __shared__ MemberDev M;
@@ -150,7 +149,7 @@ __global__ void __launch_bounds__(NTHREADS) k_mode_to_layer(const MemberDev* __r
 // operator the DST-I solve inverts).  qm is the FP32 modal right-hand side.
 // ---------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(NTHREADS) k_residual(const MemberDev* __restrict__ members,
-                                                       const StencilTile* __restrict__ tiles,
+                                                       const StencilTile* __restrict__ tiles, int TX, int TY,
                                                        const float* __restrict__ qm,
                                                        const float* __restrict__ psi_hat,
                                                        void* out, int out_fmt, int64_t xplane) {
@@ -183,7 +182,7 @@ __global__ void __launch_bounds__(NTHREADS) k_residual(const MemberDev* __restri
 // both interior-written and averaged back to T points.  Sums accumulate in double.
 // ---------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(NTHREADS) k_diag(const MemberDev* __restrict__ members,
-                                                   const StencilTile* __restrict__ tiles,
+                                                   const StencilTile* __restrict__ tiles, int TX, int TY,
                                                    const float* __restrict__ q,
                                                    const float* __restrict__ psi_hat,
                                                    double* __restrict__ acc) {
@@ -263,15 +262,19 @@ __global__ void k_diag_finish(const double* __restrict__ acc, int64_t n, float* 
 // ---------------------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------------------
-size_t stencil_smem_bytes(int max_nl) { return (size_t)2 * max_nl * BOX * sizeof(float) + 128; }
+size_t stencil_smem_bytes(int max_nl, int large) {
+    return (large ? tile_box_bytes<TileL>(max_nl) + tile_lap_bytes<TileL>(max_nl)
+                  : tile_box_bytes<TileS>(max_nl) + tile_lap_bytes<TileS>(max_nl)) + 128;
+}
 
 // 3-D boxes (BX, BY, nl) over a member's x-row planes: dims (Nx, Ny, nl), row pitch Px.
-cudaError_t stencil_encode_maps(const MemberDev& M, const float* const planes[4], void* out) {
+cudaError_t stencil_encode_maps(const MemberDev& M, const float* const planes[4], int large, void* out) {
     StencilMaps sm;
     memset(&sm, 0, sizeof(sm));
     const uint64_t dims[3] = {(uint64_t)M.Nx, (uint64_t)M.Ny, (uint64_t)M.nl};
     const uint64_t strides[2] = {(uint64_t)M.Px * 4, (uint64_t)M.Px * M.Ny * 4};
-    const uint32_t box[3] = {(uint32_t)BX, (uint32_t)BY, (uint32_t)M.nl};
+    const uint32_t box[3] = {(uint32_t)(large ? TileL::BX : TileS::BX), (uint32_t)(large ? TileL::BY : TileS::BY),
+                             (uint32_t)M.nl};
     cudaError_t e = cudaSuccess;
     for (int k = 0; k < 4 && !e; ++k) {
         CUtensorMap* m = k < 3 ? &sm.q[k] : &sm.psi;
@@ -282,37 +285,44 @@ cudaError_t stencil_encode_maps(const MemberDev& M, const float* const planes[4]
 }
 
 void stencil_init() {
-    cudaFuncSetAttribute(k_stencil, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)stencil_smem_bytes(kMaxLayers));
+    cudaFuncSetAttribute(k_stencil<TileS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)stencil_smem_bytes(kMaxLayers, 0));
+    cudaFuncSetAttribute(k_stencil<TileL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)stencil_smem_bytes(kMaxLayers, 1));
 }
 
 cudaError_t launch_prep(const PrepArgs& a, int ntiles, cudaStream_t s, bool pdl) {
     return launch_k(k_prep, ntiles, NTHREADS, 0, s, pdl, a);
 }
 
-cudaError_t launch_unpack(const MemberDev* members, const StencilTile* tiles, int ntiles, const float* src,
-                          float* q, cudaStream_t s, bool pdl) {
-    return launch_k(k_unpack, ntiles, NTHREADS, 0, s, pdl, members, tiles, src, q);
+cudaError_t launch_unpack(const MemberDev* members, const StencilTile* tiles, int ntiles, int large,
+                          const float* src, float* q, cudaStream_t s, bool pdl) {
+    return launch_k(k_unpack, ntiles, NTHREADS, 0, s, pdl, members, tiles, large ? TileL::TX : TileS::TX,
+                    large ? TileL::TY : TileS::TY, src, q);
 }
 
-cudaError_t launch_stencil(const StencilArgs& a, int ntiles, int max_nl, cudaStream_t s, bool pdl) {
-    return launch_k(k_stencil, ntiles, NTHREADS, stencil_smem_bytes(max_nl), s, pdl, a);
+cudaError_t launch_stencil(const StencilArgs& a, int ntiles, int max_nl, int large, cudaStream_t s, bool pdl) {
+    if (large) return launch_k(k_stencil<TileL>, ntiles, NTHREADS, stencil_smem_bytes(max_nl, 1), s, pdl, a);
+    return launch_k(k_stencil<TileS>, ntiles, NTHREADS, stencil_smem_bytes(max_nl, 0), s, pdl, a);
 }
 
-cudaError_t launch_mode_to_layer(const MemberDev* members, const StencilTile* tiles, int ntiles,
+cudaError_t launch_mode_to_layer(const MemberDev* members, const StencilTile* tiles, int ntiles, int large,
                                  const float* psi_hat, float* psi, cudaStream_t s, bool pdl) {
-    return launch_k(k_mode_to_layer, ntiles, NTHREADS, 0, s, pdl, members, tiles, psi_hat, psi);
+    return launch_k(k_mode_to_layer, ntiles, NTHREADS, 0, s, pdl, members, tiles, large ? TileL::TX : TileS::TX,
+                    large ? TileL::TY : TileS::TY, psi_hat, psi);
 }
 
-cudaError_t launch_residual(const MemberDev* members, const StencilTile* tiles, int ntiles,
+cudaError_t launch_residual(const MemberDev* members, const StencilTile* tiles, int ntiles, int large,
                             const float* qm, const float* psi_hat, void* out, int out_fmt,
                             int64_t xplane, cudaStream_t s, bool pdl) {
-    return launch_k(k_residual, ntiles, NTHREADS, 0, s, pdl, members, tiles, qm, psi_hat, out, out_fmt, xplane);
+    return launch_k(k_residual, ntiles, NTHREADS, 0, s, pdl, members, tiles, large ? TileL::TX : TileS::TX,
+                    large ? TileL::TY : TileS::TY, qm, psi_hat, out, out_fmt, xplane);
 }
 
-cudaError_t launch_diag_acc(const MemberDev* members, const StencilTile* tiles, int ntiles,
+cudaError_t launch_diag_acc(const MemberDev* members, const StencilTile* tiles, int ntiles, int large,
                             const float* q, const float* psi_hat, double* acc, cudaStream_t s) {
-    return launch_k(k_diag, ntiles, NTHREADS, 0, s, false, members, tiles, q, psi_hat, acc);
+    return launch_k(k_diag, ntiles, NTHREADS, 0, s, false, members, tiles, large ? TileL::TX : TileS::TX,
+                    large ? TileL::TY : TileS::TY, q, psi_hat, acc);
 }
 
 cudaError_t launch_diag_finish(const double* acc, int64_t n_layers, float* ke, float* ens,

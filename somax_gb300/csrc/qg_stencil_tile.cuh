@@ -2,6 +2,8 @@
 // (qg_stencil.cu) and the persistent step kernel (qg_persistent.cu).  A tile is TX x TY
 // interior cells of one member, all layers, computed by 256 threads from TMA boxes of q and
 // psi_hat with a two-cell halo (x from tx0 - 4 so the box starts on a 16-byte boundary).
+// Two tile shapes: 32 x 8 (one cell per thread: short latency chains and many CTAs for small
+// grids) and 64 x 16 (four cells per thread: less halo traffic for large grids).
 #pragma once
 
 #include <cuda.h>
@@ -13,19 +15,37 @@
 namespace qg {
 namespace st {
 
-constexpr int TX = kStencilTX;      // interior tile width  (x)
-constexpr int TY = kStencilTY;      // interior tile height (y)
-constexpr int BX = TX + 8;          // TMA box width: x from tx0 - 4 (16-byte aligned start)
-constexpr int BY = TY + 4;          // box height: two halo rows each side (biharmonic)
-constexpr int BOX = BX * BY;        // floats per layer in a box
 constexpr int NTHREADS = 256;
-constexpr int ROWS_PER_THREAD = TX * TY / NTHREADS;  // 4
+
+template <int TX_, int TY_>
+struct Tile {
+    static constexpr int TX = TX_;                   // interior tile width  (x)
+    static constexpr int TY = TY_;                   // interior tile height (y)
+    static constexpr int BX = TX + 8;                // box width: x from tx0 - 4 (16-byte aligned)
+    static constexpr int BY = TY + 4;                // box height: two halo rows each side
+    static constexpr int BOX = BX * BY;              // floats per layer in a box
+    static constexpr int PER_THREAD = TX * TY / NTHREADS;
+    static_assert(TX * TY % NTHREADS == 0, "tile cells must split evenly over the threads");
+    static_assert(BX * 4 % 16 == 0, "TMA box rows must be whole 16-byte units");
+};
+using TileS = Tile<32, 8>;
+using TileL = Tile<64, 16>;
 
 struct StencilMaps {
     CUtensorMap q[3];  // stage planes S0, S1, S2
     CUtensorMap psi;   // psi_hat plane
 };
 static_assert(sizeof(StencilMaps) == kStencilMapsBytes, "StencilMaps size");
+
+// Shared memory of one tile: q and psi boxes (TMA destinations) and lap(q) (computed).
+template <class T>
+__host__ __device__ constexpr size_t tile_box_bytes(int nl) {
+    return (size_t)2 * nl * T::BOX * sizeof(float);
+}
+template <class T>
+__host__ __device__ constexpr size_t tile_lap_bytes(int nl) {
+    return (size_t)nl * T::BOX * sizeof(float);
+}
 
 // Copy a member's constants into shared memory (one 4-byte word per thread per pass).
 __device__ __forceinline__ void load_member(MemberDev* dst, const MemberDev* src) {
@@ -59,15 +79,27 @@ __device__ __forceinline__ void store_plane(void* base, int fmt, int64_t plane_e
     }
 }
 
+// Issue the two TMA box copies of tile (ty, tx) of a member: q from stage plane `q_sel` and
+// psi_hat, all layers, completing on `bar`.
+template <class T>
+__device__ __forceinline__ void tile_issue(const StencilMaps* maps, int q_sel, int nl, int ty, int tx, float* sq,
+                                           float* sp, uint64_t* bar) {
+    mbar_expect_tx(bar, (uint32_t)tile_box_bytes<T>(nl));
+    tma_load_3d(sq, &maps->q[q_sel], bar, tx * T::TX - 4, ty * T::TY - 2, 0);
+    tma_load_3d(sp, &maps->psi, bar, tx * T::TX - 4, ty * T::TY - 2, 0);
+}
 
-// After the TMA boxes landed: zero the q ring (BC on read) and mix psi_hat to layer psi in
-// place, zeroing the baroclinic psi ring (baroclinic.py:155-158).
-__device__ __forceinline__ void stencil_fix_box(const MemberDev& M, float* sq, float* sp, int j0, int i0,
-                                                int apply_bc) {
+// After the TMA boxes landed: zero the q ring (BC on read), mix psi_hat to layer psi in
+// place zeroing the baroclinic psi ring (baroclinic.py:155-158), and lap(q) of the cells one
+// ring beyond the tile (zero on the ghost ring: the interior-only Laplacian).
+template <class T>
+__device__ __forceinline__ void stencil_fix_box(const MemberDev& M, float* sq, float* sp, float* sl, int ty, int tx,
+                                                int apply_bc, bool need_lap) {
+    constexpr int BX = T::BX, BOX = T::BOX;
     const int nl = M.nl, Ny = M.Ny, Nx = M.Nx;
-    // BC on the q ring; psi = Cm2l psi_hat with the baroclinic ring zeroed
-    const bool edge = (j0 <= 0) || (i0 <= 0) || (j0 + BY >= Ny) || (i0 + BX >= Nx);
-    for (int c = threadIdx.x; c < BOX; c += blockDim.x) {
+    const int j0 = ty * T::TY - 2, i0 = tx * T::TX - 4;
+    const bool edge = (j0 <= 0) || (i0 <= 0) || (j0 + T::BY >= Ny) || (i0 + BX >= Nx);
+    for (int c = threadIdx.x; c < BOX; c += NTHREADS) {
         const int j = j0 + c / BX, i = i0 + c % BX;
         const bool ring = edge && j >= 0 && j < Ny && i >= 0 && i < Nx && on_ring(j, i, Ny, Nx);
         if (apply_bc && ring)
@@ -78,36 +110,56 @@ __device__ __forceinline__ void stencil_fix_box(const MemberDev& M, float* sq, f
             for (int l = 0; l < nl; ++l) {
                 float p = 0.f;
                 for (int m = 0; m < nl; ++m) p = fmaf(M.Cm2l[l * kMaxLayers + m], ph[m], p);
-                sp[l * BOX + c] = p;
+                sp[l * BOX + c] = (ring && !M.barotropic) ? 0.f : p;
             }
-        } else if (M.Cm2l[0] != 1.f) {
-            sp[c] *= M.Cm2l[0];
+        } else {
+            const float p = sp[c] * M.Cm2l[0];
+            sp[c] = (ring && !M.barotropic) ? 0.f : p;
         }
-        if (ring && !M.barotropic)
-            for (int l = 0; l < nl; ++l) sp[l * BOX + c] = 0.f;
+    }
+    if (!need_lap) return;
+    __syncthreads();  // lap(q) reads the BC'd neighbours
+    const float idx2 = M.inv_dx2, idy2 = M.inv_dy2;
+    constexpr int LW = T::TX + 2, LH = T::TY + 2;  // cells one beyond the tile
+    for (int c = threadIdx.x; c < LW * LH; c += NTHREADS) {
+        const int sy = 1 + c / LW, sx = 3 + c % LW;  // box coordinates
+        const int j = j0 + sy, i = i0 + sx;
+        const bool interior = j > 0 && i > 0 && j < Ny - 1 && i < Nx - 1;
+        const int b = sy * BX + sx;
+        for (int l = 0; l < nl; ++l) {
+            const float* Q = sq + l * BOX + b;
+            sl[l * BOX + b] = interior ? (Q[1] - 2.f * Q[0] + Q[-1]) * idx2 + (Q[BX] - 2.f * Q[0] + Q[-BX]) * idy2
+                                       : 0.f;
+        }
     }
 }
 
 // Compute the tile's cells from the fixed boxes: rhs mode writes dq, step mode writes the
-// stage update, the next stage's modal operand and its FP32 copy.  Returns true if a
+// stage update, the next stage's modal operand and its FP32 copy.  y0 is read directly
+// from global memory (pointwise, issued before the arithmetic).  Returns true if a
 // non-finite value was produced.
+template <class T>
 __device__ __forceinline__ bool stencil_compute(const StencilArgs& a, const MemberDev& M, const StencilTile& t,
-                                                const float* sq, const float* sp) {
+                                                const float* sq, const float* sp, const float* sl) {
+    constexpr int BX = T::BX, BOX = T::BOX;
     const int nl = M.nl, Ny = M.Ny, Nx = M.Nx;
     const float* P = a.params + (int64_t)t.member * QG_NPARAMS;
     const float nu = P[QG_P_NU], kappa = P[QG_P_KAPPA], tau0 = P[QG_P_TAU0], nu4 = P[QG_P_NU4];
     const float idx2 = M.inv_dx2, idy2 = M.inv_dy2;
-    const int lx = threadIdx.x % TX;
-    const int ly0 = (threadIdx.x / TX) * ROWS_PER_THREAD;
-    const int i = t.tx * TX + lx;
+    const int lx = threadIdx.x % T::TX;
+    const int ly0 = (threadIdx.x / T::TX) * T::PER_THREAD;
+    const int i = t.tx * T::TX + lx;
     bool bad = false;
 #pragma unroll 1
-    for (int r = 0; r < ROWS_PER_THREAD; ++r) {
+    for (int r = 0; r < T::PER_THREAD; ++r) {
         const int ly = ly0 + r;
-        const int j = t.ty * TY + ly;
+        const int j = t.ty * T::TY + ly;
         if (j >= Ny || i >= Nx) continue;
         const bool ring = on_ring(j, i, Ny, Nx);
         const int s0 = (ly + 2) * BX + (lx + 4);  // box index of the cell
+        float y0v[kMaxLayers];
+        if (!a.dq)
+            for (int l = 0; l < nl; ++l) y0v[l] = a.y0[xrow_idx(M, l, j, i)];
         const float wind = tau0 * M.F[j] * M.invH0;
         float d[kMaxLayers];
         for (int l = 0; l < nl; ++l) {
@@ -135,16 +187,9 @@ __device__ __forceinline__ bool stencil_compute(const StencilArgs& a, const Memb
             const float lq = (gE - 2.f * Q[0] + gW) * idx2 + (gN - 2.f * Q[0] + gS) * idy2;
             v += nu * lq;
             if (nu4 != 0.f) {
-                // lap(lap q) with lap(q) = 0 on the ring (interior-only Laplacian)
-                auto lap_at = [&](int dj, int di) -> float {
-                    const int jj = j + dj, ii = i + di;
-                    if (jj <= 0 || ii <= 0 || jj >= Ny - 1 || ii >= Nx - 1) return 0.f;
-                    const float* c = Q + dj * BX + di;
-                    return (c[1] - 2.f * c[0] + c[-1]) * idx2 + (c[BX] - 2.f * c[0] + c[-BX]) * idy2;
-                };
-                const float l0 = lap_at(0, 0);
-                const float bl = (lap_at(0, 1) - 2.f * l0 + lap_at(0, -1)) * idx2 +
-                                 (lap_at(1, 0) - 2.f * l0 + lap_at(-1, 0)) * idy2;
+                // lap(lap q) from lap(q) in shared memory (zero on the ghost ring)
+                const float* L = sl + l * BOX + s0;
+                const float bl = (L[1] - 2.f * L[0] + L[-1]) * idx2 + (L[BX] - 2.f * L[0] + L[-BX]) * idy2;
                 v -= nu4 * bl;
             }
             d[l] = v;
@@ -158,17 +203,15 @@ __device__ __forceinline__ bool stencil_compute(const StencilArgs& a, const Memb
         // step mode
         float yn[kMaxLayers];
         for (int l = 0; l < nl; ++l) {
-            const int64_t o = xrow_idx(M, l, j, i);
-            const float y0 = a.y0[o];
             if (ring) {
                 // The ring tendency is state independent (wind only), so every consistent
                 // RK scheme ends at y0 + dt * dq there; stage inputs carry a zero ring (BC).
-                yn[l] = a.final_stage ? y0 + a.dt * d[l] : 0.f;
+                yn[l] = a.final_stage ? y0v[l] + a.dt * d[l] : 0.f;
             } else {
-                yn[l] = a.a * y0 + a.b * (sq[l * BOX + s0] + a.dt * d[l]);
+                yn[l] = a.a * y0v[l] + a.b * (sq[l * BOX + s0] + a.dt * d[l]);
             }
             bad |= !isfinite(yn[l]);
-            a.y_next[o] = yn[l];
+            a.y_next[xrow_idx(M, l, j, i)] = yn[l];
         }
         if (a.xa) {
             for (int m = 0; m < nl; ++m) {

@@ -160,16 +160,27 @@ __device__ __forceinline__ void tc_store_bf16x2(__nv_bfloat16* p, int64_t plane,
     p[plane + idx] = __float2bfloat16_rn(v - __bfloat162float(hi));
 }
 
+// Per-warp staging buffer of the epilogue: 32 rows x 32 columns, padded.
+constexpr int TC_STAGE_FLOATS = 32 * 33;
+constexpr int TC_EPI_SMEM = 4 * TC_STAGE_FLOATS * 4;  // bytes, four epilogue warps
+
 // Epilogue of one 128 x TC_BN tile by one of four epilogue warps (TMEM lane quarter
 // `quarter`): read the accumulator and apply the pass's store.  All four warps must call it
-// (tcgen05.ld is warp-collective); `valid` false skips the stores.
+// (tcgen05.ld is warp-collective); `valid` false skips the stores.  Transposed passes store
+// straight from registers (lanes hold consecutive output rows); the row-major passes go
+// through the warp's staging buffer so that every store instruction writes 32 consecutive
+// elements of one row.
 template <int PASS>
 __device__ __forceinline__ void tc_epilogue(const MemberDev& M, const TcGeom& g, void* Cv, int c_fmt, int accumulate,
-                                            int m0, int n0, uint32_t tmem_acc, int quarter, int lane, bool valid) {
+                                            int m0, int n0, uint32_t tmem_acc, int quarter, int lane, bool valid,
+                                            float* stage) {
+    const int Mtot = g.Mtot, Mb = g.Mb, Nn = g.Nn, ldo = g.ldo;
+    const int64_t cplane = g.cplane;
     const int m = m0 + quarter * 32 + lane;
-    const int l = m < g.Mtot ? m / g.Mb : 0;
-    const int r = m - l * g.Mb;
-    const float exr = (PASS == G2_FWD_Y && m < g.Mtot) ? M.ex[r] : 0.f;
+    const int l = m < Mtot ? m / Mb : 0;
+    const int r = m - l * Mb;
+    const float* __restrict__ ey = M.ey;
+    const float exr = (PASS == G2_FWD_Y && m < Mtot) ? M.ex[r] : 0.f;
     const float laml = M.lam[l];
     float* Cf = static_cast<float*>(Cv) + g.cbase;
     __nv_bfloat16* Cb = static_cast<__nv_bfloat16*>(Cv) + g.cbase;
@@ -178,35 +189,45 @@ __device__ __forceinline__ void tc_epilogue(const MemberDev& M, const TcGeom& g,
         const uint32_t taddr = tmem_acc + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(c * 32);
         QG_LD32(v, taddr);
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        if (!valid || m >= g.Mtot) continue;
         const int nb = n0 + c * 32;
-        if (nb >= g.Nn) continue;
+        if (!valid || nb >= Nn) continue;  // warp-uniform
         if constexpr (PASS == G1_FWD_X || PASS == G3_INV_Y) {
             // transposed store out[(l, n)][r]: lanes hold consecutive r -> coalesced
+            if (m >= Mtot) continue;
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
-                if (nb + j >= g.Nn) break;
+                if (nb + j >= Nn) break;
                 const float x = __uint_as_float(v[j]);
-                const int64_t o = ((int64_t)l * g.Nn + nb + j) * g.ldo + r;
+                const int64_t o = ((int64_t)l * Nn + nb + j) * ldo + r;
                 if (c_fmt == FMT_F32)
                     Cf[o] = x;
                 else
-                    tc_store_bf16x2(Cb, g.cplane, o, x);
+                    tc_store_bf16x2(Cb, cplane, o, x);
             }
         } else {
-            const int64_t o = (int64_t)m * g.ldo + nb;
+            float eyv = 0.f;
+            if (PASS == G2_FWD_Y) eyv = (nb + lane < Nn) ? ey[nb + lane] : 1.f;
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
-                if (nb + j >= g.Nn) break;
                 float x = __uint_as_float(v[j]);
-                if constexpr (PASS == G2_FWD_Y) x = x / (exr + M.ey[nb + j] - laml);
-                if (c_fmt == FMT_F32) {
-                    if (PASS == G4_INV_X && accumulate) x += Cf[o + j];
-                    Cf[o + j] = x;
-                } else {
-                    tc_store_bf16x2(Cb, g.cplane, o + j, x);
+                if constexpr (PASS == G2_FWD_Y) x = x / (exr + __shfl_sync(0xffffffffu, eyv, j) - laml);
+                stage[lane * 33 + j] = x;  // row = lane, column = j
+            }
+            __syncwarp();
+            const int n = nb + lane;
+            for (int rr = 0; rr < 32; ++rr) {
+                const int mm = m0 + quarter * 32 + rr;
+                if (mm >= Mtot) break;
+                if (n < Nn) {
+                    const int64_t o = (int64_t)mm * ldo + n;
+                    const float x = stage[rr * 33 + lane];
+                    if (c_fmt == FMT_F32)
+                        Cf[o] = (PASS == G4_INV_X && accumulate) ? Cf[o] + x : x;
+                    else
+                        tc_store_bf16x2(Cb, cplane, o, x);
                 }
             }
+            __syncwarp();
         }
     }
 }

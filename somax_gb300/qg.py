@@ -183,6 +183,8 @@ class Plan:
         self._L = L
         self.members = list(members)
         self.precision = precision
+        self.refine = int(refine)
+        self.persistent = bool(persistent)
         self.state_size = int(L.qg_plan_state_size(handle))
         self.offsets = [int(L.qg_plan_member_offset(handle, i)) for i in range(len(members))]
 
@@ -261,6 +263,14 @@ class Plan:
         if code not in (0, K["QG_ERR_NONFINITE"], K["QG_ERR_TIMEOUT"]):
             check(code, "qg_status")
         return code
+
+    def launches_per_call(self, n_steps: int, scheme: str) -> int:
+        """Kernels libqgcore launches for one ``step`` call of ``n_steps`` steps."""
+        stages = {"heun": 2, "ssprk3": 3}[scheme]
+        if self.persistent and self.precision != "fp32" and self.refine == 0:
+            return 3  # pack, the persistent step kernel, unpack
+        per_stage = 4 * (1 + self.refine) + self.refine + 1
+        return 2 + n_steps * stages * per_stage
 
     def set_profiling(self, on: bool):
         check(self._L.qg_set_profiling(self._h, int(on)), "qg_set_profiling")
@@ -608,3 +618,13 @@ class QGEnsemble:
         if scheme not in ("heun", "ssprk3"):
             raise ValueError("ensembles step with heun or ssprk3")
         return self.plan.step(packed, self.params(packed.device), dt, n_steps, scheme, apply_bc)
+
+    def step_host(self, packed_host: torch.Tensor, out: torch.Tensor, dt: float, n_steps: int = 1,
+                  solver="ssprk3", apply_bc=True) -> torch.Tensor:
+        """``step`` for a packed state in (pinned) host memory: copy in, step, copy out."""
+        if packed_host.numel() != self.state_size:
+            raise ValueError("packed state has the wrong size")
+        q = packed_host.reshape(-1).to(device=self.plan.device, dtype=torch.float32, non_blocking=True)
+        self.step(q, dt, n_steps, solver, apply_bc)
+        out.reshape(-1).copy_(q, non_blocking=True)
+        return out
