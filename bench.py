@@ -368,7 +368,7 @@ def main():
                    "precision": args.precision, "persistent": bool(args.persistent),
                    "l2": "flushed between timed steps (256 MB write)",
                    "replicas": "independent basins per rank" if world > 1 else "one device",
-                   "status": status},
+                   "tuning": plan.tuning(), "status": status},
         "e2e": {"value": e2e_value, "unit": W.unit, "h2d_bytes_per_step": qbytes, "d2h_bytes_per_step": qbytes,
                 "api": "BaroclinicQG.step / QGEnsemble.step_host with pinned host q -> qg_step"},
         "roofline": roof,

@@ -105,7 +105,8 @@ typedef struct qg_options {
     int use_graphs;     /* 1: qg_step replays a captured CUDA graph per step */
     int persistent;     /* 1: qg_step advances all steps in one persistent cooperative launch
                            (tensor-core precisions without refinement) */
-    int reserved[4];
+    int autotune;       /* 1: qg_plan_create times the stencil tile shapes and keeps the faster */
+    int reserved[3];
 } qg_options;
 
 typedef struct qg_plan qg_plan;
@@ -170,6 +171,10 @@ const char* qg_strerror(int code);
 #define QG_K_COUNT 5
 int qg_set_profiling(qg_plan* plan, int enable); /* resets the counters */
 int qg_kernel_stats(qg_plan* plan, int kclass, double* total_ms, int64_t* launches);
+
+/* The plan's tuned choices: stencil tile shape (0 = 32 x 8, 1 = 64 x 16) and the autotuner's
+   per-launch times of both shapes in ms (-1 when not measured). */
+int qg_plan_tuning(const qg_plan* plan, int* tile_shape, float* ms_small, float* ms_large);
 
 #ifdef __cplusplus
 }

@@ -128,15 +128,12 @@ struct StencilArgs {
 cudaError_t launch_prep(const PrepArgs& a, int ntiles, cudaStream_t s, bool pdl);
 cudaError_t launch_unpack(const MemberDev* members, const StencilTile* tiles, int ntiles, int large,
                           const float* src, float* q, cudaStream_t s, bool pdl);
-cudaError_t launch_stencil(const StencilArgs& a, int ntiles, int max_nl, int large, cudaStream_t s, bool pdl);
-size_t stencil_smem_bytes(int max_nl, int large);
 cudaError_t launch_mode_to_layer(const MemberDev* members, const StencilTile* tiles, int ntiles, int large,
                                  const float* psi_hat, float* psi, cudaStream_t s, bool pdl);
 cudaError_t launch_diag_acc(const MemberDev* members, const StencilTile* tiles, int ntiles, int large,
                             const float* q, const float* psi_hat, double* acc, cudaStream_t s);
 cudaError_t launch_diag_finish(const double* acc, int64_t n_layers, float* ke, float* ens,
                                cudaStream_t s);
-void stencil_init();
 cudaError_t launch_residual(const MemberDev* members, const StencilTile* tiles, int ntiles, int large,
                             const float* qm, const float* psi_hat, void* out, int out_fmt,
                             int64_t xplane, cudaStream_t s, bool pdl);
@@ -177,6 +174,7 @@ struct PersistArgs {
     size_t lap_offset;        // shared-memory offset of the lap(q) buffer
     int st_nbuf;              // stencil box buffers (2: next tile loads during compute)
     int st_large;             // stencil tile shape: 0 = 32 x 8, 1 = 64 x 16
+    int g4_accumulate;        // the last GEMM pass adds into psi_hat (refinement)
     int op_fmt;
     int n_stages, n_steps;
     float sa[4], sb[4], dt;   // Shu-Osher stage coefficients
@@ -186,11 +184,15 @@ struct PersistArgs {
 };
 size_t persistent_smem_bytes(int precision, int max_nl, int large, PersistArgs* a);
 cudaError_t persistent_init();
-cudaError_t launch_persistent(const PersistArgs& a, int grid, int precision, cudaStream_t s);  // 4 CUtensorMap per (member, pass)
+cudaError_t launch_persistent(const PersistArgs& a, int grid, int precision, cudaStream_t s);
+// multi-tile stand-alone launches (the graph-captured multi-launch path)
+cudaError_t launch_gemm_mt(const PersistArgs& a, int pass, int grid, int precision, cudaStream_t s, bool pdl);
+cudaError_t launch_stencil_mt(const StencilArgs& sa, int n_st, int grid, int max_nl, int large, cudaStream_t s,
+                              bool pdl);
+int stencil_mt_blocks_per_sm(int max_nl, int large);  // 4 CUtensorMap per (member, pass)
 cudaError_t gemm_tc_encode(const MemberDev& M, int pass, const void* a_plane, int64_t a_plane_elems, int prec,
                            void* out);
 cudaError_t launch_gemm_simt(const GemmArgs& g, int ntiles, cudaStream_t s, bool pdl);
-cudaError_t launch_gemm_tc(const GemmArgs& g, int ntiles, int precision, cudaStream_t s, bool pdl);
 
 // host helpers shared by the plan and the plan-free entry points
 int validate_member(const qg_member_desc& d);

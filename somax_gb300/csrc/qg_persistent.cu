@@ -150,8 +150,8 @@ __device__ void gemm_phase(const PersistArgs& a, uint8_t* smem, Shared& sh, uint
             if (!have) break;
             tc_fence_after();
             float* stage = reinterpret_cast<float*>(smem + C::STAGES * tc_stage_bytes<PREC>()) + (warp - 4) * TC_STAGE_FLOATS;
-            tc_epilogue<PASS>(M, g, Cv, c_fmt, 0, tl.mt * TC_BM, tl.nt * TC_BN, tmem + buf * TC_BN, warp & 3, lane,
-                              true, stage);
+            tc_epilogue<PASS>(M, g, Cv, c_fmt, PASS == G4_INV_X ? a.g4_accumulate : 0, tl.mt * TC_BM, tl.nt * TC_BN,
+                              tmem + buf * TC_BN, warp & 3, lane, true, stage);
             tc_fence_before();
             mbar_arrive(&sh.tempty[buf]);
             ++c.epi_tiles;
@@ -159,12 +159,56 @@ __device__ void gemm_phase(const PersistArgs& a, uint8_t* smem, Shared& sh, uint
     }
 }
 
-// Stencil phase of stage `k`: tiles round-robin; with two box buffers the next tile's TMA
-// copies run while the current tile is computed.
+// Stencil tiles of one launch or phase, round-robin over the CTAs; with two box buffers the
+// next tile's TMA copies run while the current tile is computed.  `sa` selects the input
+// stage plane (q_sel), the mode (rhs / step) and the outputs.
+template <class T>
+__device__ void stencil_tiles(const StencilArgs& sa, int n_st, uint8_t* smem, size_t slot_bytes, size_t lap_offset,
+                              int nbuf, Shared& sh, Counters& c) {
+    using namespace st;
+    const StencilMaps* maps = static_cast<const StencilMaps*>(sa.maps);
+    float* sl = reinterpret_cast<float*>(smem + lap_offset);
+    auto issue = [&](int t, int b) {
+        const StencilTile tl = sa.tiles[t];
+        const int nl = sa.members[tl.member].nl;
+        float* sq = reinterpret_cast<float*>(smem + b * slot_bytes);
+        proxy_fence_shared();  // generic accesses of this buffer finished before TMA rewrites it
+        tile_issue<T>(&maps[tl.member], sa.q_sel, nl, tl.ty, tl.tx, sq, sq + nl * T::BOX, &sh.sbar[b]);
+    };
+    if (nbuf == 2 && threadIdx.x == 0 && (int)blockIdx.x < n_st) issue(blockIdx.x, 0);
+    bool bad = false;
+    for (int u = 0;; ++u) {
+        const int t = blockIdx.x + u * gridDim.x;
+        if (t >= n_st || sh.abort) break;
+        const int b = nbuf == 2 ? (u & 1) : 0;
+        if (threadIdx.x == 0) {
+            if (nbuf == 1) {
+                issue(t, 0);
+            } else if (t + (int)gridDim.x < n_st) {
+                issue(t + gridDim.x, b ^ 1);
+            }
+        }
+        const StencilTile tl = sa.tiles[t];
+        load_member(&sh.M, sa.members + tl.member);
+        const bool need_lap = sa.params[(int64_t)tl.member * QG_NPARAMS + QG_P_NU4] != 0.f;
+        __syncthreads();
+        const bool have = mbar_wait(&sh.sbar[b], c.st_use[b] & 1, &sh.abort);
+        ++c.st_use[b];
+        float* sq = reinterpret_cast<float*>(smem + b * slot_bytes);
+        float* sp = sq + sh.M.nl * T::BOX;
+        bad |= stencil_tile<T>(sa, sh.M, tl, sq, sp, sl, sa.apply_bc, need_lap) || !have;
+        __syncthreads();
+    }
+    if (bad && sa.flags) atomicOr(sa.flags, 1);
+    // a prefetch issued for a tile beyond an abort is drained before the buffers are reused
+    if (sh.abort && threadIdx.x == 0) {
+        for (int b = 0; b < nbuf; ++b) mbar_drain(&sh.sbar[b], c.st_use[b] & 1);
+    }
+}
+
+// Stencil phase of stage `k` of the persistent kernel.
 template <class T>
 __device__ void stencil_phase(const PersistArgs& a, int k, uint8_t* smem, Shared& sh, Counters& c) {
-    using namespace st;
-    const StencilMaps* maps = static_cast<const StencilMaps*>(a.st_maps);
     const bool fin = (k == a.n_stages - 1);
     StencilArgs sa{};
     sa.members = a.members;
@@ -184,58 +228,12 @@ __device__ void stencil_phase(const PersistArgs& a, int k, uint8_t* smem, Shared
     sa.xa_fmt = a.op_fmt;
     sa.xq = nullptr;
     sa.flags = a.flags;
-    float* sl = reinterpret_cast<float*>(smem + a.lap_offset);
-    const int nbuf = a.st_nbuf;
-
-    auto issue = [&](int t, int b) {
-        const StencilTile tl = a.st[t];
-        const int nl = a.members[tl.member].nl;
-        float* sq = reinterpret_cast<float*>(smem + b * a.slot_bytes);
-        proxy_fence_shared();  // generic accesses of this buffer finished before TMA rewrites it
-        tile_issue<T>(&maps[tl.member], k, nl, tl.ty, tl.tx, sq, sq + nl * T::BOX, &sh.sbar[b]);
-    };
-    if (nbuf == 2 && threadIdx.x == 0 && (int)blockIdx.x < a.n_st) issue(blockIdx.x, 0);
-    bool bad = false;
-    for (int u = 0;; ++u) {
-        const int t = blockIdx.x + u * gridDim.x;
-        if (t >= a.n_st || sh.abort) break;
-        const int b = nbuf == 2 ? (u & 1) : 0;
-        if (threadIdx.x == 0) {
-            if (nbuf == 1) {
-                issue(t, 0);
-            } else if (t + (int)gridDim.x < a.n_st) {
-                issue(t + gridDim.x, b ^ 1);
-            }
-        }
-        const StencilTile tl = a.st[t];
-        load_member(&sh.M, a.members + tl.member);
-        const bool need_lap = a.params[(int64_t)tl.member * QG_NPARAMS + QG_P_NU4] != 0.f;
-        __syncthreads();
-        const bool have = mbar_wait(&sh.sbar[b], c.st_use[b] & 1, &sh.abort);
-        ++c.st_use[b];
-        float* sq = reinterpret_cast<float*>(smem + b * a.slot_bytes);
-        float* sp = sq + sh.M.nl * T::BOX;
-        stencil_fix_box<T>(sh.M, sq, sp, sl, tl.ty, tl.tx, 1, need_lap);
-        __syncthreads();
-        bad |= stencil_compute<T>(sa, sh.M, tl, sq, sp, sl) || !have;
-        __syncthreads();
-    }
-    if (bad && a.flags) atomicOr(a.flags, 1);
-    // a prefetch issued for a tile beyond an abort is drained before the buffers are reused
-    if (sh.abort && threadIdx.x == 0) {
-        for (int b = 0; b < nbuf; ++b) mbar_drain(&sh.sbar[b], c.st_use[b] & 1);
-    }
+    stencil_tiles<T>(sa, a.n_st, smem, a.slot_bytes, a.lap_offset, a.st_nbuf, sh, c);
 }
 
-template <int PREC, class T>
-__global__ void __launch_bounds__(PT, 1) k_persistent(PersistArgs a) {
-    using C = TcCfg<PREC>;
-    extern __shared__ uint8_t smem_raw[];
-    __shared__ Shared sh;
-    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    const int warp = threadIdx.x >> 5;
+__device__ void init_shared(Shared& sh, int stages) {
     if (threadIdx.x == 0) {
-        for (int s = 0; s < C::STAGES; ++s) {
+        for (int s = 0; s < stages; ++s) {
             mbar_init(&sh.full[s], 1);
             mbar_init(&sh.empty[s], 1);
         }
@@ -248,6 +246,74 @@ __global__ void __launch_bounds__(PT, 1) k_persistent(PersistArgs a) {
         sh.issued = sh.consumed = sh.committed = 0;
         mbar_init_fence();
     }
+}
+
+// After an abort: drain TMA copies issued but not consumed, then the MMAs of the last
+// committed accumulator, so that shared memory and TMEM are quiet before the CTA exits.
+template <int STAGES>
+__device__ void drain_after_abort(Shared& sh) {
+    if (sh.abort && threadIdx.x == 0) {
+        for (int kb = sh.consumed; kb < sh.issued; ++kb) mbar_drain(&sh.full[kb % STAGES], (kb / STAGES) & 1);
+        if (sh.committed > 0) {
+            const int t = sh.committed - 1;
+            mbar_drain(&sh.tfull[t & 1], (t >> 1) & 1);
+        }
+    }
+}
+
+// One DST-I GEMM pass as its own launch: output tiles of all members round-robin over
+// min(tiles, SMs) CTAs, two TMEM accumulators so a tile's epilogue overlaps the next
+// tile's MMAs.
+template <int PREC, int PASS>
+__global__ void __launch_bounds__(PT, 1) k_gemm_mt(PersistArgs a) {
+    using C = TcCfg<PREC>;
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ Shared sh;
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    init_shared(sh, C::STAGES);
+    if ((threadIdx.x >> 5) == 1) tc_alloc(&sh.tmem_slot, 2 * TC_BN);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = sh.tmem_slot;
+    pdl_wait();
+    pdl_launch_dependents();
+    Counters c;
+    gemm_phase<PREC, PASS>(a, smem, sh, tmem, c);
+    __syncthreads();
+    drain_after_abort<C::STAGES>(sh);
+    tc_fence_before();
+    __syncthreads();
+    if ((threadIdx.x >> 5) == 1) {
+        tc_fence_after();
+        tc_dealloc(tmem, 2 * TC_BN);
+    }
+    if (threadIdx.x == 0 && sh.abort && a.flags) atomicOr(a.flags, 2);
+}
+
+// The RHS stencil as its own launch: tiles round-robin, double-buffered TMA boxes.
+template <class T>
+__global__ void __launch_bounds__(PT, 3) k_stencil_mt(StencilArgs sa, int n_st, size_t slot_bytes, size_t lap_offset,
+                                                      int nbuf) {
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ Shared sh;
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    init_shared(sh, 0);
+    __syncthreads();
+    pdl_wait();
+    pdl_launch_dependents();
+    Counters c;
+    stencil_tiles<T>(sa, n_st, smem, slot_bytes, lap_offset, nbuf, sh, c);
+}
+
+template <int PREC, class T>
+__global__ void __launch_bounds__(PT, 1) k_persistent(PersistArgs a) {
+    using C = TcCfg<PREC>;
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ Shared sh;
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int warp = threadIdx.x >> 5;
+    init_shared(sh, C::STAGES);
     if (warp == 1) tc_alloc(&sh.tmem_slot, 2 * TC_BN);
     tc_fence_before();
     __syncthreads();
@@ -272,15 +338,7 @@ __global__ void __launch_bounds__(PT, 1) k_persistent(PersistArgs a) {
     }
 done:
     __syncthreads();
-    if (*abort && threadIdx.x == 0) {
-        // drain: TMA copies issued but not consumed, then the MMAs of the last committed tile
-        for (int kb = sh.consumed; kb < sh.issued; ++kb)
-            mbar_drain(&sh.full[kb % C::STAGES], (kb / C::STAGES) & 1);
-        if (sh.committed > 0) {
-            const int t = sh.committed - 1;
-            mbar_drain(&sh.tfull[t & 1], (t >> 1) & 1);
-        }
-    }
+    drain_after_abort<C::STAGES>(sh);
     tc_fence_before();
     __syncthreads();
     if (warp == 1) {
@@ -313,8 +371,69 @@ size_t persistent_smem_bytes(int precision, int max_nl, int large, PersistArgs* 
     return std::max(gemm, sten) + 1024;
 }
 
+size_t stencil_mt_smem_bytes(int max_nl, int large, size_t* slot, size_t* lap_off, int* nbuf) {
+    PersistArgs a{};
+    const size_t b = large ? stencil_layout<st::TileL>(max_nl, &a) : stencil_layout<st::TileS>(max_nl, &a);
+    if (slot) *slot = a.slot_bytes;
+    if (lap_off) *lap_off = a.lap_offset;
+    if (nbuf) *nbuf = a.st_nbuf;
+    return b + 1024;
+}
+
+int stencil_mt_blocks_per_sm(int max_nl, int large) {
+    int n = 0;
+    const size_t smem = stencil_mt_smem_bytes(max_nl, large, nullptr, nullptr, nullptr);
+    if (large)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_stencil_mt<st::TileL>, PT, smem);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_stencil_mt<st::TileS>, PT, smem);
+    return n > 0 ? n : 1;
+}
+
+cudaError_t launch_stencil_mt(const StencilArgs& sa, int n_st, int grid, int max_nl, int large, cudaStream_t s,
+                              bool pdl) {
+    size_t slot = 0, lap = 0;
+    int nbuf = 1;
+    const size_t smem = stencil_mt_smem_bytes(max_nl, large, &slot, &lap, &nbuf);
+    if (large) return launch_k(k_stencil_mt<st::TileL>, grid, PT, smem, s, pdl, sa, n_st, slot, lap, nbuf);
+    return launch_k(k_stencil_mt<st::TileS>, grid, PT, smem, s, pdl, sa, n_st, slot, lap, nbuf);
+}
+
+template <int PREC>
+size_t gemm_mt_smem() {
+    return (size_t)TcCfg<PREC>::STAGES * tc_stage_bytes<PREC>() + TC_EPI_SMEM + 1024;
+}
+
+cudaError_t launch_gemm_mt(const PersistArgs& a, int pass, int grid, int precision, cudaStream_t s, bool pdl) {
+#define QG_GMT(P)                                                                                                  \
+    switch (pass) {                                                                                                \
+        case G1_FWD_X: return launch_k(k_gemm_mt<P, G1_FWD_X>, grid, PT, gemm_mt_smem<P>(), s, pdl, a);          \
+        case G2_FWD_Y: return launch_k(k_gemm_mt<P, G2_FWD_Y>, grid, PT, gemm_mt_smem<P>(), s, pdl, a);          \
+        case G3_INV_Y: return launch_k(k_gemm_mt<P, G3_INV_Y>, grid, PT, gemm_mt_smem<P>(), s, pdl, a);          \
+        case G4_INV_X: return launch_k(k_gemm_mt<P, G4_INV_X>, grid, PT, gemm_mt_smem<P>(), s, pdl, a);          \
+        default: return cudaErrorInvalidValue;                                                                     \
+    }
+    if (precision == QG_DST_TF32) { QG_GMT(QG_DST_TF32) }
+    if (precision == QG_DST_BF16X3) { QG_GMT(QG_DST_BF16X3) }
+#undef QG_GMT
+    return cudaErrorInvalidValue;
+}
+
 cudaError_t persistent_init() {
     cudaError_t e = cudaSuccess;
+#define QG_MTATTR(K, B)                                                                                       \
+    if (!e) e = cudaFuncSetAttribute(K, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(B));
+    QG_MTATTR(k_stencil_mt<st::TileS>, stencil_mt_smem_bytes(kMaxLayers, 0, nullptr, nullptr, nullptr))
+    QG_MTATTR(k_stencil_mt<st::TileL>, stencil_mt_smem_bytes(kMaxLayers, 1, nullptr, nullptr, nullptr))
+    QG_MTATTR((k_gemm_mt<QG_DST_TF32, G1_FWD_X>), gemm_mt_smem<QG_DST_TF32>())
+    QG_MTATTR((k_gemm_mt<QG_DST_TF32, G2_FWD_Y>), gemm_mt_smem<QG_DST_TF32>())
+    QG_MTATTR((k_gemm_mt<QG_DST_TF32, G3_INV_Y>), gemm_mt_smem<QG_DST_TF32>())
+    QG_MTATTR((k_gemm_mt<QG_DST_TF32, G4_INV_X>), gemm_mt_smem<QG_DST_TF32>())
+    QG_MTATTR((k_gemm_mt<QG_DST_BF16X3, G1_FWD_X>), gemm_mt_smem<QG_DST_BF16X3>())
+    QG_MTATTR((k_gemm_mt<QG_DST_BF16X3, G2_FWD_Y>), gemm_mt_smem<QG_DST_BF16X3>())
+    QG_MTATTR((k_gemm_mt<QG_DST_BF16X3, G3_INV_Y>), gemm_mt_smem<QG_DST_BF16X3>())
+    QG_MTATTR((k_gemm_mt<QG_DST_BF16X3, G4_INV_X>), gemm_mt_smem<QG_DST_BF16X3>())
+#undef QG_MTATTR
 #define QG_PATTR(P, T, L)                                                                                      \
     if (!e)                                                                                                    \
         e = cudaFuncSetAttribute(k_persistent<P, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,              \

@@ -242,7 +242,14 @@ struct qg_plan {
     void* st_maps = nullptr;  // TMA descriptors of the stencil halo boxes
     unsigned* bar = nullptr;  // grid barrier words of the persistent kernel (count, generation)
     int n_sm = 0;
-    int st_large = 0;         // stencil tile shape: 0 = 32 x 8, 1 = 64 x 16
+    int st_large = 0;         // stencil tile shape in use: 0 = 32 x 8, 1 = 64 x 16
+    int st_grid = 1;          // CTAs of a stencil launch (tiles round-robin over them)
+    // both stencil tile shapes are prepared; the autotuner (or a size rule) picks one
+    StencilTile* st_tiles_v[2] = {nullptr, nullptr};
+    int n_st_v[2] = {0, 0};
+    void* st_maps_v[2] = {nullptr, nullptr};
+    float tune_ms[2] = {-1.f, -1.f};
+    PersistArgs pa{};         // constant part of the tensor-core launches' arguments
     // graphs
     cudaStream_t cap = nullptr;
     StepGraph graph;
@@ -328,7 +335,10 @@ cudaError_t run_gemm(qg_plan* p, const GemmArgs& g, cudaStream_t s) {
     const int nt = (g.pass == G1_FWD_X || g.pass == G4_INV_X) ? p->n_gx : p->n_gy;
     return timed(p, QG_K_GEMM, s, [&] {
         if (p->opts.dst_precision == QG_DST_FP32) return launch_gemm_simt(g, nt, s, use_pdl(p));
-        return launch_gemm_tc(g, nt, p->opts.dst_precision, s, use_pdl(p));
+        PersistArgs a = p->pa;
+        a.g4_accumulate = g.accumulate;
+        const int grid = std::max(1, std::min(nt, p->n_sm));
+        return launch_gemm_mt(a, g.pass, grid, p->opts.dst_precision, s, use_pdl(p));
     });
 }
 
@@ -428,13 +438,74 @@ cudaError_t run_one_step(qg_plan* p, const float* params, float dt, int scheme, 
         a.dt = dt;
         a.xa = p->XA;
         a.xq = p->XQ;
-        e = timed(p, QG_K_STENCIL, s, [&] { return launch_stencil(a, p->n_st, p->max_nl, p->st_large, s, use_pdl(p)); });
+        e = timed(p, QG_K_STENCIL, s, [&] { return launch_stencil_mt(a, p->n_st, p->st_grid, p->max_nl, p->st_large, s, use_pdl(p)); });
         if (e) return e;
     }
     return cudaSuccess;
 }
 
 int cuda_err(cudaError_t e) { return e == cudaSuccess ? QG_OK : QG_ERR_CUDA; }
+
+// Make stencil tile shape `large` the active one (tile list, TMA maps, launch grid).
+void select_tile(qg_plan* p, int large) {
+    p->st_large = large;
+    p->st_tiles = p->st_tiles_v[large];
+    p->n_st = p->n_st_v[large];
+    p->st_maps = p->st_maps_v[large];
+    const int bps = stencil_mt_blocks_per_sm(p->max_nl, large);
+    p->st_grid = std::max(1, std::min(p->n_st, bps * std::max(p->n_sm, 1)));
+    PersistArgs& a = p->pa;
+    a.st = p->st_tiles;
+    a.n_st = p->n_st;
+    a.st_maps = p->st_maps;
+    a.st_large = large;
+    if (p->opts.dst_precision != QG_DST_FP32) persistent_smem_bytes(p->opts.dst_precision, p->max_nl, large, &a);
+}
+
+// Autotuner: time one step-mode stencil launch of each tile shape on the plan's own planes
+// (zero state, zero parameters) with CUDA events and keep the faster shape.
+cudaError_t autotune_stencil(qg_plan* p) {
+    cudaStream_t s = p->cap;
+    cudaEvent_t e0, e1;
+    cudaError_t e = cudaEventCreate(&e0);
+    if (!e) e = cudaEventCreate(&e1);
+    if (e) return e;
+    float best = 0.f;
+    int pick = p->st_large;
+    for (int v = 0; v < 2 && !e; ++v) {
+        select_tile(p, v);
+        StencilArgs a = stencil_args(p, p->params);
+        a.q_sel = 1;
+        a.apply_bc = 1;
+        a.y0 = p->S0;
+        a.y_next = p->S2;
+        a.a = 0.f;
+        a.b = 1.f;
+        a.dt = 1.f;
+        a.xa = p->XA;
+        float ms = 0.f;
+        for (int rep = 0; rep < 2 && !e; ++rep)
+            e = launch_stencil_mt(a, p->n_st, p->st_grid, p->max_nl, v, s, false);
+        if (!e) e = cudaEventRecord(e0, s);
+        for (int rep = 0; rep < 5 && !e; ++rep)
+            e = launch_stencil_mt(a, p->n_st, p->st_grid, p->max_nl, v, s, false);
+        if (!e) e = cudaEventRecord(e1, s);
+        if (!e) e = cudaEventSynchronize(e1);
+        if (!e) e = cudaEventElapsedTime(&ms, e0, e1);
+        p->tune_ms[v] = ms / 5.f;
+        if (!e && (v == 0 || ms < best)) {
+            best = ms;
+            pick = v;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (!e) select_tile(p, pick);
+    if (!e) e = cudaMemsetAsync(p->S2, 0, sizeof(float) * p->xplane, s);
+    if (!e) e = cudaMemsetAsync(p->XA, 0, sizeof(float) * p->xplane, s);
+    if (!e) e = cudaStreamSynchronize(s);
+    return e;
+}
 
 }  // namespace
 
@@ -485,6 +556,7 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
     o.refine_sweeps = 0;
     o.use_graphs = 1;
     o.persistent = 1;
+    o.autotune = 1;
     if (opts) o = *opts;
     if (o.dst_precision < QG_DST_FP32 || o.dst_precision > QG_DST_BF16X3) return QG_ERR_ARG;
     if (o.refine_sweeps < 0 || o.refine_sweeps > 1) return QG_ERR_ARG;
@@ -498,13 +570,12 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
     p->opts = o;
     p->desc.assign(members, members + n_members);
     cudaGetDevice(&p->device);
-    stencil_init();
-    if (tmap_init() != cudaSuccess) {
+    if (tmap_init() != cudaSuccess || persistent_init() != cudaSuccess) {
         delete p;
         return QG_ERR_UNSUPPORTED;
     }
     if (o.dst_precision != QG_DST_FP32) {
-        if (gemm_tc_init() != cudaSuccess || persistent_init() != cudaSuccess) {
+        if (gemm_tc_init() != cudaSuccess) {
             delete p;
             return QG_ERR_UNSUPPORTED;
         }
@@ -512,14 +583,15 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
     }
     cudaError_t e = cudaDeviceGetAttribute(&p->n_sm, cudaDevAttrMultiProcessorCount, p->device);
     {
-        // stencil tile shape: the large tile once it still gives every SM two tiles per stage
+        // default stencil tile shape (the autotuner may overrule it): the large tile once it
+        // still gives every SM two tiles per stage
         int64_t large_tiles = 0;
         for (int i = 0; i < n_members; ++i)
             large_tiles += (int64_t)((members[i].ny + 2 + kTileLY - 1) / kTileLY) *
                            ((members[i].nx + 2 + kTileLX - 1) / kTileLX);
         p->st_large = large_tiles >= 2 * (int64_t)std::max(p->n_sm, 1);
     }
-    const int TX = p->st_large ? kTileLX : kTileSX, TY = p->st_large ? kTileLY : kTileSY;
+    std::vector<StencilTile> st_v[2];
     // geometry and offsets
     p->mh.resize(n_members);
     int64_t off_state = 0, off_x = 0, off_y = 0, off_layer = 0;
@@ -599,8 +671,11 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
             M.Sy_bf = byy;
         }
         // tiles
-        for (int ty = 0; ty < (M.Ny + TY - 1) / TY; ++ty)
-            for (int tx = 0; tx < (M.Nx + TX - 1) / TX; ++tx) st.push_back({i, ty, tx});
+        for (int v = 0; v < 2; ++v) {
+            const int TX = v ? kTileLX : kTileSX, TY = v ? kTileLY : kTileSY;
+            for (int ty = 0; ty < (M.Ny + TY - 1) / TY; ++ty)
+                for (int tx = 0; tx < (M.Nx + TX - 1) / TX; ++tx) st_v[v].push_back({i, ty, tx});
+        }
         for (int mt = 0; mt < (n * M.Ny + BMg - 1) / BMg; ++mt)
             for (int nt = 0; nt < (M.Nx + BNg - 1) / BNg; ++nt) gx.push_back({i, mt, nt});
         for (int mt = 0; mt < (n * M.Nx + BMg - 1) / BMg; ++mt)
@@ -615,11 +690,13 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
         e = upload(p, &p->md, mv);
     }
     if (e == cudaSuccess) {
-        p->n_st = (int)st.size();
         p->n_gx = (int)gx.size();
         p->n_gy = (int)gy.size();
-        if (!(e = upload(p, &p->st_tiles, st)) && !(e = upload(p, &p->gx_tiles, gx)))
-            e = upload(p, &p->gy_tiles, gy);
+        for (int v = 0; v < 2 && !e; ++v) {
+            p->n_st_v[v] = (int)st_v[v].size();
+            e = upload(p, &p->st_tiles_v[v], st_v[v]);
+        }
+        if (!e && !(e = upload(p, &p->gx_tiles, gx))) e = upload(p, &p->gy_tiles, gy);
     }
     if (e == cudaSuccess) {
         const size_t xb = (size_t)p->xplane * 4, yb = (size_t)p->yplane * 4;
@@ -644,11 +721,40 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
     }
     if (e == cudaSuccess) {
         // TMA descriptors of the stencil's halo boxes: the three stage planes and psi_hat
-        std::vector<uint8_t> maps((size_t)n_members * kStencilMapsBytes);
         const float* planes[4] = {p->S0, p->S1, p->S2, p->XC};
-        for (int i = 0; i < n_members && !e; ++i)
-            e = stencil_encode_maps(p->mh[i], planes, p->st_large, maps.data() + (size_t)i * kStencilMapsBytes);
-        if (!e) e = upload(p, (uint8_t**)&p->st_maps, maps);
+        for (int v = 0; v < 2 && !e; ++v) {
+            std::vector<uint8_t> maps((size_t)n_members * kStencilMapsBytes);
+            for (int i = 0; i < n_members && !e; ++i)
+                e = stencil_encode_maps(p->mh[i], planes, v, maps.data() + (size_t)i * kStencilMapsBytes);
+            if (!e) e = upload(p, (uint8_t**)&p->st_maps_v[v], maps);
+        }
+    }
+    if (e == cudaSuccess) {
+        PersistArgs& a = p->pa;
+        a.members = p->md;
+        a.gx = p->gx_tiles;
+        a.gy = p->gy_tiles;
+        a.n_gx = p->n_gx;
+        a.n_gy = p->n_gy;
+        a.max_nl = p->max_nl;
+        a.tc_maps = p->tc_maps;
+        a.XA = p->XA;
+        a.YA = p->YA;
+        a.YB = p->YB;
+        a.XB = p->XB;
+        a.XC = p->XC;
+        a.S[0] = p->S0;
+        a.S[1] = p->S1;
+        a.S[2] = p->S2;
+        a.params = p->params;
+        a.xplane = p->xplane;
+        a.yplane = p->yplane;
+        a.op_fmt = p->op_fmt;
+        a.flags = p->flags;
+        a.bar_count = p->bar;
+        a.bar_gen = p->bar + 1;
+        select_tile(p, p->st_large);
+        if (o.autotune) e = autotune_stencil(p);
     }
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
@@ -717,7 +823,7 @@ int qg_rhs(qg_plan* p, const float* q, float* dq, const float* params, int flags
         a.q_sel = 1;
         a.apply_bc = bc;
         a.dq = dq;
-        e = timed(p, QG_K_STENCIL, s, [&] { return launch_stencil(a, p->n_st, p->max_nl, p->st_large, s, use_pdl(p)); });
+        e = timed(p, QG_K_STENCIL, s, [&] { return launch_stencil_mt(a, p->n_st, p->st_grid, p->max_nl, p->st_large, s, use_pdl(p)); });
     }
     return cuda_err(e);
 }
@@ -741,31 +847,7 @@ int qg_step(qg_plan* p, float* q, const float* params, double dt, int n_steps, i
                             p->opts.refine_sweeps == 0 && !p->profiling;
     const bool use_graph = p->opts.use_graphs && !p->profiling;
     if (persistent && n_steps > 0) {
-        PersistArgs a{};
-        a.members = p->md;
-        a.gx = p->gx_tiles;
-        a.gy = p->gy_tiles;
-        a.st = p->st_tiles;
-        a.n_gx = p->n_gx;
-        a.n_gy = p->n_gy;
-        a.n_st = p->n_st;
-        a.max_nl = p->max_nl;
-        a.tc_maps = p->tc_maps;
-        a.st_maps = p->st_maps;
-        a.XA = p->XA;
-        a.YA = p->YA;
-        a.YB = p->YB;
-        a.XB = p->XB;
-        a.XC = p->XC;
-        a.S[0] = p->S0;
-        a.S[1] = p->S1;
-        a.S[2] = p->S2;
-        a.params = p->params;
-        a.xplane = p->xplane;
-        a.yplane = p->yplane;
-        a.st_large = p->st_large;
-        persistent_smem_bytes(p->opts.dst_precision, p->max_nl, p->st_large, &a);
-        a.op_fmt = p->op_fmt;
+        PersistArgs a = p->pa;
         a.n_stages = scheme_stages(scheme, st);
         for (int k = 0; k < a.n_stages; ++k) {
             a.sa[k] = st[k].a;
@@ -773,9 +855,7 @@ int qg_step(qg_plan* p, float* q, const float* params, double dt, int n_steps, i
         }
         a.dt = (float)dt;
         a.n_steps = n_steps;
-        a.flags = p->flags;
-        a.bar_count = p->bar;
-        a.bar_gen = p->bar + 1;
+        a.g4_accumulate = 0;
         const int grid = std::max(1, std::min(p->n_sm, std::max(p->n_st, std::max(p->n_gx, p->n_gy))));
         e = timed(p, QG_K_PERSISTENT, s, [&] { return launch_persistent(a, grid, p->opts.dst_precision, s); });
     } else if (!use_graph) {
@@ -838,6 +918,14 @@ int qg_status(qg_plan* p, int* flags, void* stream) {
     if (flags) *flags = h;
     if (h & 2) return QG_ERR_TIMEOUT;
     if (h & 1) return QG_ERR_NONFINITE;
+    return QG_OK;
+}
+
+int qg_plan_tuning(const qg_plan* p, int* tile_shape, float* ms_small, float* ms_large) {
+    if (!p) return QG_ERR_NULL;
+    if (tile_shape) *tile_shape = p->st_large;
+    if (ms_small) *ms_small = p->tune_ms[0];
+    if (ms_large) *ms_large = p->tune_ms[1];
     return QG_OK;
 }
 

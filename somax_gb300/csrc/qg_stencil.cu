@@ -68,53 +68,6 @@ __global__ void __launch_bounds__(NTHREADS) k_unpack(const MemberDev* __restrict
 }
 
 // ---------------------------------------------------------------------------------------
-// Fused RHS stencil.  Per cell and layer (baroclinic.py:161-190, barotropic.py:123-152):
-//   dq = -J(psi, q + beta y) + [l = 0] tau0 F / H0 - [l = nl-1] kappa lap(psi) + nu lap(q)
-//        - nu4 lap(lap q)                                   (biharmonic extension)
-// with psi = Cm2l psi_hat (ring zeroed for the baroclinic model).  J(psi, beta y) is
-// evaluated in closed form for the linear beta y (exact for the Arakawa stencil), which
-// keeps FP32 from losing q against the much larger beta y.  On the ring dq is the wind
-// term only (J and the Laplacians are interior-only there).
-//
-// The halo tile of q and psi_hat, all layers, arrives by two 3-D TMA copies (zero fill
-// outside the array).  Step mode fuses the Shu-Osher stage update
-// y_next = a y0 + b (y_s + dt dq) and the next stage's layer->mode prologue.
-// ---------------------------------------------------------------------------------------
-template <class T>
-__global__ void __launch_bounds__(NTHREADS) k_stencil(StencilArgs a) {
-    extern __shared__ uint8_t smem_raw[];
-    float* smem = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
-    __shared__ MemberDev M;
-    __shared__ __align__(8) uint64_t bar;
-    __shared__ int abort_flag;
-    const StencilTile t = a.tiles[blockIdx.x];
-    const StencilMaps* maps = static_cast<const StencilMaps*>(a.maps) + t.member;
-    load_member(&M, a.members + t.member);
-    if (threadIdx.x == 0) {
-        mbar_init(&bar, 1);
-        mbar_init_fence();
-        abort_flag = 0;
-        tma_prefetch_desc(&maps->q[a.q_sel]);
-        tma_prefetch_desc(&maps->psi);
-    }
-    __syncthreads();
-    pdl_wait();
-    pdl_launch_dependents();
-
-    const int nl = M.nl;
-    float* sq = smem;                      // [nl][BY][BX] q, then BC applied
-    float* sp = smem + nl * T::BOX;        // [nl][BY][BX] psi_hat, mixed in place to psi
-    float* sl = smem + 2 * nl * T::BOX;    // [nl][BY][BX] lap(q)
-    if (threadIdx.x == 0) tile_issue<T>(maps, a.q_sel, nl, t.ty, t.tx, sq, sp, &bar);
-    const bool need_lap = a.params[(int64_t)t.member * QG_NPARAMS + QG_P_NU4] != 0.f;
-    const bool have = mbar_wait(&bar, 0, &abort_flag);
-    stencil_fix_box<T>(M, sq, sp, sl, t.ty, t.tx, a.apply_bc, need_lap);
-    __syncthreads();
-    const bool bad = stencil_compute<T>(a, M, t, sq, sp, sl) || !have;
-    if (bad && a.flags) atomicOr(a.flags, have ? 1 : 2);
-}
-
-// ---------------------------------------------------------------------------------------
 // Mode -> layer epilogue for qg_invert: psi = Cm2l psi_hat, ring zeroed (baroclinic).
 // ---------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(NTHREADS) k_mode_to_layer(const MemberDev* __restrict__ members,
@@ -262,11 +215,6 @@ __global__ void k_diag_finish(const double* __restrict__ acc, int64_t n, float* 
 // ---------------------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------------------
-size_t stencil_smem_bytes(int max_nl, int large) {
-    return (large ? tile_box_bytes<TileL>(max_nl) + tile_lap_bytes<TileL>(max_nl)
-                  : tile_box_bytes<TileS>(max_nl) + tile_lap_bytes<TileS>(max_nl)) + 128;
-}
-
 // 3-D boxes (BX, BY, nl) over a member's x-row planes: dims (Nx, Ny, nl), row pitch Px.
 cudaError_t stencil_encode_maps(const MemberDev& M, const float* const planes[4], int large, void* out) {
     StencilMaps sm;
@@ -284,13 +232,6 @@ cudaError_t stencil_encode_maps(const MemberDev& M, const float* const planes[4]
     return e;
 }
 
-void stencil_init() {
-    cudaFuncSetAttribute(k_stencil<TileS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)stencil_smem_bytes(kMaxLayers, 0));
-    cudaFuncSetAttribute(k_stencil<TileL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)stencil_smem_bytes(kMaxLayers, 1));
-}
-
 cudaError_t launch_prep(const PrepArgs& a, int ntiles, cudaStream_t s, bool pdl) {
     return launch_k(k_prep, ntiles, NTHREADS, 0, s, pdl, a);
 }
@@ -299,11 +240,6 @@ cudaError_t launch_unpack(const MemberDev* members, const StencilTile* tiles, in
                           const float* src, float* q, cudaStream_t s, bool pdl) {
     return launch_k(k_unpack, ntiles, NTHREADS, 0, s, pdl, members, tiles, large ? TileL::TX : TileS::TX,
                     large ? TileL::TY : TileS::TY, src, q);
-}
-
-cudaError_t launch_stencil(const StencilArgs& a, int ntiles, int max_nl, int large, cudaStream_t s, bool pdl) {
-    if (large) return launch_k(k_stencil<TileL>, ntiles, NTHREADS, stencil_smem_bytes(max_nl, 1), s, pdl, a);
-    return launch_k(k_stencil<TileS>, ntiles, NTHREADS, stencil_smem_bytes(max_nl, 0), s, pdl, a);
 }
 
 cudaError_t launch_mode_to_layer(const MemberDev* members, const StencilTile* tiles, int ntiles, int large,

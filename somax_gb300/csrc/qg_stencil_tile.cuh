@@ -91,30 +91,35 @@ __device__ __forceinline__ void tile_issue(const StencilMaps* maps, int q_sel, i
 
 // After the TMA boxes landed: zero the q ring (BC on read), mix psi_hat to layer psi in
 // place zeroing the baroclinic psi ring (baroclinic.py:155-158), and lap(q) of the cells one
-// ring beyond the tile (zero on the ghost ring: the interior-only Laplacian).
-template <class T>
+// ring beyond the tile (zero on the ghost ring: the interior-only Laplacian).  NL = layers.
+template <class T, int NL>
 __device__ __forceinline__ void stencil_fix_box(const MemberDev& M, float* sq, float* sp, float* sl, int ty, int tx,
                                                 int apply_bc, bool need_lap) {
     constexpr int BX = T::BX, BOX = T::BOX;
-    const int nl = M.nl, Ny = M.Ny, Nx = M.Nx;
+    const int Ny = M.Ny, Nx = M.Nx;
     const int j0 = ty * T::TY - 2, i0 = tx * T::TX - 4;
     const bool edge = (j0 <= 0) || (i0 <= 0) || (j0 + T::BY >= Ny) || (i0 + BX >= Nx);
+    float C[NL][NL];
+#pragma unroll
+    for (int l = 0; l < NL; ++l)
+#pragma unroll
+        for (int m = 0; m < NL; ++m) C[l][m] = M.Cm2l[l * kMaxLayers + m];
     for (int c = threadIdx.x; c < BOX; c += NTHREADS) {
         const int j = j0 + c / BX, i = i0 + c % BX;
         const bool ring = edge && j >= 0 && j < Ny && i >= 0 && i < Nx && on_ring(j, i, Ny, Nx);
         if (apply_bc && ring)
-            for (int l = 0; l < nl; ++l) sq[l * BOX + c] = 0.f;
-        if (nl > 1) {
-            float ph[kMaxLayers];
-            for (int m = 0; m < nl; ++m) ph[m] = sp[m * BOX + c];
-            for (int l = 0; l < nl; ++l) {
-                float p = 0.f;
-                for (int m = 0; m < nl; ++m) p = fmaf(M.Cm2l[l * kMaxLayers + m], ph[m], p);
-                sp[l * BOX + c] = (ring && !M.barotropic) ? 0.f : p;
-            }
-        } else {
-            const float p = sp[c] * M.Cm2l[0];
-            sp[c] = (ring && !M.barotropic) ? 0.f : p;
+#pragma unroll
+            for (int l = 0; l < NL; ++l) sq[l * BOX + c] = 0.f;
+        float ph[NL];
+#pragma unroll
+        for (int m = 0; m < NL; ++m) ph[m] = sp[m * BOX + c];
+        const bool zero = ring && !M.barotropic;
+#pragma unroll
+        for (int l = 0; l < NL; ++l) {
+            float p = 0.f;
+#pragma unroll
+            for (int m = 0; m < NL; ++m) p = fmaf(C[l][m], ph[m], p);
+            sp[l * BOX + c] = zero ? 0.f : p;
         }
     }
     if (!need_lap) return;
@@ -126,7 +131,8 @@ __device__ __forceinline__ void stencil_fix_box(const MemberDev& M, float* sq, f
         const int j = j0 + sy, i = i0 + sx;
         const bool interior = j > 0 && i > 0 && j < Ny - 1 && i < Nx - 1;
         const int b = sy * BX + sx;
-        for (int l = 0; l < nl; ++l) {
+#pragma unroll
+        for (int l = 0; l < NL; ++l) {
             const float* Q = sq + l * BOX + b;
             sl[l * BOX + b] = interior ? (Q[1] - 2.f * Q[0] + Q[-1]) * idx2 + (Q[BX] - 2.f * Q[0] + Q[-BX]) * idy2
                                        : 0.f;
@@ -135,34 +141,42 @@ __device__ __forceinline__ void stencil_fix_box(const MemberDev& M, float* sq, f
 }
 
 // Compute the tile's cells from the fixed boxes: rhs mode writes dq, step mode writes the
-// stage update, the next stage's modal operand and its FP32 copy.  y0 is read directly
-// from global memory (pointwise, issued before the arithmetic).  Returns true if a
-// non-finite value was produced.
-template <class T>
+// stage update, the next stage's modal operand and its FP32 copy.  y0 of every cell of the
+// thread is loaded before any arithmetic.  Returns true if a non-finite value was produced.
+template <class T, int NL>
 __device__ __forceinline__ bool stencil_compute(const StencilArgs& a, const MemberDev& M, const StencilTile& t,
                                                 const float* sq, const float* sp, const float* sl) {
-    constexpr int BX = T::BX, BOX = T::BOX;
-    const int nl = M.nl, Ny = M.Ny, Nx = M.Nx;
+    constexpr int BX = T::BX, BOX = T::BOX, R = T::PER_THREAD;
+    const int Ny = M.Ny, Nx = M.Nx;
     const float* P = a.params + (int64_t)t.member * QG_NPARAMS;
     const float nu = P[QG_P_NU], kappa = P[QG_P_KAPPA], tau0 = P[QG_P_TAU0], nu4 = P[QG_P_NU4];
     const float idx2 = M.inv_dx2, idy2 = M.inv_dy2;
     const int lx = threadIdx.x % T::TX;
-    const int ly0 = (threadIdx.x / T::TX) * T::PER_THREAD;
+    const int ly0 = (threadIdx.x / T::TX) * R;
     const int i = t.tx * T::TX + lx;
+    const bool step = a.dq == nullptr;
+    float y0r[R][NL];
+    float Fj[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int j = t.ty * T::TY + ly0 + r;
+        const bool in = j < Ny && i < Nx;
+        Fj[r] = in ? M.F[j] : 0.f;
+#pragma unroll
+        for (int l = 0; l < NL; ++l) y0r[r][l] = (step && in) ? a.y0[xrow_idx(M, l, j, i)] : 0.f;
+    }
     bool bad = false;
-#pragma unroll 1
-    for (int r = 0; r < T::PER_THREAD; ++r) {
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
         const int ly = ly0 + r;
         const int j = t.ty * T::TY + ly;
         if (j >= Ny || i >= Nx) continue;
         const bool ring = on_ring(j, i, Ny, Nx);
         const int s0 = (ly + 2) * BX + (lx + 4);  // box index of the cell
-        float y0v[kMaxLayers];
-        if (!a.dq)
-            for (int l = 0; l < nl; ++l) y0v[l] = a.y0[xrow_idx(M, l, j, i)];
-        const float wind = tau0 * M.F[j] * M.invH0;
-        float d[kMaxLayers];
-        for (int l = 0; l < nl; ++l) {
+        const float wind = tau0 * Fj[r] * M.invH0;
+        float d[NL];
+#pragma unroll
+        for (int l = 0; l < NL; ++l) {
             if (ring) {
                 d[l] = (l == 0) ? wind : 0.f;
                 continue;
@@ -180,7 +194,7 @@ __device__ __forceinline__ bool stencil_compute(const StencilArgs& a, const Memb
             const float Jb = (4.f * (fE - fW) + (fNE - fNW) + (fSE - fSW)) * M.beta_12dx;
             float v = -(Jq + Jb);
             if (l == 0) v += wind;
-            if (l == nl - 1) {
+            if (l == NL - 1) {
                 const float lp = (fE - 2.f * S[0] + fW) * idx2 + (fN - 2.f * S[0] + fS) * idy2;
                 v += -kappa * lp;
             }
@@ -194,36 +208,64 @@ __device__ __forceinline__ bool stencil_compute(const StencilArgs& a, const Memb
             }
             d[l] = v;
         }
-        for (int l = 0; l < nl; ++l) bad |= !isfinite(d[l]);
+#pragma unroll
+        for (int l = 0; l < NL; ++l) bad |= !isfinite(d[l]);
 
-        if (a.dq) {
-            for (int l = 0; l < nl; ++l) a.dq[caller_idx(M, l, j, i)] = d[l];
+        if (!step) {
+#pragma unroll
+            for (int l = 0; l < NL; ++l) a.dq[caller_idx(M, l, j, i)] = d[l];
             continue;
         }
-        // step mode
-        float yn[kMaxLayers];
-        for (int l = 0; l < nl; ++l) {
+        float yn[NL];
+#pragma unroll
+        for (int l = 0; l < NL; ++l) {
             if (ring) {
                 // The ring tendency is state independent (wind only), so every consistent
                 // RK scheme ends at y0 + dt * dq there; stage inputs carry a zero ring (BC).
-                yn[l] = a.final_stage ? y0v[l] + a.dt * d[l] : 0.f;
+                yn[l] = a.final_stage ? y0r[r][l] + a.dt * d[l] : 0.f;
             } else {
-                yn[l] = a.a * y0v[l] + a.b * (sq[l * BOX + s0] + a.dt * d[l]);
+                yn[l] = a.a * y0r[r][l] + a.b * (sq[l * BOX + s0] + a.dt * d[l]);
             }
             bad |= !isfinite(yn[l]);
             a.y_next[xrow_idx(M, l, j, i)] = yn[l];
         }
         if (a.xa) {
-            for (int m = 0; m < nl; ++m) {
+#pragma unroll
+            for (int m = 0; m < NL; ++m) {
                 float s = 0.f;
                 if (!ring)
-                    for (int l = 0; l < nl; ++l) s = fmaf(M.Cl2m[m * kMaxLayers + l], yn[l], s);
+#pragma unroll
+                    for (int l = 0; l < NL; ++l) s = fmaf(M.Cl2m[m * kMaxLayers + l], yn[l], s);
                 store_plane(a.xa, a.xa_fmt, a.xplane, xrow_idx(M, m, j, i), s);
                 if (a.xq) a.xq[xrow_idx(M, m, j, i)] = s;
             }
         }
     }
     return bad;
+}
+
+// Fix the boxes of one tile and compute it; dispatches on the member's layer count.
+template <class T>
+__device__ __forceinline__ bool stencil_tile(const StencilArgs& a, const MemberDev& M, const StencilTile& t,
+                                             float* sq, float* sp, float* sl, int apply_bc, bool need_lap) {
+#define QG_NL_CASE(N)                                                \
+    case N:                                                          \
+        stencil_fix_box<T, N>(M, sq, sp, sl, t.ty, t.tx, apply_bc, need_lap); \
+        __syncthreads();                                             \
+        return stencil_compute<T, N>(a, M, t, sq, sp, sl);
+    switch (M.nl) {
+        QG_NL_CASE(1)
+        QG_NL_CASE(2)
+        QG_NL_CASE(3)
+        QG_NL_CASE(4)
+        QG_NL_CASE(5)
+        QG_NL_CASE(6)
+        QG_NL_CASE(7)
+        QG_NL_CASE(8)
+        default:
+            return true;
+    }
+#undef QG_NL_CASE
 }
 
 }  // namespace st

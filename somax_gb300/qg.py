@@ -166,7 +166,7 @@ class Plan:
     """Owns a ``qg_plan`` (device constants + workspace) on one CUDA device."""
 
     def __init__(self, members: Sequence["MemberSpec"], precision="fp32", refine=0, use_graphs=True,
-                 device=None, persistent=True):
+                 device=None, persistent=True, autotune=True):
         if not torch.cuda.is_available():
             raise RuntimeError("somax_gb300 needs a CUDA device (no CPU fallback)")
         self.device = torch.device(device or "cuda", torch.cuda.current_device()) if device is None \
@@ -175,7 +175,8 @@ class Plan:
         arr = (MemberDesc * len(members))()
         for i, m in enumerate(members):
             m.fill(arr[i])
-        opts = Options(PRECISIONS[precision], int(refine), int(bool(use_graphs)), int(bool(persistent)))
+        opts = Options(PRECISIONS[precision], int(refine), int(bool(use_graphs)), int(bool(persistent)),
+                       int(bool(autotune)))
         handle = C.c_void_p()
         with torch.cuda.device(self.device):
             check(L.qg_plan_create(arr, len(members), C.byref(opts), C.byref(handle)), "qg_plan_create")
@@ -271,6 +272,12 @@ class Plan:
             return 3  # pack, the persistent step kernel, unpack
         per_stage = 4 * (1 + self.refine) + self.refine + 1
         return 2 + n_steps * stages * per_stage
+
+    def tuning(self) -> dict:
+        shape = C.c_int()
+        a, b = C.c_float(), C.c_float()
+        check(self._L.qg_plan_tuning(self._h, C.byref(shape), C.byref(a), C.byref(b)), "qg_plan_tuning")
+        return {"stencil_tile": "64x16" if shape.value else "32x8", "ms_32x8": a.value, "ms_64x16": b.value}
 
     def set_profiling(self, on: bool):
         check(self._L.qg_set_profiling(self._h, int(on)), "qg_set_profiling")

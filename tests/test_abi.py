@@ -52,7 +52,7 @@ def test_plan_create_validates_before_cuda(L):
     d[0].wind_profile = 7
     assert L.qg_plan_create(d, 1, None, C.byref(h)) == _lib.K["QG_ERR_ARG"]
     d[0].wind_profile = 0
-    o = _lib.Options(5, 0, 1, 1)
+    o = _lib.Options(5, 0, 1, 1, 1)
     assert L.qg_plan_create(d, 1, C.byref(o), C.byref(h)) == _lib.K["QG_ERR_ARG"]
     assert h.value is None
 
