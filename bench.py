@@ -258,8 +258,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="baroclinic3_128")
-    ap.add_argument("--precision", default="fp32")
-    ap.add_argument("--persistent", type=int, default=1, help="tensor-core precisions: one launch per call")
+    ap.add_argument("--precision", default="bf16x3", help="DST-I GEMM arithmetic: fp32 | tf32 | bf16x3")
+    ap.add_argument("--persistent", type=int, default=0,
+                    help="1: all steps of a call in one persistent cooperative launch (tensor-core precisions)")
     ap.add_argument("--ref-sample-steps", type=int, default=12)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

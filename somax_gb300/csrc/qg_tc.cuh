@@ -210,7 +210,9 @@ __device__ __forceinline__ void tc_epilogue(const MemberDev& M, const TcGeom& g,
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
                 float x = __uint_as_float(v[j]);
-                if constexpr (PASS == G2_FWD_Y) x = x / (exr + __shfl_sync(0xffffffffu, eyv, j) - laml);
+                // spectral divide: the fast division is exact to ~2 ulp, far inside the
+                // BF16x3 / TF32 error of the transform itself
+                if constexpr (PASS == G2_FWD_Y) x = __fdividef(x, exr + __shfl_sync(0xffffffffu, eyv, j) - laml);
                 stage[lane * 33 + j] = x;  // row = lane, column = j
             }
             __syncwarp();
