@@ -106,8 +106,10 @@ def peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "src": "fallback"}
 
 
-def cpu_baseline(cfg, sample_steps: int, threads: int):
-    """Float32 oracle restatement of one RK step loop on the host cores."""
+def cpu_baseline(cfg, threads: int, min_seconds: float = 10.0, chunk: int = 12):
+    """Float32 oracle restatement of the RK step loop on the host cores: whole chunks of
+    ``chunk`` steps until at least ``min_seconds`` have elapsed.  Returns (model-days/s,
+    steps, seconds)."""
     from oracle import qg as O
     from somax_gb300 import testcases as tc
 
@@ -119,64 +121,79 @@ def cpu_baseline(cfg, sample_steps: int, threads: int):
                             biharmonic_viscosity=cfg.biharmonic_viscosity)
     q = tc.initial_pv(cfg, seed=0).astype(np.float32)
     O.integrate(om, q, cfg.dt, 1, cfg.scheme)  # warm
-    t0 = time.perf_counter()
-    O.integrate(om, q, cfg.dt, sample_steps, cfg.scheme)
-    el = time.perf_counter() - t0
-    days_per_s = sample_steps * cfg.dt / 86400.0 / el
-    return days_per_s, el
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        q = O.integrate(om, q, cfg.dt, chunk, cfg.scheme).astype(np.float32)
+        steps += chunk
+        el = time.perf_counter() - t0
+        if el >= min_seconds:
+            break
+    return steps * cfg.dt / 86400.0 / el, steps, el
 
 
-def ensemble_cpu_rate(threads: int, sample_steps: int):
+def ensemble_cpu_rate(threads: int, min_seconds: float = 10.0):
     """member-days/s of the 256-member mix on the host: one member of each class timed for
-    `sample_steps` steps, the ensemble's step time is the count-weighted sum."""
+    ``min_seconds / 4``; the ensemble's step time is the count-weighted sum."""
     from somax_gb300 import testcases as tc
 
-    t_step = 0.0
+    t_step, desc = 0.0, []
     for count, cfg in tc.C4_MIX:
-        _, el = cpu_baseline(cfg, sample_steps, threads)
-        t_step += count * el / sample_steps
-    return 256 * tc.C4_MIX[0][1].dt / 86400.0 / t_step
+        _, steps, el = cpu_baseline(cfg, threads, min_seconds / len(tc.C4_MIX), chunk=4)
+        t_step += count * el / steps
+        desc.append(f"{steps} steps of {cfg.name}")
+    return 256 * tc.C4_MIX[0][1].dt / 86400.0 / t_step, ", ".join(desc)
 
 
-def run_reference(args, cfg):
+ENSEMBLE_METRIC = "QG member-days/sec per GB300 (256-member ragged ensemble, SSP-RK3 dt=1200 s)"
+ENSEMBLE_DESC = ("ensemble256: 96 x 1-layer 64^2 (Rd 50 km) + 96 x 3-layer 128^2 + 48 x 3-layer 256^2 + "
+                 "16 x 5-layer 256^2 double gyres, tau0 ~ U(0.05, 0.12) N/m^2, ssprk3 dt=1200s")
+
+
+def describe(name):
+    """(metric, unit, workload text) of a bench configuration, shared by both arms."""
+    from somax_gb300 import testcases as tc
+
+    if name == "ensemble256":
+        return ENSEMBLE_METRIC, "member-days/s", ENSEMBLE_DESC + ", 72 steps = 1 model day per bench step"
+    cfg = tc.CONFIGS[name]
+    metric = METRIC if name == "baroclinic3_128" else f"QG model-days/sec per GB300 ({name})"
+    steps = int(round(86400.0 / cfg.dt))
+    return metric, UNIT, (f"{name}: {cfg.nl}-layer {cfg.n}x{cfg.n} double gyre (Lx=Ly=5120 km), "
+                          f"{cfg.scheme} dt={cfg.dt:g}s, {steps} steps = 1 model day per bench step")
+
+
+def run_reference(args):
+    """The reference's CPU path (its JAX code cannot be installed here): the float32
+    NumPy/SciPy restatement on every host core, each bench step a bounded time sample."""
+    from somax_gb300 import testcases as tc
+
     rank = _env_int("RANK", 0)
     if rank != 0:
         return
     threads = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
-    if args.config == "ensemble256":
-        vals = [ensemble_cpu_rate(threads, 2) for _ in range(args.steps)]
-        value = statistics.median(vals)
-        line = {
-            "impl": "reference", "metric": "QG member-days/sec per GB300 (256-member ragged ensemble, SSP-RK3 dt=1200 s)",
-            "value": value, "unit": "member-days/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1000.0 / value, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "ensemble256", "sample": "2 steps of one member per class, count-weighted"},
-            "cpu_baseline": {"value": value, "unit": "member-days/s", "cores": threads, "kind": "port",
-                             "sample": "float32 NumPy/SciPy restatement, one member of each class"},
-            "e2e": {"value": value, "unit": "member-days/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        }
-        print(json.dumps(line), flush=True)
-        return
-    sample = max(1, min(args.ref_sample_steps, int(round(86400 / cfg.dt))))
-    for _ in range(args.warmup):
-        cpu_baseline(cfg, 1, threads)
-    vals, tot = [], 0.0
-    for _ in range(args.steps):
-        v, el = cpu_baseline(cfg, sample, threads)
-        vals.append(v)
-        tot += el
+    metric, unit, workload = describe(args.config)
+    per_step_s = 5.0
+    vals, samples = [], []
+    for k in range(args.warmup + args.steps):
+        if args.config == "ensemble256":
+            v, desc = ensemble_cpu_rate(threads, per_step_s if k >= args.warmup else 1.0)
+        else:
+            cfg = tc.CONFIGS[args.config]
+            v, n, el = cpu_baseline(cfg, threads, per_step_s if k >= args.warmup else 1.0)
+            desc = f"{n} {cfg.scheme} steps of {cfg.name} ({el:.1f} s)"
+        if k >= args.warmup:
+            vals.append(v)
+            samples.append(desc)
     value = statistics.median(vals)
+    sample = (f"per bench step >= {per_step_s:g} s of the float32 NumPy/SciPy restatement "
+              f"(scipy.fft workers={threads}), e.g. {samples[0]}; the reference's JAX path is not installable")
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "impl": "reference", "metric": metric, "value": value, "unit": unit, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"{cfg.name}: 3-layer {cfg.n}x{cfg.n} double gyre, {cfg.scheme} dt={cfg.dt:g}s",
-                   "sample": f"{sample} time steps per bench step, scaled to model-days/s"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{sample} {cfg.scheme} steps of {cfg.name} in float32 NumPy/SciPy "
-                                   f"(scipy.fft workers={threads}); the reference's JAX path is not installable"},
-        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "config": {"workload": workload, "sample": sample},
+        "cpu_baseline": {"value": value, "unit": unit, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
@@ -209,10 +226,6 @@ class Workload:
             self.q0 = np.concatenate([q.reshape(-1) for q in q0s])
             self.members = [(c.n + 2, c.nl) for c in cfgs]
             self.dt, self.scheme = cfgs[0].dt, cfgs[0].scheme
-            self.unit = "member-days/s"
-            self.metric = "QG member-days/sec per GB300 (256-member ragged ensemble, SSP-RK3 dt=1200 s)"
-            self.describe = ("ensemble256: 96 x 1-layer 64^2 (Rd 50 km) + 96 x 3-layer 128^2 + 48 x 3-layer 256^2 + "
-                             "16 x 5-layer 256^2 double gyres, tau0 ~ U(0.05, 0.12) N/m^2, ssprk3 dt=1200s")
             self.model = None
         else:
             cfg = tc.CONFIGS[name]
@@ -222,11 +235,8 @@ class Workload:
             self.q0 = tc.initial_pv(cfg, seed=seed).astype(np.float32)
             self.members = [(cfg.n + 2, cfg.nl)]
             self.dt, self.scheme = cfg.dt, cfg.scheme
-            self.unit = "model-days/s"
-            self.metric = METRIC if name == "baroclinic3_128" else f"QG model-days/sec per GB300 ({name})"
-            self.describe = (f"{name}: {cfg.nl}-layer {cfg.n}x{cfg.n} double gyre (Lx=Ly=5120 km), "
-                             f"{cfg.scheme} dt={cfg.dt:g}s")
             self.ens = None
+        self.metric, self.unit, self.describe = describe(name)
         self.n_members = len(self.members)
         self.steps_per_day = int(round(86400.0 / self.dt))
         self.q = torch.tensor(self.q0, device=dev).reshape(-1)
@@ -251,6 +261,67 @@ class Workload:
         return sum(2.0 * nl * N ** 3 for N, nl in self.members)
 
 
+KERNEL_CLASSES = {0: "prep", 1: "dst_gemm", 2: "rhs_stencil", 3: "other", 4: "persistent"}
+
+
+def traffic_table():
+    """DRAM bytes per launch measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum),
+    committed with the profiles: {workload: {kernel class: bytes}}."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return {}
+    with open(p) as f:
+        return json.load(f).get("bytes_per_launch", {})
+
+
+def roofline(W, stats, precision, name):
+    """Roofline of every kernel class from the profiled pass's per-launch event times.
+
+    Algorithmic HBM bytes per launch, per layer-cell of every member (lc = sum nl Ny Nx):
+      dst_gemm     one DST-I pass: operand in (4 B: FP32, or BF16 hi + lo) + result out (4 B)
+      rhs_stencil  step mode: q of the stage, psi_hat, y0 in (12 B); y_next and the next
+                   stage's modal operand out (8 B)
+      prep / other pack q (4 B in, 8 B out) / unpack (4 B in, 4 B out)
+    Issued tensor flops of a DST-I pass: 2 N per element (three products for BF16x3).  A
+    kernel is HBM-bound when its bytes / peak bandwidth exceed its flops / peak throughput.
+    The dominant class (largest total time) is the headline."""
+    pk = peaks()
+    lc = W.cells()
+    bytes_per = {0: 12.0 * lc, 1: 8.0 * lc, 2: 20.0 * lc, 3: 8.0 * lc}
+    flops_per = {1: W.gemm_flops_per_pass() * (3.0 if precision == "bf16x3" else 1.0)}
+    traffic = traffic_table().get(name, {})
+    kernels = {}
+    for k, (ms, n) in stats.items():
+        if not n or k not in bytes_per:
+            continue
+        avg_s = ms / 1000.0 / n
+        gbs = bytes_per[k] / avg_s / 1e9
+        ent = {"launches": n, "total_ms": ms, "avg_us": avg_s * 1e6, "bytes_per_launch": bytes_per[k],
+               "achieved_gbs": gbs, "hbm_frac": gbs / pk["hbm_gbs"]}
+        if k in flops_per:
+            tf = flops_per[k] / avg_s / 1e12
+            ent.update({"issued_tflops": tf, "tensor_frac": tf / pk["bf16_tflops"]})
+            t_hbm = bytes_per[k] / (pk["hbm_gbs"] * 1e9)
+            t_tc = flops_per[k] / (pk["bf16_tflops"] * 1e12)
+            ent["bound"] = "tensor" if t_tc > t_hbm else "hbm"
+        else:
+            ent["bound"] = "hbm"
+        ent["traffic"] = traffic.get(KERNEL_CLASSES[k])
+        kernels[KERNEL_CLASSES[k]] = ent
+    dom = max((k for k in (1, 2) if KERNEL_CLASSES[k] in kernels), key=lambda k: stats[k][0])
+    d = kernels[KERNEL_CLASSES[dom]]
+    if d["bound"] == "tensor":
+        roof = {"bound": "tensor", "achieved": d["issued_tflops"], "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+                "frac": d["tensor_frac"]}
+    else:
+        roof = {"bound": "hbm", "achieved": d["achieved_gbs"], "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": d["hbm_frac"]}
+    roof.update({"kernel": KERNEL_CLASSES[dom], "traffic": d["traffic"], "peak_src": pk["src"],
+                 "algorithmic_bytes_per_launch": d["bytes_per_launch"], "avg_launch_us": d["avg_us"],
+                 "kernels": kernels})
+    return roof
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -268,7 +339,7 @@ def main():
     from somax_gb300 import testcases as tc
 
     if args.impl == "reference":
-        run_reference(args, tc.CONFIGS.get(args.config))
+        run_reference(args)
         return
 
     import torch
@@ -340,32 +411,13 @@ def main():
     torch.cuda.synchronize()
     stats = {k: plan.kernel_stats(k) for k in range(5)}
     plan.set_profiling(False)
-    kern = {0: "prep", 1: "dst_gemm", 2: "rhs_stencil", 3: "other", 4: "persistent"}
-    dom = max(stats, key=lambda k: stats[k][0])
-    pk = peaks()
-    stages = {"heun": 2, "ssprk3": 3}[W.scheme]
-    if dom == 1:
-        avg_s = stats[1][0] / 1000.0 / stats[1][1]
-        achieved = W.gemm_flops_per_pass() / avg_s / 1e12
-        peak = pk["bf16_tflops"]
-        roof = {"bound": "tensor", "kernel": "dst_gemm", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak, "traffic": None, "peak_src": pk["src"],
-                "note": "achieved counts the algorithmic 2MNK of one DST pass (BF16x3 issues three products)"}
-    else:
-        # stencil in step mode: read y_s, psi_hat, y0 (stages > 0), write y_next and the
-        # next-stage modal operand: (5 * stages - 1) / stages * 4 bytes per cell per layer
-        bpc = 4.0 * (5 * stages - 1) / stages
-        avg_s = stats[dom][0] / 1000.0 / max(stats[dom][1], 1)
-        achieved = bpc * W.cells() / avg_s / 1e9
-        roof = {"bound": "hbm", "kernel": kern[dom], "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved / pk["hbm_gbs"], "traffic": None, "peak_src": pk["src"]}
-    roof["kernel_ms"] = {kern[k]: {"total_ms": v[0], "launches": v[1]} for k, v in stats.items() if v[1]}
+    roof = roofline(W, stats, args.precision, args.config)
 
     line = {
         "metric": W.metric, "value": value, "unit": W.unit, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": W.describe + f", {W.steps_per_day} steps = 1 model day per bench step",
+        "config": {"workload": W.describe,
                    "precision": args.precision, "persistent": bool(args.persistent),
                    "l2": "flushed between timed steps (256 MB write)",
                    "replicas": "independent basins per rank" if world > 1 else "one device",
@@ -379,16 +431,13 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = len(os.sched_getaffinity(0))
         if W.model is not None:
-            sample = 6
             cfg = tc.CONFIGS[args.config]
-            v, el = cpu_baseline(cfg, sample, threads)
-            line["cpu_baseline"] = {"value": v, "unit": W.unit, "cores": threads, "kind": "port",
-                                    "sample": f"{sample} {cfg.scheme} steps of {cfg.name}, float32 NumPy/SciPy "
-                                              f"restatement ({el:.2f} s)"}
+            v, n, el = cpu_baseline(cfg, threads, 10.0)
+            sample = f"{n} {cfg.scheme} steps of {cfg.name}, float32 NumPy/SciPy restatement ({el:.1f} s)"
         else:
-            v = ensemble_cpu_rate(threads, 1)
-            line["cpu_baseline"] = {"value": v, "unit": W.unit, "cores": threads, "kind": "port",
-                                    "sample": "1 step of one member per class, count-weighted, float32 NumPy/SciPy"}
+            v, desc = ensemble_cpu_rate(threads, 10.0)
+            sample = f"one member per class, count-weighted: {desc}; float32 NumPy/SciPy restatement"
+        line["cpu_baseline"] = {"value": v, "unit": W.unit, "cores": threads, "kind": "port", "sample": sample}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
