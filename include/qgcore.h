@@ -15,6 +15,9 @@
  *                    it is SomaxModel.build_terms._rhs (somax/_src/core/model.py:47-49)
  *   qg_step          SomaxModel.integrate with ConstantStepSize (core/model.py:53-88)
  *   qg_diagnose      BaroclinicQG.diagnose KE / enstrophy (baroclinic.py:197-228)
+ *   qg_rhs_vjp       reverse-mode derivative of vector_field / _rhs, and
+ *   qg_invert_vjp    of _invert_pv, that the reference takes with JAX autodiff
+ *                    (eqx.filter_grad through integrate: tests/models/test_qg_baroclinic.py:293-312)
  *   qg_status        non-finite check of the runner (somax/_src/cli/_run.py:671-686)
  *
  * Conventions: every field is float32, layout (n_layers, Ny, Nx) row-major per member with
@@ -139,6 +142,17 @@ int qg_rhs(qg_plan* plan, const float* q, float* dq, const float* params, int fl
    same result as one call over all their steps. */
 int qg_step(qg_plan* plan, float* q, const float* params, double dt, int n_steps, int scheme,
             int flags, void* stream);
+
+/* Vector-Jacobian products (hand-written adjoints; device pointers, packed fields).
+   qg_rhs_vjp: for the qg_rhs call with the same q, params and flags, and the cotangent
+   dq_bar of its dq: q_bar = (d dq / d q)^T dq_bar and, when params_bar is not NULL,
+   params_bar = (d dq / d params)^T dq_bar (n_members * QG_NPARAMS floats, overwritten).
+   qg_invert_vjp: q_bar = (d psi / d q)^T psi_bar for qg_invert.  Both run one adjoint
+   Helmholtz solve on the plan's DST-I GEMMs (the solve is self-adjoint) with the plan's
+   precision and refinement. */
+int qg_rhs_vjp(qg_plan* plan, const float* q, const float* params, const float* dq_bar, float* q_bar,
+               float* params_bar, int flags, void* stream);
+int qg_invert_vjp(qg_plan* plan, const float* psi_bar, float* q_bar, void* stream);
 
 /* Kinetic energy and enstrophy per layer: ke, ens each sum(n_layers) floats (device). */
 int qg_diagnose(qg_plan* plan, const float* q, float* ke, float* ens, void* stream);

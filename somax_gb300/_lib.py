@@ -78,6 +78,8 @@ def lib() -> C.CDLL:
         "qg_invert_static": (C.c_int, [C.POINTER(MemberDesc), vp, vp, vp]),
         "qg_rhs": (C.c_int, [vp, vp, vp, vp, C.c_int, vp]),
         "qg_step": (C.c_int, [vp, vp, vp, C.c_double, C.c_int, C.c_int, C.c_int, vp]),
+        "qg_rhs_vjp": (C.c_int, [vp, vp, vp, vp, vp, vp, C.c_int, vp]),
+        "qg_invert_vjp": (C.c_int, [vp, vp, vp, vp]),
         "qg_diagnose": (C.c_int, [vp, vp, vp, vp, vp]),
         "qg_status": (C.c_int, [vp, C.POINTER(C.c_int), vp]),
         "qg_strerror": (C.c_char_p, [C.c_int]),

@@ -138,6 +138,28 @@ cudaError_t launch_residual(const MemberDev* members, const StencilTile* tiles, 
                             const float* qm, const float* psi_hat, void* out, int out_fmt,
                             int64_t xplane, cudaStream_t s, bool pdl);
 
+// Adjoint (qg_adjoint.cu): the RHS / inversion VJP around one adjoint DST solve.
+struct VjpArgs {
+    const MemberDev* members;
+    const StencilTile* tiles;
+    int ntiles, tile_x, tile_y, max_nl, n_members;
+    const float* q;       // caller packing
+    int apply_bc;         // the forward zeroed the ring of q on read
+    const float* psi;     // layer psi of the forward, caller packing
+    const float* gbar;    // cotangent of dq, caller packing
+    const float* params;  // n_members * QG_NPARAMS
+    float* direct;        // x-row plane: cotangent of qb from the stencil terms (null: none)
+    float* rhs;           // FP32 x-row modal plane: Cm2l^T Z psi_bar (zeroed before the stencil)
+    double* pacc;         // parameter cotangents (zeroed before the stencil)
+    void* xa;             // GEMM operand of the adjoint solve
+    int xa_fmt;
+    float* xq;            // its FP32 copy for the refinement residual (may be null)
+    int64_t xplane;
+};
+cudaError_t launch_vjp_stencil(const VjpArgs& v, cudaStream_t s);
+cudaError_t launch_vjp_operand(const VjpArgs& v, const float* psi_bar, cudaStream_t s);
+cudaError_t launch_vjp_finish(const VjpArgs& v, const float* xbar, float* qbar, float* pbar, cudaStream_t s);
+
 // host: cuTensorMapEncodeTiled through the driver entry point (no libcuda link needed)
 cudaError_t tmap_encode(void* map, int bf16, int rank, const void* base, const uint64_t* dims,
                         const uint64_t* strides_bytes, const uint32_t* box, int swizzle128);

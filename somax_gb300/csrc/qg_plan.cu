@@ -237,6 +237,7 @@ struct qg_plan {
     float* params = nullptr;  // plan-owned copy of the params (graph-stable)
     int* flags = nullptr;
     double* diag_acc = nullptr;
+    double* vjp_acc = nullptr;  // parameter cotangents of qg_rhs_vjp (QG_NPARAMS per member)
     int op_fmt = FMT_F32;
     void* tc_maps = nullptr;  // TMA descriptors of the tensor-core GEMMs
     void* st_maps = nullptr;  // TMA descriptors of the stencil halo boxes
@@ -539,6 +540,27 @@ cudaError_t tmap_encode(void* map, int bf16, int rank, const void* base, const u
 // =======================================================================================
 // C ABI
 // =======================================================================================
+namespace {
+
+VjpArgs vjp_args(qg_plan* p) {
+    VjpArgs v{};
+    v.members = p->md;
+    v.tiles = p->st_tiles;
+    v.ntiles = p->n_st;
+    v.tile_x = p->st_large ? kTileLX : kTileSX;
+    v.tile_y = p->st_large ? kTileLY : kTileSY;
+    v.max_nl = p->max_nl;
+    v.n_members = p->n_members;
+    v.pacc = p->vjp_acc;
+    v.xa = p->XA;
+    v.xa_fmt = p->op_fmt;
+    v.xq = p->XQ;
+    v.xplane = p->xplane;
+    return v;
+}
+
+}  // namespace
+
 extern "C" {
 
 const char* qg_strerror(int code) {
@@ -706,6 +728,7 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
             !(e = dalloc(p, &p->S2, xb)) && !(e = dalloc(p, &p->params, (size_t)n_members * QG_NPARAMS * 4)) &&
             !(e = dalloc(p, &p->flags, 16)) && !(e = dalloc(p, &p->bar, 16)))
             e = dalloc(p, &p->diag_acc, (size_t)2 * p->total_layers * sizeof(double));
+        if (!e) e = dalloc(p, &p->vjp_acc, (size_t)n_members * QG_NPARAMS * sizeof(double));
         if (!e && o.refine_sweeps > 0) e = dalloc(p, &p->XQ, xb);
     }
     if (e == cudaSuccess && tc) {
@@ -889,6 +912,47 @@ int qg_step(qg_plan* p, float* q, const float* params, double dt, int n_steps, i
         e = timed(p, QG_K_OTHER, s, [&] {
             return launch_unpack(p->md, p->st_tiles, p->n_st, p->st_large, p->S0, q, s, use_pdl(p));
         });
+    return cuda_err(e);
+}
+
+int qg_rhs_vjp(qg_plan* p, const float* q, const float* params, const float* dq_bar, float* q_bar,
+               float* params_bar, int flags, void* stream) {
+    if (!p || !q || !params || !dq_bar || !q_bar) return QG_ERR_NULL;
+    if (flags & ~QG_RHS_APPLY_BC) return QG_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int bc = (flags & QG_RHS_APPLY_BC) ? 1 : 0;
+    // forward psi (layer, caller packing) into the YA plane, which holds at least one field
+    cudaError_t e = run_prep(p, q, nullptr, 0, bc, s);
+    if (!e) e = run_dst_solve(p, s);
+    if (!e)
+        e = timed(p, QG_K_OTHER, s, [&] {
+            return launch_mode_to_layer(p->md, p->st_tiles, p->n_st, p->st_large, p->XC, p->YA, s, use_pdl(p));
+        });
+    // stencil transposes: direct cotangent into S2, the adjoint solve's modal rhs into XB
+    VjpArgs v = vjp_args(p);
+    v.q = q;
+    v.apply_bc = bc;
+    v.psi = p->YA;
+    v.gbar = dq_bar;
+    v.params = params;
+    v.direct = p->S2;
+    v.rhs = p->XB;
+    if (!e) e = cudaMemsetAsync(p->XB, 0, (size_t)p->xplane * sizeof(float), s);
+    if (!e) e = cudaMemsetAsync(p->vjp_acc, 0, (size_t)p->n_members * QG_NPARAMS * sizeof(double), s);
+    if (!e) e = timed(p, QG_K_STENCIL, s, [&] { return launch_vjp_stencil(v, s); });
+    if (!e) e = timed(p, QG_K_PREP, s, [&] { return launch_vjp_operand(v, nullptr, s); });
+    if (!e) e = run_dst_solve(p, s);
+    if (!e) e = timed(p, QG_K_OTHER, s, [&] { return launch_vjp_finish(v, p->XC, q_bar, params_bar, s); });
+    return cuda_err(e);
+}
+
+int qg_invert_vjp(qg_plan* p, const float* psi_bar, float* q_bar, void* stream) {
+    if (!p || !psi_bar || !q_bar) return QG_ERR_NULL;
+    cudaStream_t s = (cudaStream_t)stream;
+    VjpArgs v = vjp_args(p);
+    cudaError_t e = timed(p, QG_K_PREP, s, [&] { return launch_vjp_operand(v, psi_bar, s); });
+    if (!e) e = run_dst_solve(p, s);
+    if (!e) e = timed(p, QG_K_OTHER, s, [&] { return launch_vjp_finish(v, p->XC, q_bar, nullptr, s); });
     return cuda_err(e);
 }
 

@@ -18,7 +18,7 @@ from typing import Sequence
 import numpy as np
 import torch
 
-from . import _lib
+from . import _lib, adjoint
 from ._lib import K, MemberDesc, Options, check
 from .transforms import ModalTransform, StratificationProfile
 
@@ -236,6 +236,35 @@ class Plan:
                              C.c_void_p(params.data_ptr()), flags, _stream_handle(q.device)), "qg_rhs")
         return out
 
+    def _params(self, params: torch.Tensor, device) -> torch.Tensor:
+        params = params.detach().to(device=device, dtype=torch.float32).contiguous()
+        if params.numel() != 4 * len(self.members):
+            raise ValueError("params must hold 4 values per member")
+        return params
+
+    def rhs_vjp(self, q: torch.Tensor, params: torch.Tensor, dq_bar: torch.Tensor, apply_bc=False,
+                want_params=True):
+        """(q_bar, params_bar) of ``rhs(q, params, apply_bc)`` for the cotangent ``dq_bar``."""
+        self._check_field(q, "q")
+        self._check_field(dq_bar, "dq_bar")
+        params = self._params(params, q.device)
+        q_bar = torch.empty_like(q)
+        p_bar = torch.empty_like(params) if want_params else None
+        flags = K["QG_RHS_APPLY_BC"] if apply_bc else 0
+        check(self._L.qg_rhs_vjp(self._h, C.c_void_p(q.data_ptr()), C.c_void_p(params.data_ptr()),
+                                 C.c_void_p(dq_bar.data_ptr()), C.c_void_p(q_bar.data_ptr()),
+                                 C.c_void_p(p_bar.data_ptr() if p_bar is not None else None), flags,
+                                 _stream_handle(q.device)), "qg_rhs_vjp")
+        return q_bar, p_bar
+
+    def invert_vjp(self, psi_bar: torch.Tensor) -> torch.Tensor:
+        """q_bar of ``invert(q)`` for the cotangent ``psi_bar`` (the map is linear in q)."""
+        self._check_field(psi_bar, "psi_bar")
+        q_bar = torch.empty_like(psi_bar)
+        check(self._L.qg_invert_vjp(self._h, C.c_void_p(psi_bar.data_ptr()), C.c_void_p(q_bar.data_ptr()),
+                                    _stream_handle(psi_bar.device)), "qg_invert_vjp")
+        return q_bar
+
     def step(self, q: torch.Tensor, params: torch.Tensor, dt: float, n_steps: int, scheme: str,
              apply_bc: bool = True) -> torch.Tensor:
         """Advance q in place: BC on every stage input; ``apply_bc`` zeroes the ring of the
@@ -397,16 +426,32 @@ class _QGBase(SomaxModel):
     def _param_vector(self, device) -> torch.Tensor:
         return self.params.vector(device)
 
+    def _param_tensors(self):
+        p = self.params
+        return (p.lateral_viscosity, p.bottom_drag, p.wind_amplitude, p.biharmonic_viscosity)
+
+    @staticmethod
+    def _grad_needed(*ts) -> bool:
+        return torch.is_grad_enabled() and any(isinstance(t, torch.Tensor) and t.requires_grad for t in ts)
+
     # -- reference API -------------------------------------------------------------------
     def _invert_pv(self, q: torch.Tensor) -> torch.Tensor:
+        """psi from q; differentiable in q (hand-written adjoint, ``qg_invert_vjp``)."""
         q = self._field(q)
-        return self.plan(q.device).invert(q)
+        plan = self.plan(q.device)
+        if self._grad_needed(q):
+            return adjoint.invert(plan, q)
+        return plan.invert(q)
 
     def vector_field(self, t, state, args=None):
-        """dq/dt for ``state.q`` as given (no BC applied, like the reference)."""
+        """dq/dt for ``state.q`` as given (no BC applied, like the reference); differentiable
+        in q and the parameters (hand-written adjoint, ``qg_rhs_vjp``)."""
         q = self._field(state.q)
-        dq = self.plan(q.device).rhs(q, self._param_vector(q.device), apply_bc=False)
-        return self.state_cls(q=dq)
+        pv = self._param_vector(q.device)
+        plan = self.plan(q.device)
+        if self._grad_needed(q, pv):
+            return self.state_cls(q=adjoint.rhs(plan, q, pv, apply_bc=False))
+        return self.state_cls(q=plan.rhs(q, pv, apply_bc=False))
 
     def apply_boundary_conditions(self, state):
         return self.state_cls(q=_zero_ring(state.q))
@@ -467,9 +512,15 @@ class _QGBase(SomaxModel):
         return y
 
     def integrate(self, state0, t0: float, t1: float, dt: float, solver=None, saveat=None, **kw):
-        """``SomaxModel.integrate`` with constant steps (``core/model.py:53-88``)."""
+        """``SomaxModel.integrate`` with constant steps (``core/model.py:53-88``).
+
+        Differentiable in ``state0.q`` and the parameters: when either requires grad, each
+        saved interval runs through the checkpointed adjoint (``checkpoint_every`` steps per
+        checkpoint, default 10), as diffrax's recursive-checkpoint adjoint does for the
+        reference's ``eqx.filter_grad`` (``tests/models/test_qg_baroclinic.py:293-312``)."""
         if kw.get("stepsize_controller") not in (None, "constant"):
             raise ValueError("only constant step sizes are supported")
+        every = int(kw.get("checkpoint_every", 10))
         scheme = _solver_name(solver)
         saveat = saveat or SaveAt(t1=True)
         n_total = int(round((t1 - t0) / dt))
@@ -482,12 +533,21 @@ class _QGBase(SomaxModel):
         state = self.apply_boundary_conditions(state0)
         ys, done = [], 0
         q = state.q
+        pv = None
+        grad = self._grad_needed(q) or self._grad_needed(*self._param_tensors())
+        if grad:
+            q = self._field(q)
+            pv = self._param_vector(q.device)
         for tgt in targets:
             if tgt < done:
                 raise ValueError("saveat.ts must be increasing")
             if tgt > done:
                 # one continuous integration: only the first chunk starts from a BC'd state
-                q = self.step(self.state_cls(q=q), dt, tgt - done, scheme, apply_bc=False).q
+                if grad:
+                    q = adjoint.integrate(self.plan(q.device), q, pv, dt, tgt - done, scheme, apply_bc=False,
+                                          checkpoint_every=every)
+                else:
+                    q = self.step(self.state_cls(q=q), dt, tgt - done, scheme, apply_bc=False).q
                 done = tgt
             ys.append(q.clone())
         ts = torch.tensor([t0 + k * dt for k in targets], dtype=torch.float64)
