@@ -108,8 +108,9 @@ typedef struct qg_options {
     int use_graphs;     /* 1: qg_step replays a captured CUDA graph per step */
     int persistent;     /* 1: qg_step advances all steps in one persistent cooperative launch
                            (tensor-core precisions without refinement) */
-    int autotune;       /* 1: qg_plan_create times the stencil tile shapes and keeps the faster */
-    int reserved[3];
+    int autotune;       /* 1: qg_plan_create times the stencil variants and keeps the fastest */
+    int stencil;        /* 0: autotuner's choice; QG_STENCIL_* + 1: run that variant */
+    int reserved[2];
 } qg_options;
 
 typedef struct qg_plan qg_plan;
@@ -186,9 +187,19 @@ const char* qg_strerror(int code);
 int qg_set_profiling(qg_plan* plan, int enable); /* resets the counters */
 int qg_kernel_stats(qg_plan* plan, int kclass, double* total_ms, int64_t* launches);
 
-/* The plan's tuned choices: stencil tile shape (0 = 32 x 8, 1 = 64 x 16) and the autotuner's
-   per-launch times of both shapes in ms (-1 when not measured). */
-int qg_plan_tuning(const qg_plan* plan, int* tile_shape, float* ms_small, float* ms_large);
+/* Stencil variants the autotuner times (one RK stage each: the four DST passes and the
+   step-mode stencil, on the plan's own planes):
+   the tile stencil with 32 x 8 or 64 x 16 tiles (TMA halo boxes; also the persistent kernel's
+   stencil phase) and the column-sweep stencil with 16-, 32- or 64-row strips. */
+#define QG_STENCIL_TILE_32X8 0
+#define QG_STENCIL_TILE_64X16 1
+#define QG_STENCIL_SWEEP_16 2
+#define QG_STENCIL_SWEEP_32 3
+#define QG_STENCIL_SWEEP_64 4
+#define QG_STENCIL_VARIANTS 5
+/* The plan's tuned choice: *variant = the stencil the multi-launch path runs; ms[k] (k < n)
+   the autotuner's time of one stage with variant k in ms (-1 when not measured). */
+int qg_plan_tuning(const qg_plan* plan, int* variant, float* ms, int n);
 
 #ifdef __cplusplus
 }

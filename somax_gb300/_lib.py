@@ -51,7 +51,8 @@ class MemberDesc(C.Structure):
 
 class Options(C.Structure):
     _fields_ = [("dst_precision", C.c_int), ("refine_sweeps", C.c_int), ("use_graphs", C.c_int),
-                ("persistent", C.c_int), ("autotune", C.c_int), ("reserved", C.c_int * 3)]
+                ("persistent", C.c_int), ("autotune", C.c_int), ("stencil", C.c_int),
+                ("reserved", C.c_int * 2)]
 
 
 _lib = None
@@ -85,7 +86,7 @@ def lib() -> C.CDLL:
         "qg_strerror": (C.c_char_p, [C.c_int]),
         "qg_set_profiling": (C.c_int, [vp, C.c_int]),
         "qg_kernel_stats": (C.c_int, [vp, C.c_int, C.POINTER(C.c_double), C.POINTER(i64)]),
-        "qg_plan_tuning": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+        "qg_plan_tuning": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_float), C.c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

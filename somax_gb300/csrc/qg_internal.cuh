@@ -122,7 +122,21 @@ struct StencilArgs {
     int xa_fmt;
     float* xq;             // FP32 copy of the modal q for the refinement residual; may be null
     int* flags;            // device status word
+    // the column-sweep stencil reads the planes directly
+    const float* qin;      // stage plane holding the input q (x-row)
+    const float* psi_hat;  // psi_hat plane (x-row)
 };
+
+// Work item of the column-sweep stencil: strip sx (28 output columns) of row block sy.
+struct SweepItem {
+    int member, sx, sy;
+};
+int sweep_columns();
+int sweep_warps_per_block();
+int sweep_blocks_per_sm(int nl);
+// one launch per layer count k + 1 with n_items[k] > 0 (items grouped by layer count)
+cudaError_t launch_sweep(const StencilArgs& a, const SweepItem* const* items, const int* n_items, int R,
+                         const int* grid, cudaStream_t s, bool pdl);
 
 // launchers (return cudaError_t of the launch)
 cudaError_t launch_prep(const PrepArgs& a, int ntiles, cudaStream_t s, bool pdl);

@@ -249,7 +249,16 @@ struct qg_plan {
     StencilTile* st_tiles_v[2] = {nullptr, nullptr};
     int n_st_v[2] = {0, 0};
     void* st_maps_v[2] = {nullptr, nullptr};
-    float tune_ms[2] = {-1.f, -1.f};
+    float tune_ms[QG_STENCIL_VARIANTS] = {-1.f, -1.f, -1.f, -1.f, -1.f};
+    // column-sweep stencil: item lists for 16-, 32- and 64-row strips; sw_sel = the one the
+    // multi-launch path runs (-1: the tile stencil)
+    SweepItem* sw_items_v[3] = {nullptr, nullptr, nullptr};
+    int n_sw_v[3] = {0, 0, 0};
+    // items of each list grouped by layer count: group k (k + 1 layers) at offset sw_off
+    int sw_off[3][kMaxLayers] = {};
+    int sw_cnt[3][kMaxLayers] = {};
+    int sw_sel = -1;
+    int sw_grid[kMaxLayers] = {};
     PersistArgs pa{};         // constant part of the tensor-core launches' arguments
     // graphs
     cudaStream_t cap = nullptr;
@@ -397,6 +406,22 @@ StencilArgs stencil_args(qg_plan* p, const float* params) {
     return a;
 }
 
+constexpr int kSweepRows[3] = {16, 32, 64};
+
+// The multi-launch path's stencil launch: the column sweep if selected, else the tiles.
+cudaError_t launch_stencil(qg_plan* p, StencilArgs a, cudaStream_t s, bool pdl) {
+    const float* planes[3] = {p->S0, p->S1, p->S2};
+    a.qin = planes[a.q_sel];
+    a.psi_hat = p->XC;
+    if (p->sw_sel >= 0) {
+        const int v = p->sw_sel;
+        const SweepItem* items[kMaxLayers];
+        for (int k = 0; k < kMaxLayers; ++k) items[k] = p->sw_items_v[v] + p->sw_off[v][k];
+        return launch_sweep(a, items, p->sw_cnt[v], kSweepRows[v], p->sw_grid, s, pdl);
+    }
+    return launch_stencil_mt(a, p->n_st, p->st_grid, p->max_nl, p->st_large, s, pdl);
+}
+
 struct Stage {
     float a, b;
 };
@@ -439,13 +464,23 @@ cudaError_t run_one_step(qg_plan* p, const float* params, float dt, int scheme, 
         a.dt = dt;
         a.xa = p->XA;
         a.xq = p->XQ;
-        e = timed(p, QG_K_STENCIL, s, [&] { return launch_stencil_mt(a, p->n_st, p->st_grid, p->max_nl, p->st_large, s, use_pdl(p)); });
+        e = timed(p, QG_K_STENCIL, s, [&] { return launch_stencil(p, a, s, use_pdl(p)); });
         if (e) return e;
     }
     return cudaSuccess;
 }
 
 int cuda_err(cudaError_t e) { return e == cudaSuccess ? QG_OK : QG_ERR_CUDA; }
+
+void select_sweep(qg_plan* p, int v) {
+    p->sw_sel = v;
+    if (v < 0) return;
+    const int per_cta = sweep_warps_per_block();  // one strip per warp
+    for (int k = 0; k < kMaxLayers; ++k) {
+        const int ctas = (p->sw_cnt[v][k] + per_cta - 1) / per_cta;
+        p->sw_grid[k] = std::max(1, std::min(ctas, sweep_blocks_per_sm(k + 1) * std::max(p->n_sm, 1)));
+    }
+}
 
 // Make stencil tile shape `large` the active one (tile list, TMA maps, launch grid).
 void select_tile(qg_plan* p, int large) {
@@ -463,46 +498,61 @@ void select_tile(qg_plan* p, int large) {
     if (p->opts.dst_precision != QG_DST_FP32) persistent_smem_bytes(p->opts.dst_precision, p->max_nl, large, &a);
 }
 
-// Autotuner: time one step-mode stencil launch of each tile shape on the plan's own planes
-// (zero state, zero parameters) with CUDA events and keep the faster shape.
+// Autotuner: time every stencil variant (tile shapes, sweep strip heights) in its setting,
+// one RK stage (the four DST passes, then the step-mode stencil) on the plan's own planes
+// (zero state, zero parameters), with CUDA events; the passes are common to all variants,
+// so the differences are the stencil's, including what the GEMM passes leave in L2.  The
+// fastest tile shape is the persistent kernel's; the fastest variant overall is the
+// multi-launch path's.
 cudaError_t autotune_stencil(qg_plan* p) {
     cudaStream_t s = p->cap;
     cudaEvent_t e0, e1;
     cudaError_t e = cudaEventCreate(&e0);
     if (!e) e = cudaEventCreate(&e1);
     if (e) return e;
-    float best = 0.f;
-    int pick = p->st_large;
-    for (int v = 0; v < 2 && !e; ++v) {
-        select_tile(p, v);
+    const int tile_default = p->st_large;
+    for (int v = 0; v < QG_STENCIL_VARIANTS && !e; ++v) {
+        if (v < 2) {
+            select_tile(p, v);
+            select_sweep(p, -1);
+        } else {
+            select_tile(p, tile_default);
+            select_sweep(p, v - 2);
+        }
         StencilArgs a = stencil_args(p, p->params);
         a.q_sel = 1;
         a.apply_bc = 1;
         a.y0 = p->S0;
         a.y_next = p->S2;
-        a.a = 0.f;
-        a.b = 1.f;
+        a.a = 0.5f;
+        a.b = 0.5f;
         a.dt = 1.f;
         a.xa = p->XA;
         float ms = 0.f;
-        for (int rep = 0; rep < 2 && !e; ++rep)
-            e = launch_stencil_mt(a, p->n_st, p->st_grid, p->max_nl, v, s, false);
+        for (int rep = 0; rep < 1 && !e; ++rep) {
+            e = run_dst_solve(p, s);
+            if (!e) e = launch_stencil(p, a, s, false);
+        }
         if (!e) e = cudaEventRecord(e0, s);
-        for (int rep = 0; rep < 5 && !e; ++rep)
-            e = launch_stencil_mt(a, p->n_st, p->st_grid, p->max_nl, v, s, false);
+        for (int rep = 0; rep < 3 && !e; ++rep) {
+            e = run_dst_solve(p, s);
+            if (!e) e = launch_stencil(p, a, s, false);
+        }
         if (!e) e = cudaEventRecord(e1, s);
         if (!e) e = cudaEventSynchronize(e1);
         if (!e) e = cudaEventElapsedTime(&ms, e0, e1);
-        p->tune_ms[v] = ms / 5.f;
-        if (!e && (v == 0 || ms < best)) {
-            best = ms;
-            pick = v;
-        }
+        p->tune_ms[v] = ms / 3.f;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    if (!e) select_tile(p, pick);
-    if (!e) e = cudaMemsetAsync(p->S2, 0, sizeof(float) * p->xplane, s);
+    if (e) return e;
+    const int tile = p->tune_ms[1] < p->tune_ms[0] ? 1 : 0;
+    int best = tile;
+    for (int v = 2; v < QG_STENCIL_VARIANTS; ++v)
+        if (p->tune_ms[v] < p->tune_ms[best]) best = v;
+    select_tile(p, tile);
+    select_sweep(p, best >= 2 ? best - 2 : -1);
+    e = cudaMemsetAsync(p->S2, 0, sizeof(float) * p->xplane, s);
     if (!e) e = cudaMemsetAsync(p->XA, 0, sizeof(float) * p->xplane, s);
     if (!e) e = cudaStreamSynchronize(s);
     return e;
@@ -582,6 +632,7 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
     if (opts) o = *opts;
     if (o.dst_precision < QG_DST_FP32 || o.dst_precision > QG_DST_BF16X3) return QG_ERR_ARG;
     if (o.refine_sweeps < 0 || o.refine_sweeps > 1) return QG_ERR_ARG;
+    if (o.stencil < 0 || o.stencil > QG_STENCIL_VARIANTS) return QG_ERR_ARG;
     for (int i = 0; i < n_members; ++i) {
         const int v = validate_member(members[i]);
         if (v != QG_OK) return v;
@@ -614,6 +665,7 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
         p->st_large = large_tiles >= 2 * (int64_t)std::max(p->n_sm, 1);
     }
     std::vector<StencilTile> st_v[2];
+    std::vector<SweepItem> sw_v[3];
     // geometry and offsets
     p->mh.resize(n_members);
     int64_t off_state = 0, off_x = 0, off_y = 0, off_layer = 0;
@@ -692,6 +744,12 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
             M.Sx_bf = bx;
             M.Sy_bf = byy;
         }
+        // column-sweep strips
+        for (int v = 0; v < 3; ++v) {
+            const int R = kSweepRows[v], W = sweep_columns();
+            for (int sy = 0; sy < (M.Ny + R - 1) / R; ++sy)
+                for (int sx = 0; sx < (M.Nx + W - 1) / W; ++sx) sw_v[v].push_back({i, sx, sy});
+        }
         // tiles
         for (int v = 0; v < 2; ++v) {
             const int TX = v ? kTileLX : kTileSX, TY = v ? kTileLY : kTileSY;
@@ -717,6 +775,18 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
         for (int v = 0; v < 2 && !e; ++v) {
             p->n_st_v[v] = (int)st_v[v].size();
             e = upload(p, &p->st_tiles_v[v], st_v[v]);
+        }
+        for (int v = 0; v < 3 && !e; ++v) {
+            // group by layer count: one sweep launch per group
+            std::vector<SweepItem> g;
+            for (int k = 0; k < kMaxLayers; ++k) {
+                p->sw_off[v][k] = (int)g.size();
+                for (const SweepItem& it : sw_v[v])
+                    if (members[it.member].n_layers == k + 1) g.push_back(it);
+                p->sw_cnt[v][k] = (int)g.size() - p->sw_off[v][k];
+            }
+            p->n_sw_v[v] = (int)g.size();
+            e = upload(p, &p->sw_items_v[v], g);
         }
         if (!e && !(e = upload(p, &p->gx_tiles, gx))) e = upload(p, &p->gy_tiles, gy);
     }
@@ -778,6 +848,12 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
         a.bar_gen = p->bar + 1;
         select_tile(p, p->st_large);
         if (o.autotune) e = autotune_stencil(p);
+        if (!e && o.stencil > 0) {
+            // a forced variant (tests, benchmarks of one variant)
+            const int v = o.stencil - 1;
+            if (v < 2) select_tile(p, v);
+            select_sweep(p, v >= 2 ? v - 2 : -1);
+        }
     }
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
@@ -846,7 +922,7 @@ int qg_rhs(qg_plan* p, const float* q, float* dq, const float* params, int flags
         a.q_sel = 1;
         a.apply_bc = bc;
         a.dq = dq;
-        e = timed(p, QG_K_STENCIL, s, [&] { return launch_stencil_mt(a, p->n_st, p->st_grid, p->max_nl, p->st_large, s, use_pdl(p)); });
+        e = timed(p, QG_K_STENCIL, s, [&] { return launch_stencil(p, a, s, use_pdl(p)); });
     }
     return cuda_err(e);
 }
@@ -985,11 +1061,10 @@ int qg_status(qg_plan* p, int* flags, void* stream) {
     return QG_OK;
 }
 
-int qg_plan_tuning(const qg_plan* p, int* tile_shape, float* ms_small, float* ms_large) {
+int qg_plan_tuning(const qg_plan* p, int* variant, float* ms, int n) {
     if (!p) return QG_ERR_NULL;
-    if (tile_shape) *tile_shape = p->st_large;
-    if (ms_small) *ms_small = p->tune_ms[0];
-    if (ms_large) *ms_large = p->tune_ms[1];
+    if (variant) *variant = p->sw_sel >= 0 ? 2 + p->sw_sel : p->st_large;
+    for (int k = 0; ms && k < n && k < QG_STENCIL_VARIANTS; ++k) ms[k] = p->tune_ms[k];
     return QG_OK;
 }
 

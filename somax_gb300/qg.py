@@ -166,7 +166,7 @@ class Plan:
     """Owns a ``qg_plan`` (device constants + workspace) on one CUDA device."""
 
     def __init__(self, members: Sequence["MemberSpec"], precision="fp32", refine=0, use_graphs=True,
-                 device=None, persistent=True, autotune=True):
+                 device=None, persistent=True, autotune=True, stencil=None):
         if not torch.cuda.is_available():
             raise RuntimeError("somax_gb300 needs a CUDA device (no CPU fallback)")
         self.device = torch.device(device or "cuda", torch.cuda.current_device()) if device is None \
@@ -175,8 +175,9 @@ class Plan:
         arr = (MemberDesc * len(members))()
         for i, m in enumerate(members):
             m.fill(arr[i])
+        forced = 0 if stencil is None else 1 + self.STENCIL_VARIANTS.index(stencil)
         opts = Options(PRECISIONS[precision], int(refine), int(bool(use_graphs)), int(bool(persistent)),
-                       int(bool(autotune)))
+                       int(bool(autotune)), forced)
         handle = C.c_void_p()
         with torch.cuda.device(self.device):
             check(L.qg_plan_create(arr, len(members), C.byref(opts), C.byref(handle)), "qg_plan_create")
@@ -299,14 +300,23 @@ class Plan:
         stages = {"heun": 2, "ssprk3": 3}[scheme]
         if self.persistent and self.precision != "fp32" and self.refine == 0:
             return 3  # pack, the persistent step kernel, unpack
-        per_stage = 4 * (1 + self.refine) + self.refine + 1
+        # the column-sweep stencil launches once per distinct layer count
+        sweep = self.tuning()["stencil"].startswith("sweep")
+        stencil = len({m.n_layers for m in self.members}) if sweep else 1
+        per_stage = 4 * (1 + self.refine) + self.refine + stencil
         return 2 + n_steps * stages * per_stage
 
+    STENCIL_VARIANTS = ("tile32x8", "tile64x16", "sweep16", "sweep32", "sweep64")
+
     def tuning(self) -> dict:
-        shape = C.c_int()
-        a, b = C.c_float(), C.c_float()
-        check(self._L.qg_plan_tuning(self._h, C.byref(shape), C.byref(a), C.byref(b)), "qg_plan_tuning")
-        return {"stencil_tile": "64x16" if shape.value else "32x8", "ms_32x8": a.value, "ms_64x16": b.value}
+        """The autotuner's stencil choice and the time (ms) of one RK stage (four DST passes
+        and the stencil) it measured with every variant."""
+        v = C.c_int()
+        n = len(self.STENCIL_VARIANTS)
+        ms = (C.c_float * n)()
+        check(self._L.qg_plan_tuning(self._h, C.byref(v), ms, n), "qg_plan_tuning")
+        return {"stencil": self.STENCIL_VARIANTS[v.value],
+                "ms": {name: round(float(t), 5) for name, t in zip(self.STENCIL_VARIANTS, ms)}}
 
     def set_profiling(self, on: bool):
         check(self._L.qg_set_profiling(self._h, int(on)), "qg_set_profiling")
@@ -389,13 +399,14 @@ class _QGBase(SomaxModel):
     barotropic = False
 
     def __init__(self, spec: MemberSpec, params: QGParams, precision="fp32", refine=0, use_graphs=True,
-                 strat=None, modal=None, persistent=True):
+                 strat=None, modal=None, persistent=True, stencil=None):
         self.spec = spec
         self.params = params
         self.precision = precision
         self.refine = refine
         self.use_graphs = use_graphs
         self.persistent = persistent
+        self.stencil = stencil
         self.strat = strat
         self.modal = modal
         self.grid = Grid(spec.nx, spec.ny, spec.Lx, spec.Ly)
@@ -408,7 +419,8 @@ class _QGBase(SomaxModel):
             device = torch.device("cuda", torch.cuda.current_device())
         key = device.index
         if key not in self._plans:
-            self._plans[key] = Plan([self.spec], self.precision, self.refine, self.use_graphs, device, self.persistent)
+            self._plans[key] = Plan([self.spec], self.precision, self.refine, self.use_graphs, device, self.persistent,
+                                    stencil=self.stencil)
         return self._plans[key]
 
     @property
@@ -597,7 +609,7 @@ class BaroclinicQG(_QGBase):
                H=(400.0, 1100.0, 2600.0), g_prime=(9.81, 0.025, 0.0125), stratification=None,
                lateral_viscosity=0.0, bottom_drag=0.0, wind_amplitude=0.0, wind_profile="doublegyre",
                poisson_bc="dst", biharmonic_viscosity=0.0, precision="fp32", refine=0, eigs="consistent",
-               use_graphs=True, persistent=True) -> "BaroclinicQG":
+               use_graphs=True, persistent=True, stencil=None) -> "BaroclinicQG":
         """``BaroclinicQG.create`` (``baroclinic.py:230-332``) with the same keyword arguments,
         plus ``biharmonic_viscosity`` (extension), ``precision`` of the DST-I GEMMs
         ("fp32", "tf32", "bf16x3"), ``refine`` sweeps, the ``eigs`` mode and whether ``step`` runs
@@ -616,7 +628,7 @@ class BaroclinicQG(_QGBase):
                           eigs, modal)
         params = QGParams(*(torch.tensor(float(v)) for v in (lateral_viscosity, bottom_drag, wind_amplitude,
                                                              biharmonic_viscosity)))
-        return BaroclinicQG(spec, params, precision, refine, use_graphs, strat, modal, persistent)
+        return BaroclinicQG(spec, params, precision, refine, use_graphs, strat, modal, persistent, stencil)
 
     @property
     def n_layers(self):
@@ -632,12 +644,12 @@ class BarotropicQG(_QGBase):
     @staticmethod
     def create(nx=64, ny=64, Lx=1e6, Ly=1e6, f0=1e-4, beta=1.6e-11, lateral_viscosity=0.0,
                bottom_drag=0.0, wind_amplitude=0.0, wind_profile="doublegyre", biharmonic_viscosity=0.0,
-               precision="fp32", refine=0, use_graphs=True, persistent=True) -> "BarotropicQG":
+               precision="fp32", refine=0, use_graphs=True, persistent=True, stencil=None) -> "BarotropicQG":
         """``BarotropicQG.create`` (``barotropic.py:186-248``)."""
         spec = MemberSpec(nx, ny, Lx, Ly, f0, beta, [1.0], [1.0], True, wind_profile)
         params = QGParams(*(torch.tensor(float(v)) for v in (lateral_viscosity, bottom_drag, wind_amplitude,
                                                              biharmonic_viscosity)))
-        return BarotropicQG(spec, params, precision, refine, use_graphs, persistent=persistent)
+        return BarotropicQG(spec, params, precision, refine, use_graphs, persistent=persistent, stencil=stencil)
 
 
 class QGEnsemble:
@@ -646,11 +658,12 @@ class QGEnsemble:
     tensor-core precisions).  States are packed member after member in the reference layout."""
 
     def __init__(self, models: Sequence[_QGBase], precision="bf16x3", refine=0, use_graphs=True, persistent=True,
-                 device=None):
+                 device=None, stencil=None):
         if not models:
             raise ValueError("an ensemble needs at least one member")
         self.models = list(models)
-        self.plan = Plan([m.spec for m in self.models], precision, refine, use_graphs, device, persistent)
+        self.plan = Plan([m.spec for m in self.models], precision, refine, use_graphs, device, persistent,
+                         stencil=stencil)
         self.offsets = self.plan.offsets
         self.sizes = [int(np.prod(m.shape)) for m in self.models]
 

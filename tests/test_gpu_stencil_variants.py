@@ -1,0 +1,84 @@
+"""Every stencil variant (tile 32x8 / 64x16 with TMA halo boxes, column sweep with 16-, 32- and
+64-row strips) against the float64 oracle, forced through ``qg_options.stencil`` so that the
+autotuner's pick does not decide what is tested.  FP32 GEMMs isolate the stencil; the
+ensemble case mixes layer counts (the sweep launches once per layer count)."""
+
+import numpy as np
+import pytest
+import torch
+
+import somax_gb300 as sg
+from oracle import qg as O
+from somax_gb300 import testcases as tc
+
+pytestmark = pytest.mark.gpu
+
+RTOL_RHS = 2e-5
+RTOL_STEP = 1e-5
+VARIANTS = sg.Plan.STENCIL_VARIANTS
+
+
+def rel(a, b):
+    a = a.detach().cpu().double().numpy() if isinstance(a, torch.Tensor) else a
+    b = b.detach().cpu().double().numpy() if isinstance(b, torch.Tensor) else b
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def pair(nx, ny, nl, seed):
+    H = (400.0, 1100.0, 2600.0, 900.0, 1500.0, 700.0, 300.0, 2000.0)[:nl] if nl > 1 else (4000.0,)
+    g = (9.81, 0.025, 0.0125, 0.01, 0.008, 0.006, 0.004, 0.003)[:nl] if nl > 1 else (0.0055,)
+    kw = dict(lateral_viscosity=60.0, bottom_drag=1e-7, wind_amplitude=1e-10, biharmonic_viscosity=1e9)
+    m = sg.BaroclinicQG.create(nx=nx, ny=ny, Lx=1.2e6, Ly=1e6, n_layers=nl, H=H, g_prime=g, **kw)
+    o = O.baroclinic_model(nx=nx, ny=ny, Lx=1.2e6, Ly=1e6, H=H, g_prime=g, **kw)
+    rng = np.random.default_rng(seed)
+    q = tc.kminus3_field(max(nx, ny), seed, nl)[:, : ny + 2, : nx + 2] * 1e-6
+    q = q + 1e-7 * rng.standard_normal(q.shape)  # a non-zero ring too
+    return m, o, q
+
+
+SHAPES = [(3, 5, 2), (17, 13, 3), (30, 30, 1), (61, 29, 3), (24, 24, 5), (40, 33, 8), (100, 70, 4)]
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+@pytest.mark.parametrize("nx,ny,nl", SHAPES)
+def test_variant_rhs_and_steps(variant, nx, ny, nl):
+    m, o, q = pair(nx, ny, nl, 40 + nl)
+    plan = sg.Plan([m.spec], "fp32", stencil=variant)
+    assert plan.tuning()["stencil"] == variant
+    pv = m._param_vector(torch.device("cuda"))
+    qd = torch.tensor(q, dtype=torch.float32, device="cuda")
+    for bc in (False, True):
+        ref = O.vector_field(o, O.zero_boundaries(q) if bc else q)
+        assert rel(plan.rhs(qd, pv, apply_bc=bc), ref) < RTOL_RHS
+    for scheme in ("heun", "ssprk3"):
+        got = plan.step(qd.clone(), pv, 1200.0, 3, scheme)
+        assert plan.status() == 0
+        assert rel(got, O.integrate(o, q, 1200.0, 3, scheme)) < RTOL_STEP
+
+
+@pytest.mark.parametrize("variant", ["sweep16", "sweep32", "sweep64"])
+def test_sweep_ensemble_mixed_layers(variant):
+    specs = [((30, 30), 1, 3), ((40, 33), 3, 4), ((24, 24), 5, 5), ((130, 66), 2, 6), ((17, 13), 3, 7)]
+    ms, os, qs = [], [], []
+    for (nx, ny), nl, seed in specs:
+        m, o, q = pair(nx, ny, nl, seed)
+        ms.append(m)
+        os.append(o)
+        qs.append(q)
+    ens = sg.QGEnsemble(ms, precision="bf16x3", persistent=False, stencil=variant)
+    packed = ens.pack([torch.tensor(q, dtype=torch.float32, device="cuda") for q in qs])
+    for d, o, q in zip(ens.unpack(ens.rhs(packed)), os, qs):
+        assert rel(d, O.vector_field(o, q)) < 1e-4  # split-BF16x3 inversion inside
+    ens.step(packed, 1200.0, 3, "ssprk3")
+    assert ens.plan.status() == 0
+    for got, o, q in zip(ens.unpack(packed), os, qs):
+        assert rel(got, O.integrate(o, q, 1200.0, 3, "ssprk3")) < RTOL_STEP
+
+
+def test_sweep_equals_tile_stencil():
+    m, _, q = pair(130, 98, 3, 9)
+    pv = m._param_vector(torch.device("cuda"))
+    qd = torch.tensor(q, dtype=torch.float32, device="cuda")
+    a = sg.Plan([m.spec], "fp32", stencil="tile32x8").step(qd.clone(), pv, 1200.0, 5, "ssprk3")
+    b = sg.Plan([m.spec], "fp32", stencil="sweep32").step(qd.clone(), pv, 1200.0, 5, "ssprk3")
+    assert rel(b, a) < 1e-6
