@@ -199,6 +199,7 @@ struct PersistArgs {
     const GemmTile* gy;
     const StencilTile* st;
     int n_gx, n_gy, n_st, max_nl;
+    int tile_n;               // DST GEMM output tile width (<= TC_BN, a multiple of 16)
     const void* tc_maps;
     const void* st_maps;
     void *XA, *YA, *YB, *XB;  // operand-format planes

@@ -115,7 +115,7 @@ __device__ void gemm_phase(const PersistArgs& a, uint8_t* smem, Shared& sh, uint
                     tma_load_2d(stg + q * tc_tile_a_bytes<PREC>(), &tm->a[q], &sh.full[s], kb * C::BK, tl.mt * TC_BM);
                 for (int q = 0; q < C::NB; ++q)
                     tma_load_2d(stg + C::NA * tc_tile_a_bytes<PREC>() + q * tc_tile_b_bytes<PREC>(), &tm->b[q],
-                                &sh.full[s], kb * C::BK, tl.nt * TC_BN);
+                                &sh.full[s], kb * C::BK, tl.nt * a.tile_n);
                 sh.issued = (int)++c.prod_kb;
             }
         }
@@ -127,13 +127,15 @@ __device__ void gemm_phase(const PersistArgs& a, uint8_t* smem, Shared& sh, uint
             const uint32_t buf = c.mma_tiles & 1, use = c.mma_tiles >> 1;
             if (!mbar_wait(&sh.tempty[buf], (use & 1) ^ 1, abort)) break;
             tc_fence_after();
-            const uint32_t acc = tmem + buf * TC_BN;
+            const uint32_t acc = tmem + buf * TC_TMEM_BUF;
+            const int width = tc_tile_width(g.Nn, tl.nt, a.tile_n);
             for (int kb = 0; kb < nkb; ++kb) {
                 const int s = c.mma_kb % C::STAGES;
                 if (!mbar_wait(&sh.full[s], (c.mma_kb / C::STAGES) & 1, abort)) break;
                 tc_fence_after();
                 const uint32_t sa = su32(smem + s * tc_stage_bytes<PREC>());
-                tc_mma_kblock<PREC>(acc, sa, sa + C::NA * tc_tile_a_bytes<PREC>(), kb == 0);
+                const int ksteps = (min(C::BK, g.K - kb * C::BK) + C::UMMA_K - 1) / C::UMMA_K;
+                tc_mma_kblock<PREC>(acc, sa, sa + C::NA * tc_tile_a_bytes<PREC>(), kb == 0, ksteps, width);
                 tc_commit(&sh.empty[s]);
                 sh.consumed = (int)++c.mma_kb;
             }
@@ -150,8 +152,9 @@ __device__ void gemm_phase(const PersistArgs& a, uint8_t* smem, Shared& sh, uint
             if (!have) break;
             tc_fence_after();
             float* stage = reinterpret_cast<float*>(smem + C::STAGES * tc_stage_bytes<PREC>()) + (warp - 4) * TC_STAGE_FLOATS;
-            tc_epilogue<PASS>(M, g, Cv, c_fmt, PASS == G4_INV_X ? a.g4_accumulate : 0, tl.mt * TC_BM, tl.nt * TC_BN,
-                              tmem + buf * TC_BN, warp & 3, lane, true, stage);
+            tc_epilogue<PASS>(M, g, Cv, c_fmt, PASS == G4_INV_X ? a.g4_accumulate : 0, tl.mt * TC_BM,
+                              tl.nt * a.tile_n, tc_tile_width(g.Nn, tl.nt, a.tile_n), tmem + buf * TC_TMEM_BUF,
+                              warp & 3, lane, true, stage);
             tc_fence_before();
             mbar_arrive(&sh.tempty[buf]);
             ++c.epi_tiles;
@@ -271,7 +274,7 @@ __global__ void __launch_bounds__(PT, 1) k_gemm_mt(PersistArgs a) {
     __shared__ Shared sh;
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     init_shared(sh, C::STAGES);
-    if ((threadIdx.x >> 5) == 1) tc_alloc(&sh.tmem_slot, 2 * TC_BN);
+    if ((threadIdx.x >> 5) == 1) tc_alloc(&sh.tmem_slot, TC_TMEM_COLS);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -286,7 +289,7 @@ __global__ void __launch_bounds__(PT, 1) k_gemm_mt(PersistArgs a) {
     __syncthreads();
     if ((threadIdx.x >> 5) == 1) {
         tc_fence_after();
-        tc_dealloc(tmem, 2 * TC_BN);
+        tc_dealloc(tmem, TC_TMEM_COLS);
     }
     if (threadIdx.x == 0 && sh.abort && a.flags) atomicOr(a.flags, 2);
 }
@@ -314,7 +317,7 @@ __global__ void __launch_bounds__(PT, 1) k_persistent(PersistArgs a) {
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const int warp = threadIdx.x >> 5;
     init_shared(sh, C::STAGES);
-    if (warp == 1) tc_alloc(&sh.tmem_slot, 2 * TC_BN);
+    if (warp == 1) tc_alloc(&sh.tmem_slot, TC_TMEM_COLS);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -343,7 +346,7 @@ done:
     __syncthreads();
     if (warp == 1) {
         tc_fence_after();
-        tc_dealloc(tmem, 2 * TC_BN);
+        tc_dealloc(tmem, TC_TMEM_COLS);
     }
 }
 

@@ -229,6 +229,13 @@ struct qg_plan {
     GemmTile* gx_tiles = nullptr;  // passes with A in x-row planes (G1, G4)
     GemmTile* gy_tiles = nullptr;  // passes with A in y-row planes (G2, G3)
     int n_gx = 0, n_gy = 0;
+    // tensor-core tile lists for each candidate output tile width (kGemmBN); the autotuner
+    // keeps the fastest (wide tiles for large members, narrow ones spread small members)
+    GemmTile* gx_v[3] = {nullptr, nullptr, nullptr};
+    GemmTile* gy_v[3] = {nullptr, nullptr, nullptr};
+    int n_gx_v[3] = {0, 0, 0}, n_gy_v[3] = {0, 0, 0};
+    int n_bn = 1, bn_sel = 0;
+    float tune_gemm_ms[3] = {-1.f, -1.f, -1.f};
     // device memory: x-row planes XA (modal operand), XB (V^T), XC (psi_hat), XQ (FP32 modal
     // rhs for refinement), S0 (state), S1/S2 (stage inputs); y-row planes YA (T1^T), YB (U)
     std::vector<void*> allocs;
@@ -407,6 +414,7 @@ StencilArgs stencil_args(qg_plan* p, const float* params) {
 }
 
 constexpr int kSweepRows[3] = {16, 32, 64};
+constexpr int kGemmBN[3] = {144, 80, 48};  // tensor-core output tile widths the autotuner tries
 
 // The multi-launch path's stencil launch: the column sweep if selected, else the tiles.
 cudaError_t launch_stencil(qg_plan* p, StencilArgs a, cudaStream_t s, bool pdl) {
@@ -496,6 +504,48 @@ void select_tile(qg_plan* p, int large) {
     a.st_maps = p->st_maps;
     a.st_large = large;
     if (p->opts.dst_precision != QG_DST_FP32) persistent_smem_bytes(p->opts.dst_precision, p->max_nl, large, &a);
+}
+
+// Make tensor-core tile width kGemmBN[v] the active one (tile lists, persistent arguments).
+void select_gemm(qg_plan* p, int v) {
+    p->bn_sel = v;
+    p->gx_tiles = p->gx_v[v];
+    p->gy_tiles = p->gy_v[v];
+    p->n_gx = p->n_gx_v[v];
+    p->n_gy = p->n_gy_v[v];
+    PersistArgs& a = p->pa;
+    a.gx = p->gx_tiles;
+    a.gy = p->gy_tiles;
+    a.n_gx = p->n_gx;
+    a.n_gy = p->n_gy;
+    a.tile_n = kGemmBN[v];
+}
+
+// Autotuner: time the four DST passes with each tensor-core tile width (zero planes) and keep
+// the fastest.
+cudaError_t autotune_gemm(qg_plan* p) {
+    cudaStream_t s = p->cap;
+    cudaEvent_t e0, e1;
+    cudaError_t e = cudaEventCreate(&e0);
+    if (!e) e = cudaEventCreate(&e1);
+    if (e) return e;
+    int best = 0;
+    for (int v = 0; v < p->n_bn && !e; ++v) {
+        select_gemm(p, v);
+        float ms = 0.f;
+        e = run_dst_solve(p, s);
+        if (!e) e = cudaEventRecord(e0, s);
+        for (int rep = 0; rep < 3 && !e; ++rep) e = run_dst_solve(p, s);
+        if (!e) e = cudaEventRecord(e1, s);
+        if (!e) e = cudaEventSynchronize(e1);
+        if (!e) e = cudaEventElapsedTime(&ms, e0, e1);
+        p->tune_gemm_ms[v] = ms / 3.f;
+        if (!e && p->tune_gemm_ms[v] < p->tune_gemm_ms[best]) best = v;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (!e) select_gemm(p, best);
+    return e;
 }
 
 // Autotuner: time every stencil variant (tile shapes, sweep strip heights) in its setting,
@@ -633,6 +683,8 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
     if (o.dst_precision < QG_DST_FP32 || o.dst_precision > QG_DST_BF16X3) return QG_ERR_ARG;
     if (o.refine_sweeps < 0 || o.refine_sweeps > 1) return QG_ERR_ARG;
     if (o.stencil < 0 || o.stencil > QG_STENCIL_VARIANTS) return QG_ERR_ARG;
+    if (o.gemm_tile != 0 && o.gemm_tile != kGemmBN[0] && o.gemm_tile != kGemmBN[1] && o.gemm_tile != kGemmBN[2])
+        return QG_ERR_ARG;
     for (int i = 0; i < n_members; ++i) {
         const int v = validate_member(members[i]);
         if (v != QG_OK) return v;
@@ -670,10 +722,10 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
     p->mh.resize(n_members);
     int64_t off_state = 0, off_x = 0, off_y = 0, off_layer = 0;
     std::vector<StencilTile> st;
-    std::vector<GemmTile> gx, gy;
     const bool tc = o.dst_precision != QG_DST_FP32;
     const int BMg = tc ? 128 : kSimtBM;
-    const int BNg = tc ? gemm_tc_tile_n(o.dst_precision) : kSimtBN;
+    const int n_bn = tc ? 3 : 1;
+    std::vector<GemmTile> gxv[3], gyv[3];
     for (int i = 0; i < n_members; ++i) {
         const qg_member_desc& d = members[i];
         MemberDev& M = p->mh[i];
@@ -756,10 +808,13 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
             for (int ty = 0; ty < (M.Ny + TY - 1) / TY; ++ty)
                 for (int tx = 0; tx < (M.Nx + TX - 1) / TX; ++tx) st_v[v].push_back({i, ty, tx});
         }
-        for (int mt = 0; mt < (n * M.Ny + BMg - 1) / BMg; ++mt)
-            for (int nt = 0; nt < (M.Nx + BNg - 1) / BNg; ++nt) gx.push_back({i, mt, nt});
-        for (int mt = 0; mt < (n * M.Nx + BMg - 1) / BMg; ++mt)
-            for (int nt = 0; nt < (M.Ny + BNg - 1) / BNg; ++nt) gy.push_back({i, mt, nt});
+        for (int v = 0; v < n_bn; ++v) {
+            const int BNg = tc ? kGemmBN[v] : kSimtBN;
+            for (int mt = 0; mt < (n * M.Ny + BMg - 1) / BMg; ++mt)
+                for (int nt = 0; nt < (M.Nx + BNg - 1) / BNg; ++nt) gxv[v].push_back({i, mt, nt});
+            for (int mt = 0; mt < (n * M.Nx + BMg - 1) / BMg; ++mt)
+                for (int nt = 0; nt < (M.Ny + BNg - 1) / BNg; ++nt) gyv[v].push_back({i, mt, nt});
+        }
     }
     if (e == cudaSuccess) {
         p->state_size = off_state;
@@ -770,8 +825,7 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
         e = upload(p, &p->md, mv);
     }
     if (e == cudaSuccess) {
-        p->n_gx = (int)gx.size();
-        p->n_gy = (int)gy.size();
+        p->n_bn = n_bn;
         for (int v = 0; v < 2 && !e; ++v) {
             p->n_st_v[v] = (int)st_v[v].size();
             e = upload(p, &p->st_tiles_v[v], st_v[v]);
@@ -788,7 +842,17 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
             p->n_sw_v[v] = (int)g.size();
             e = upload(p, &p->sw_items_v[v], g);
         }
-        if (!e && !(e = upload(p, &p->gx_tiles, gx))) e = upload(p, &p->gy_tiles, gy);
+        for (int v = 0; v < n_bn && !e; ++v) {
+            p->n_gx_v[v] = (int)gxv[v].size();
+            p->n_gy_v[v] = (int)gyv[v].size();
+            if (!(e = upload(p, &p->gx_v[v], gxv[v]))) e = upload(p, &p->gy_v[v], gyv[v]);
+        }
+        if (!e) {
+            p->gx_tiles = p->gx_v[0];
+            p->gy_tiles = p->gy_v[0];
+            p->n_gx = p->n_gx_v[0];
+            p->n_gy = p->n_gy_v[0];
+        }
     }
     if (e == cudaSuccess) {
         const size_t xb = (size_t)p->xplane * 4, yb = (size_t)p->yplane * 4;
@@ -829,6 +893,7 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
         a.gy = p->gy_tiles;
         a.n_gx = p->n_gx;
         a.n_gy = p->n_gy;
+        a.tile_n = tc ? kGemmBN[0] : kSimtBN;
         a.max_nl = p->max_nl;
         a.tc_maps = p->tc_maps;
         a.XA = p->XA;
@@ -847,7 +912,11 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
         a.bar_count = p->bar;
         a.bar_gen = p->bar + 1;
         select_tile(p, p->st_large);
-        if (o.autotune) e = autotune_stencil(p);
+        if (o.autotune && tc) e = autotune_gemm(p);
+        if (!e && tc && o.gemm_tile)
+            for (int v = 0; v < 3; ++v)
+                if (kGemmBN[v] == o.gemm_tile) select_gemm(p, v);
+        if (!e && o.autotune) e = autotune_stencil(p);
         if (!e && o.stencil > 0) {
             // a forced variant (tests, benchmarks of one variant)
             const int v = o.stencil - 1;
@@ -1065,6 +1134,13 @@ int qg_plan_tuning(const qg_plan* p, int* variant, float* ms, int n) {
     if (!p) return QG_ERR_NULL;
     if (variant) *variant = p->sw_sel >= 0 ? 2 + p->sw_sel : p->st_large;
     for (int k = 0; ms && k < n && k < QG_STENCIL_VARIANTS; ++k) ms[k] = p->tune_ms[k];
+    return QG_OK;
+}
+
+int qg_plan_gemm_tuning(const qg_plan* p, int* tile_n, float* ms, int n) {
+    if (!p) return QG_ERR_NULL;
+    if (tile_n) *tile_n = p->opts.dst_precision == QG_DST_FP32 ? kSimtBN : kGemmBN[p->bn_sel];
+    for (int k = 0; ms && k < n && k < 3; ++k) ms[k] = p->tune_gemm_ms[k];
     return QG_OK;
 }
 

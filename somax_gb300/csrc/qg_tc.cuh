@@ -15,7 +15,18 @@
 namespace qg {
 
 constexpr int TC_BM = 128;
-constexpr int TC_BN = 128;
+// Largest output tile width (N): 144 = 9 x 16 so that the N = n + 2 sizes of the DST (66,
+// 130, 258, 514) need one, one, two and four tiles; a plan may cut narrower tiles (more
+// CTAs for small members), and the last tile of a member runs its MMAs at the width it needs
+// (a multiple of 16), so little of the tensor work is padding.  The S operand's TMA box is
+// always TC_BN rows.
+constexpr int TC_BN = 144;
+constexpr int TC_TMEM_BUF = 256;   // TMEM column stride of the two accumulators
+constexpr int TC_TMEM_COLS = 512;  // allocation (power of two >= 2 buffers)
+// Width of output tile nt of a pass with Nn columns cut into tiles of bn (<= TC_BN) columns.
+__host__ __device__ constexpr int tc_tile_width(int Nn, int nt, int bn) {
+    return (Nn - nt * bn >= bn) ? bn : ((Nn - nt * bn + 15) / 16) * 16;
+}
 
 struct TcMaps {
     CUtensorMap a[2];  // A hi (or f32), A lo
@@ -53,10 +64,11 @@ __host__ __device__ constexpr int tc_stage_bytes() {
     return TcCfg<PREC>::NA * tc_tile_a_bytes<PREC>() + TcCfg<PREC>::NB * tc_tile_b_bytes<PREC>();
 }
 
-// Instruction descriptor: D f32, A/B format FMT, both K-major, N = TC_BN, M = TC_BM.
+// Instruction descriptor: D f32, A/B format FMT, both K-major, N = n (a multiple of 16 up to
+// TC_BN), M = TC_BM.
 template <int PREC>
-__device__ __forceinline__ uint32_t tc_idesc() {
-    return (1u << 4) | (TcCfg<PREC>::FMT << 7) | (TcCfg<PREC>::FMT << 10) | ((uint32_t)(TC_BN >> 3) << 17) |
+__device__ __forceinline__ uint32_t tc_idesc(int n) {
+    return (1u << 4) | (TcCfg<PREC>::FMT << 7) | (TcCfg<PREC>::FMT << 10) | ((uint32_t)(n >> 3) << 17) |
            ((uint32_t)(TC_BM >> 4) << 24);
 }
 
@@ -135,13 +147,17 @@ __device__ __forceinline__ TcGeom tc_geom(const MemberDev& M, int64_t xplane, in
     return g;
 }
 
-// Issue the MMAs of one k-block (operands at shared addresses sa / sb) into tmem_d.
+// Issue the MMAs of one k-block (operands at shared addresses sa / sb) into tmem_d: `ksteps`
+// UMMA_K-wide steps (the last k-block of a member stops at its K; the zero fill beyond it
+// contributes nothing) at output width n.
 template <int PREC>
-__device__ __forceinline__ void tc_mma_kblock(uint32_t tmem_d, uint32_t sa, uint32_t sb, bool first) {
+__device__ __forceinline__ void tc_mma_kblock(uint32_t tmem_d, uint32_t sa, uint32_t sb, bool first, int ksteps,
+                                              int n) {
     using C = TcCfg<PREC>;
-    const uint32_t idesc = tc_idesc<PREC>();
+    const uint32_t idesc = tc_idesc<PREC>(n);
 #pragma unroll
     for (int k = 0; k < C::BK / C::UMMA_K; ++k) {
+        if (k >= ksteps) break;
         const uint32_t koff = k * C::UMMA_K * C::ESIZE;  // 32 bytes per step
         const uint64_t a0 = tc_sdesc(sa + koff), b0 = tc_sdesc(sb + koff);
         tc_mma<C::FMT>(tmem_d, a0, b0, idesc, (!first || k > 0) ? 1u : 0u);
@@ -164,7 +180,7 @@ __device__ __forceinline__ void tc_store_bf16x2(__nv_bfloat16* p, int64_t plane,
 constexpr int TC_STAGE_FLOATS = 32 * 33;
 constexpr int TC_EPI_SMEM = 4 * TC_STAGE_FLOATS * 4;  // bytes, four epilogue warps
 
-// Epilogue of one 128 x TC_BN tile by one of four epilogue warps (TMEM lane quarter
+// Epilogue of one 128 x width tile by one of four epilogue warps (TMEM lane quarter
 // `quarter`): read the accumulator and apply the pass's store.  All four warps must call it
 // (tcgen05.ld is warp-collective); `valid` false skips the stores.  Transposed passes store
 // straight from registers (lanes hold consecutive output rows); the row-major passes go
@@ -172,9 +188,11 @@ constexpr int TC_EPI_SMEM = 4 * TC_STAGE_FLOATS * 4;  // bytes, four epilogue wa
 // elements of one row.
 template <int PASS>
 __device__ __forceinline__ void tc_epilogue(const MemberDev& M, const TcGeom& g, void* Cv, int c_fmt, int accumulate,
-                                            int m0, int n0, uint32_t tmem_acc, int quarter, int lane, bool valid,
-                                            float* stage) {
-    const int Mtot = g.Mtot, Mb = g.Mb, Nn = g.Nn, ldo = g.ldo;
+                                            int m0, int n0, int width, uint32_t tmem_acc, int quarter, int lane,
+                                            bool valid, float* stage) {
+    const int Mtot = g.Mtot, Mb = g.Mb, ldo = g.ldo;
+    const int Nn = g.Nn;                    // columns of the pass (layer stride of transposed stores)
+    const int nend = min(Nn, n0 + width);   // this tile's columns end here
     const int64_t cplane = g.cplane;
     const int m = m0 + quarter * 32 + lane;
     const int l = m < Mtot ? m / Mb : 0;
@@ -184,19 +202,19 @@ __device__ __forceinline__ void tc_epilogue(const MemberDev& M, const TcGeom& g,
     const float laml = M.lam[l];
     float* Cf = static_cast<float*>(Cv) + g.cbase;
     __nv_bfloat16* Cb = static_cast<__nv_bfloat16*>(Cv) + g.cbase;
-    for (int c = 0; c < TC_BN / 32; ++c) {
+    for (int c = 0; c < (TC_BN + 31) / 32; ++c) {
         uint32_t v[32];
         const uint32_t taddr = tmem_acc + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(c * 32);
         QG_LD32(v, taddr);
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
         const int nb = n0 + c * 32;
-        if (!valid || nb >= Nn) continue;  // warp-uniform
+        if (!valid || nb >= nend) continue;  // warp-uniform
         if constexpr (PASS == G1_FWD_X || PASS == G3_INV_Y) {
             // transposed store out[(l, n)][r]: lanes hold consecutive r -> coalesced
             if (m >= Mtot) continue;
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
-                if (nb + j >= Nn) break;
+                if (nb + j >= nend) break;
                 const float x = __uint_as_float(v[j]);
                 const int64_t o = ((int64_t)l * Nn + nb + j) * ldo + r;
                 if (c_fmt == FMT_F32)
@@ -206,7 +224,7 @@ __device__ __forceinline__ void tc_epilogue(const MemberDev& M, const TcGeom& g,
             }
         } else {
             float eyv = 0.f;
-            if (PASS == G2_FWD_Y) eyv = (nb + lane < Nn) ? ey[nb + lane] : 1.f;
+            if (PASS == G2_FWD_Y) eyv = (nb + lane < nend) ? ey[nb + lane] : 1.f;
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
                 float x = __uint_as_float(v[j]);
@@ -220,7 +238,7 @@ __device__ __forceinline__ void tc_epilogue(const MemberDev& M, const TcGeom& g,
             for (int rr = 0; rr < 32; ++rr) {
                 const int mm = m0 + quarter * 32 + rr;
                 if (mm >= Mtot) break;
-                if (n < Nn) {
+                if (n < nend) {
                     const int64_t o = (int64_t)mm * ldo + n;
                     const float x = stage[rr * 33 + lane];
                     if (c_fmt == FMT_F32)

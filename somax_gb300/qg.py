@@ -166,7 +166,7 @@ class Plan:
     """Owns a ``qg_plan`` (device constants + workspace) on one CUDA device."""
 
     def __init__(self, members: Sequence["MemberSpec"], precision="fp32", refine=0, use_graphs=True,
-                 device=None, persistent=True, autotune=True, stencil=None):
+                 device=None, persistent=True, autotune=True, stencil=None, gemm_tile=None):
         if not torch.cuda.is_available():
             raise RuntimeError("somax_gb300 needs a CUDA device (no CPU fallback)")
         self.device = torch.device(device or "cuda", torch.cuda.current_device()) if device is None \
@@ -177,7 +177,7 @@ class Plan:
             m.fill(arr[i])
         forced = 0 if stencil is None else 1 + self.STENCIL_VARIANTS.index(stencil)
         opts = Options(PRECISIONS[precision], int(refine), int(bool(use_graphs)), int(bool(persistent)),
-                       int(bool(autotune)), forced)
+                       int(bool(autotune)), forced, int(gemm_tile or 0))
         handle = C.c_void_p()
         with torch.cuda.device(self.device):
             check(L.qg_plan_create(arr, len(members), C.byref(opts), C.byref(handle)), "qg_plan_create")
@@ -315,8 +315,13 @@ class Plan:
         n = len(self.STENCIL_VARIANTS)
         ms = (C.c_float * n)()
         check(self._L.qg_plan_tuning(self._h, C.byref(v), ms, n), "qg_plan_tuning")
+        bn = C.c_int()
+        gms = (C.c_float * 3)()
+        check(self._L.qg_plan_gemm_tuning(self._h, C.byref(bn), gms, 3), "qg_plan_gemm_tuning")
         return {"stencil": self.STENCIL_VARIANTS[v.value],
-                "ms": {name: round(float(t), 5) for name, t in zip(self.STENCIL_VARIANTS, ms)}}
+                "ms": {name: round(float(t), 5) for name, t in zip(self.STENCIL_VARIANTS, ms)},
+                "gemm_tile_n": bn.value,
+                "gemm_ms": {w: round(float(t), 5) for w, t in zip((144, 80, 48), gms)}}
 
     def set_profiling(self, on: bool):
         check(self._L.qg_set_profiling(self._h, int(on)), "qg_set_profiling")

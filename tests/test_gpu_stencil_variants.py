@@ -82,3 +82,16 @@ def test_sweep_equals_tile_stencil():
     a = sg.Plan([m.spec], "fp32", stencil="tile32x8").step(qd.clone(), pv, 1200.0, 5, "ssprk3")
     b = sg.Plan([m.spec], "fp32", stencil="sweep32").step(qd.clone(), pv, 1200.0, 5, "ssprk3")
     assert rel(b, a) < 1e-6
+
+
+@pytest.mark.parametrize("precision", ["bf16x3", "tf32"])
+@pytest.mark.parametrize("tile", [144, 80, 48])
+@pytest.mark.parametrize("nx,ny,nl", [(3, 5, 2), (64, 64, 1), (128, 128, 3), (200, 130, 2), (256, 256, 3), (300, 17, 4)])
+def test_gemm_tile_widths(precision, tile, nx, ny, nl):
+    """Every tensor-core output tile width (144, 80, 48 columns, last tile of a member cut to
+    a multiple of 16) against the float64 inversion."""
+    m, o, q = pair(nx, ny, nl, 50 + nl)
+    plan = sg.Plan([m.spec], precision, gemm_tile=tile)
+    assert plan.tuning()["gemm_tile_n"] == tile
+    psi = plan.invert(torch.tensor(q, dtype=torch.float32, device="cuda"))
+    assert rel(psi, O.invert_pv(o, q)) < (3e-5 if precision == "bf16x3" else 6e-3)
