@@ -110,7 +110,7 @@ typedef struct qg_options {
                            (tensor-core precisions without refinement) */
     int autotune;       /* 1: qg_plan_create times the stencil variants and keeps the fastest */
     int stencil;        /* 0: autotuner's choice; QG_STENCIL_* + 1: run that variant */
-    int gemm_tile;      /* 0: autotuner's choice; 144, 80 or 48: that tensor-core tile width */
+    int gemm_tile;      /* 0: autotuner's choice; 144, 80, 48, 32 or 16: that tensor-core tile width */
     int reserved[1];
 } qg_options;
 
@@ -201,9 +201,9 @@ int qg_kernel_stats(qg_plan* plan, int kclass, double* total_ms, int64_t* launch
 /* The plan's tuned choice: *variant = the stencil the multi-launch path runs; ms[k] (k < n)
    the autotuner's time of one stage with variant k in ms (-1 when not measured). */
 int qg_plan_tuning(const qg_plan* plan, int* variant, float* ms, int n);
-/* The tensor-core DST passes' output tile width the autotuner kept (144, 80 or 48 columns;
-   64 for the FP32 CUDA-core passes) and the time of the four passes it measured with each
-   width in ms (ms[0..2] for 144, 80, 48; -1 when not measured). */
+/* The tensor-core DST passes' output tile width the autotuner kept (144, 80, 48, 32 or 16
+   columns; 64 for the FP32 CUDA-core passes) and the time of the four passes it measured
+   with each width in ms (ms[0..4] in that order; -1 when not measured). */
 int qg_plan_gemm_tuning(const qg_plan* plan, int* tile_n, float* ms, int n);
 
 #ifdef __cplusplus

@@ -231,11 +231,11 @@ struct qg_plan {
     int n_gx = 0, n_gy = 0;
     // tensor-core tile lists for each candidate output tile width (kGemmBN); the autotuner
     // keeps the fastest (wide tiles for large members, narrow ones spread small members)
-    GemmTile* gx_v[3] = {nullptr, nullptr, nullptr};
-    GemmTile* gy_v[3] = {nullptr, nullptr, nullptr};
-    int n_gx_v[3] = {0, 0, 0}, n_gy_v[3] = {0, 0, 0};
+    GemmTile* gx_v[5] = {};
+    GemmTile* gy_v[5] = {};
+    int n_gx_v[5] = {}, n_gy_v[5] = {};
     int n_bn = 1, bn_sel = 0;
-    float tune_gemm_ms[3] = {-1.f, -1.f, -1.f};
+    float tune_gemm_ms[5] = {-1.f, -1.f, -1.f, -1.f, -1.f};
     // device memory: x-row planes XA (modal operand), XB (V^T), XC (psi_hat), XQ (FP32 modal
     // rhs for refinement), S0 (state), S1/S2 (stage inputs); y-row planes YA (T1^T), YB (U)
     std::vector<void*> allocs;
@@ -414,7 +414,8 @@ StencilArgs stencil_args(qg_plan* p, const float* params) {
 }
 
 constexpr int kSweepRows[3] = {16, 32, 64};
-constexpr int kGemmBN[3] = {144, 80, 48};  // tensor-core output tile widths the autotuner tries
+constexpr int kNumBN = 5;
+constexpr int kGemmBN[kNumBN] = {144, 80, 48, 32, 16};  // tensor-core output tile widths the autotuner tries
 
 // The multi-launch path's stencil launch: the column sweep if selected, else the tiles.
 cudaError_t launch_stencil(qg_plan* p, StencilArgs a, cudaStream_t s, bool pdl) {
@@ -683,7 +684,7 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
     if (o.dst_precision < QG_DST_FP32 || o.dst_precision > QG_DST_BF16X3) return QG_ERR_ARG;
     if (o.refine_sweeps < 0 || o.refine_sweeps > 1) return QG_ERR_ARG;
     if (o.stencil < 0 || o.stencil > QG_STENCIL_VARIANTS) return QG_ERR_ARG;
-    if (o.gemm_tile != 0 && o.gemm_tile != kGemmBN[0] && o.gemm_tile != kGemmBN[1] && o.gemm_tile != kGemmBN[2])
+    if (o.gemm_tile != 0 && std::find(kGemmBN, kGemmBN + kNumBN, o.gemm_tile) == kGemmBN + kNumBN)
         return QG_ERR_ARG;
     for (int i = 0; i < n_members; ++i) {
         const int v = validate_member(members[i]);
@@ -724,8 +725,8 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
     std::vector<StencilTile> st;
     const bool tc = o.dst_precision != QG_DST_FP32;
     const int BMg = tc ? 128 : kSimtBM;
-    const int n_bn = tc ? 3 : 1;
-    std::vector<GemmTile> gxv[3], gyv[3];
+    const int n_bn = tc ? kNumBN : 1;
+    std::vector<GemmTile> gxv[kNumBN], gyv[kNumBN];
     for (int i = 0; i < n_members; ++i) {
         const qg_member_desc& d = members[i];
         MemberDev& M = p->mh[i];
@@ -914,7 +915,7 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
         select_tile(p, p->st_large);
         if (o.autotune && tc) e = autotune_gemm(p);
         if (!e && tc && o.gemm_tile)
-            for (int v = 0; v < 3; ++v)
+            for (int v = 0; v < kNumBN; ++v)
                 if (kGemmBN[v] == o.gemm_tile) select_gemm(p, v);
         if (!e && o.autotune) e = autotune_stencil(p);
         if (!e && o.stencil > 0) {
@@ -1140,7 +1141,7 @@ int qg_plan_tuning(const qg_plan* p, int* variant, float* ms, int n) {
 int qg_plan_gemm_tuning(const qg_plan* p, int* tile_n, float* ms, int n) {
     if (!p) return QG_ERR_NULL;
     if (tile_n) *tile_n = p->opts.dst_precision == QG_DST_FP32 ? kSimtBN : kGemmBN[p->bn_sel];
-    for (int k = 0; ms && k < n && k < 3; ++k) ms[k] = p->tune_gemm_ms[k];
+    for (int k = 0; ms && k < n && k < kNumBN; ++k) ms[k] = p->tune_gemm_ms[k];
     return QG_OK;
 }
 

@@ -316,12 +316,12 @@ class Plan:
         ms = (C.c_float * n)()
         check(self._L.qg_plan_tuning(self._h, C.byref(v), ms, n), "qg_plan_tuning")
         bn = C.c_int()
-        gms = (C.c_float * 3)()
-        check(self._L.qg_plan_gemm_tuning(self._h, C.byref(bn), gms, 3), "qg_plan_gemm_tuning")
+        gms = (C.c_float * 5)()
+        check(self._L.qg_plan_gemm_tuning(self._h, C.byref(bn), gms, 5), "qg_plan_gemm_tuning")
         return {"stencil": self.STENCIL_VARIANTS[v.value],
                 "ms": {name: round(float(t), 5) for name, t in zip(self.STENCIL_VARIANTS, ms)},
                 "gemm_tile_n": bn.value,
-                "gemm_ms": {w: round(float(t), 5) for w, t in zip((144, 80, 48), gms)}}
+                "gemm_ms": {w: round(float(t), 5) for w, t in zip((144, 80, 48, 32, 16), gms)}}
 
     def set_profiling(self, on: bool):
         check(self._L.qg_set_profiling(self._h, int(on)), "qg_set_profiling")

@@ -85,11 +85,11 @@ def test_sweep_equals_tile_stencil():
 
 
 @pytest.mark.parametrize("precision", ["bf16x3", "tf32"])
-@pytest.mark.parametrize("tile", [144, 80, 48])
+@pytest.mark.parametrize("tile", [144, 80, 48, 32, 16])
 @pytest.mark.parametrize("nx,ny,nl", [(3, 5, 2), (64, 64, 1), (128, 128, 3), (200, 130, 2), (256, 256, 3), (300, 17, 4)])
 def test_gemm_tile_widths(precision, tile, nx, ny, nl):
-    """Every tensor-core output tile width (144, 80, 48 columns, last tile of a member cut to
-    a multiple of 16) against the float64 inversion."""
+    """Every tensor-core output tile width (144, 80, 48, 32, 16 columns, last tile of a member
+    cut to a multiple of 16) against the float64 inversion."""
     m, o, q = pair(nx, ny, nl, 50 + nl)
     plan = sg.Plan([m.spec], precision, gemm_tile=tile)
     assert plan.tuning()["gemm_tile_n"] == tile
