@@ -201,7 +201,7 @@ def run_reference(args):
 class Workload:
     """One bench step = one model day of every member, on one device."""
 
-    def __init__(self, name, precision, persistent, dev, seed, stencil=None):
+    def __init__(self, name, precision, persistent, dev, seed, stencil=None, gemm_tile=None):
         import torch
 
         import somax_gb300 as sg
@@ -220,7 +220,8 @@ class Workload:
                     q0s.append(tc.initial_pv(cfg, seed=10000 * seed + k).astype(np.float32))
                     cfgs.append(cfg)
                     k += 1
-            self.ens = sg.QGEnsemble(models, precision=precision, persistent=persistent, device=dev, stencil=stencil)
+            self.ens = sg.QGEnsemble(models, precision=precision, persistent=persistent, device=dev, stencil=stencil,
+                                     gemm_tile=gemm_tile)
             self.plan = self.ens.plan
             self.params = self.ens.params(dev)
             self.q0 = np.concatenate([q.reshape(-1) for q in q0s])
@@ -230,7 +231,7 @@ class Workload:
         else:
             cfg = tc.CONFIGS[name]
             self.model = sg.BaroclinicQG.create(**cfg.model_kwargs(), precision=precision, persistent=persistent,
-                                                stencil=stencil)
+                                                stencil=stencil, gemm_tile=gemm_tile)
             self.plan = self.model.plan(dev)
             self.params = self.model._param_vector(dev)
             self.q0 = tc.initial_pv(cfg, seed=seed).astype(np.float32)
@@ -333,6 +334,8 @@ def main():
     ap.add_argument("--precision", default="bf16x3", help="DST-I GEMM arithmetic: fp32 | tf32 | bf16x3")
     ap.add_argument("--persistent", type=int, default=0,
                     help="1: all steps of a call in one persistent cooperative launch (tensor-core precisions)")
+    ap.add_argument("--gemm-tile", type=int, default=None,
+                    help="force the tensor-core DST tile width (144 | 80 | 48 | 32 | 16); default: autotuned")
     ap.add_argument("--stencil", default=None,
                     help="force a stencil variant (tile32x8 | tile64x16 | sweep16 | sweep32 | sweep64); "
                          "default: the autotuner's pick")
@@ -356,7 +359,7 @@ def main():
     if world > 1:
         dist.init_process_group("nccl", device_id=dev)
 
-    W = Workload(args.config, args.precision, bool(args.persistent), dev, rank, args.stencil)
+    W = Workload(args.config, args.precision, bool(args.persistent), dev, rank, args.stencil, args.gemm_tile)
     plan = W.plan
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
 

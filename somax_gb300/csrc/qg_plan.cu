@@ -913,11 +913,12 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
         a.bar_count = p->bar;
         a.bar_gen = p->bar + 1;
         select_tile(p, p->st_large);
-        if (o.autotune && tc) e = autotune_gemm(p);
+        // a forced choice (qg_options.gemm_tile / .stencil) skips that half of the autotuner
+        if (o.autotune && tc && !o.gemm_tile) e = autotune_gemm(p);
         if (!e && tc && o.gemm_tile)
             for (int v = 0; v < kNumBN; ++v)
                 if (kGemmBN[v] == o.gemm_tile) select_gemm(p, v);
-        if (!e && o.autotune) e = autotune_stencil(p);
+        if (!e && o.autotune && !o.stencil) e = autotune_stencil(p);
         if (!e && o.stencil > 0) {
             // a forced variant (tests, benchmarks of one variant)
             const int v = o.stencil - 1;

@@ -404,7 +404,7 @@ class _QGBase(SomaxModel):
     barotropic = False
 
     def __init__(self, spec: MemberSpec, params: QGParams, precision="fp32", refine=0, use_graphs=True,
-                 strat=None, modal=None, persistent=True, stencil=None):
+                 strat=None, modal=None, persistent=True, stencil=None, gemm_tile=None):
         self.spec = spec
         self.params = params
         self.precision = precision
@@ -412,6 +412,7 @@ class _QGBase(SomaxModel):
         self.use_graphs = use_graphs
         self.persistent = persistent
         self.stencil = stencil
+        self.gemm_tile = gemm_tile
         self.strat = strat
         self.modal = modal
         self.grid = Grid(spec.nx, spec.ny, spec.Lx, spec.Ly)
@@ -425,7 +426,7 @@ class _QGBase(SomaxModel):
         key = device.index
         if key not in self._plans:
             self._plans[key] = Plan([self.spec], self.precision, self.refine, self.use_graphs, device, self.persistent,
-                                    stencil=self.stencil)
+                                    stencil=self.stencil, gemm_tile=self.gemm_tile)
         return self._plans[key]
 
     @property
@@ -614,7 +615,7 @@ class BaroclinicQG(_QGBase):
                H=(400.0, 1100.0, 2600.0), g_prime=(9.81, 0.025, 0.0125), stratification=None,
                lateral_viscosity=0.0, bottom_drag=0.0, wind_amplitude=0.0, wind_profile="doublegyre",
                poisson_bc="dst", biharmonic_viscosity=0.0, precision="fp32", refine=0, eigs="consistent",
-               use_graphs=True, persistent=True, stencil=None) -> "BaroclinicQG":
+               use_graphs=True, persistent=True, stencil=None, gemm_tile=None) -> "BaroclinicQG":
         """``BaroclinicQG.create`` (``baroclinic.py:230-332``) with the same keyword arguments,
         plus ``biharmonic_viscosity`` (extension), ``precision`` of the DST-I GEMMs
         ("fp32", "tf32", "bf16x3"), ``refine`` sweeps, the ``eigs`` mode and whether ``step`` runs
@@ -633,7 +634,7 @@ class BaroclinicQG(_QGBase):
                           eigs, modal)
         params = QGParams(*(torch.tensor(float(v)) for v in (lateral_viscosity, bottom_drag, wind_amplitude,
                                                              biharmonic_viscosity)))
-        return BaroclinicQG(spec, params, precision, refine, use_graphs, strat, modal, persistent, stencil)
+        return BaroclinicQG(spec, params, precision, refine, use_graphs, strat, modal, persistent, stencil, gemm_tile)
 
     @property
     def n_layers(self):
@@ -649,12 +650,14 @@ class BarotropicQG(_QGBase):
     @staticmethod
     def create(nx=64, ny=64, Lx=1e6, Ly=1e6, f0=1e-4, beta=1.6e-11, lateral_viscosity=0.0,
                bottom_drag=0.0, wind_amplitude=0.0, wind_profile="doublegyre", biharmonic_viscosity=0.0,
-               precision="fp32", refine=0, use_graphs=True, persistent=True, stencil=None) -> "BarotropicQG":
+               precision="fp32", refine=0, use_graphs=True, persistent=True, stencil=None,
+               gemm_tile=None) -> "BarotropicQG":
         """``BarotropicQG.create`` (``barotropic.py:186-248``)."""
         spec = MemberSpec(nx, ny, Lx, Ly, f0, beta, [1.0], [1.0], True, wind_profile)
         params = QGParams(*(torch.tensor(float(v)) for v in (lateral_viscosity, bottom_drag, wind_amplitude,
                                                              biharmonic_viscosity)))
-        return BarotropicQG(spec, params, precision, refine, use_graphs, persistent=persistent, stencil=stencil)
+        return BarotropicQG(spec, params, precision, refine, use_graphs, persistent=persistent, stencil=stencil,
+                            gemm_tile=gemm_tile)
 
 
 class QGEnsemble:
@@ -663,12 +666,12 @@ class QGEnsemble:
     tensor-core precisions).  States are packed member after member in the reference layout."""
 
     def __init__(self, models: Sequence[_QGBase], precision="bf16x3", refine=0, use_graphs=True, persistent=True,
-                 device=None, stencil=None):
+                 device=None, stencil=None, gemm_tile=None):
         if not models:
             raise ValueError("an ensemble needs at least one member")
         self.models = list(models)
         self.plan = Plan([m.spec for m in self.models], precision, refine, use_graphs, device, persistent,
-                         stencil=stencil)
+                         stencil=stencil, gemm_tile=gemm_tile)
         self.offsets = self.plan.offsets
         self.sizes = [int(np.prod(m.shape)) for m in self.models]
 
