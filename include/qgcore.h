@@ -50,7 +50,8 @@ extern "C" {
 #define QG_ERR_TIMEOUT 5      /* a bounded device-side wait gave up */
 #define QG_ERR_ARG 6          /* bad enum / option value */
 #define QG_ERR_UNSUPPORTED 7  /* option not available on this device */
-#define QG_ERR_TOO_LARGE 8    /* member exceeds the fixed scratch of qg_invert_static */
+#define QG_ERR_TOO_LARGE 8    /* member exceeds the fixed scratch of qg_invert_static, or has
+                                  more than 28000 land boundary points */
 
 /* dst_precision: arithmetic of the DST-I GEMMs of the PV inversion */
 #define QG_DST_FP32 0    /* plain FP32 on the CUDA cores (the baseline path) */
@@ -100,6 +101,12 @@ typedef struct qg_member_desc {
     double Cl2m[QG_MAX_LAYERS * QG_MAX_LAYERS];
     double Cm2l[QG_MAX_LAYERS * QG_MAX_LAYERS];
     double lambdas[QG_MAX_LAYERS];
+    /* optional land mask (extension; host memory, (ny + 2) x (nx + 2) row-major, 1 = ocean,
+       0 = land, read during qg_plan_create only; NULL = no land).  Interior land cells read
+       q as 0, have psi = 0 and dq = 0; the inversion keeps psi = 0 on the land cells next to
+       the ocean with an FP64 capacitance-matrix correction (a second DST solve).  The ring
+       keeps the unmasked rules. */
+    const unsigned char* mask;
 } qg_member_desc;
 
 typedef struct qg_options {

@@ -46,6 +46,7 @@ class MemberDesc(C.Structure):
         ("Cl2m", C.c_double * (MAX_LAYERS * MAX_LAYERS)),
         ("Cm2l", C.c_double * (MAX_LAYERS * MAX_LAYERS)),
         ("lambdas", C.c_double * MAX_LAYERS),
+        ("mask", C.POINTER(C.c_ubyte)),
     ]
 
 

@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <utility>
+#include <vector>
 
 #include "../../include/qgcore.h"
 
@@ -38,7 +39,17 @@ struct MemberDev {
     const float* Sy;        // Ny x Ny, pitch Py
     const uint16_t* Sx_bf;  // bf16 hi/lo planes of Sx (pitch Px, hi then lo), or null
     const uint16_t* Sy_bf;
+    // masked basin (null / 0 without land)
+    const uint8_t* mask;    // (Ny, Nx), 1 = ocean; interior cells with 0 are land
+    int nb;                 // land boundary points B (capacitance correction)
+    const int* bidx;        // their linear indices j * Nx + i
+    const double* cinv;     // nl x nb x nb inverse capacitance matrices (row-major)
 };
+
+// Interior land cell of a member (false without a mask).
+__host__ __device__ __forceinline__ bool is_land(const MemberDev& M, int j, int i) {
+    return M.mask && j > 0 && i > 0 && j < M.Ny - 1 && i < M.Nx - 1 && M.mask[(int64_t)j * M.Nx + i] == 0;
+}
 
 // Stencil work item: one 2-D tile of one member (all layers).
 struct StencilTile {
@@ -230,6 +241,21 @@ int stencil_mt_blocks_per_sm(int max_nl, int large);  // 4 CUtensorMap per (memb
 cudaError_t gemm_tc_encode(const MemberDev& M, int pass, const void* a_plane, int64_t a_plane_elems, int prec,
                            void* out);
 cudaError_t launch_gemm_simt(const GemmArgs& g, int ntiles, cudaStream_t s, bool pdl);
+
+// masked basins: host construction (qg_capacitance.cu) and the device correction (qg_mask.cu)
+struct CapItem {
+    int member, mode, r0;  // rows r0 .. r0 + kCapRows - 1 of C^-1 of one mode
+};
+constexpr int kCapRows = 32;
+std::vector<int> land_boundary(const qg_member_desc& d);
+bool capacitance_inverse(const qg_member_desc& d, const double* lam, int nl, const std::vector<int>& B,
+                         std::vector<double>& cinv);
+// sigma = -C^-1 psi_hat[B] per (member, mode), written at B into the operand (and its FP32
+// copy) for the second solve
+cudaError_t launch_capacitance(const MemberDev* members, const CapItem* items, int n_items, const float* psi_hat,
+                               void* xa, int xa_fmt, float* xq, int64_t xplane, size_t smem, cudaStream_t s);
+cudaError_t capacitance_init(size_t max_smem);
+constexpr int kMaxBoundary = 28000;  // boundary points per member (FP64 gather in shared memory)
 
 // host helpers shared by the plan and the plan-free entry points
 int validate_member(const qg_member_desc& d);

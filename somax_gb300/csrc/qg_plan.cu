@@ -204,7 +204,7 @@ void dst_eigs(int n, double d, std::vector<float>& out) {
 
 const char* kErrStr[] = {"ok", "null pointer", "bad shape", "CUDA error", "non-finite value",
                          "device wait timed out", "bad argument", "unsupported",
-                         "member exceeds the static scratch limit"};
+                         "member exceeds a size limit (static scratch, or land boundary points)"};
 
 }  // namespace
 
@@ -242,6 +242,10 @@ struct qg_plan {
     float *XA = nullptr, *XB = nullptr, *XC = nullptr, *XQ = nullptr, *YA = nullptr, *YB = nullptr;
     float *S0 = nullptr, *S1 = nullptr, *S2 = nullptr;
     float* params = nullptr;  // plan-owned copy of the params (graph-stable)
+    // masked members: capacitance work items (one per mode and block of rows of C^-1)
+    CapItem* cap_items = nullptr;
+    int n_cap = 0;
+    size_t cap_smem = 0;
     int* flags = nullptr;
     double* diag_acc = nullptr;
     double* vjp_acc = nullptr;  // parameter cotangents of qg_rhs_vjp (QG_NPARAMS per member)
@@ -382,6 +386,19 @@ cudaError_t run_dst_solve(qg_plan* p, cudaStream_t s) {
     return cudaSuccess;
 }
 
+// psi_hat (XC) with the masked members' capacitance correction: solve, sigma at B into the
+// operand, solve again (the operand is otherwise unchanged: it is zero on land).
+cudaError_t run_inversion(qg_plan* p, cudaStream_t s) {
+    cudaError_t e = run_dst_solve(p, s);
+    if (e || p->n_cap == 0) return e;
+    e = timed(p, QG_K_OTHER, s, [&] {
+        return launch_capacitance(p->md, p->cap_items, p->n_cap, p->XC, p->XA, p->op_fmt, p->XQ, p->xplane,
+                                  p->cap_smem, s);
+    });
+    if (!e) e = run_dst_solve(p, s);
+    return e;
+}
+
 // q (caller packing) -> optional internal copy + the modal GEMM operand.
 cudaError_t run_prep(qg_plan* p, const float* q, float* copy, int zero_ring_copy, int bc_operand,
                      cudaStream_t s) {
@@ -460,7 +477,7 @@ cudaError_t run_one_step(qg_plan* p, const float* params, float dt, int scheme, 
     float* stage_buf[3] = {p->S0, p->S1, p->S2};
     cudaError_t e;
     for (int k = 0; k < ns; ++k) {
-        if ((e = run_dst_solve(p, s))) return e;
+        if ((e = run_inversion(p, s))) return e;
         StencilArgs a = stencil_args(p, params);
         a.q_sel = k;
         a.apply_bc = 1;
@@ -719,6 +736,8 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
     }
     std::vector<StencilTile> st_v[2];
     std::vector<SweepItem> sw_v[3];
+    std::vector<CapItem> cap;
+    bool too_large = false;
     // geometry and offsets
     p->mh.resize(n_members);
     int64_t off_state = 0, off_x = 0, off_y = 0, off_layer = 0;
@@ -797,6 +816,35 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
             M.Sx_bf = bx;
             M.Sy_bf = byy;
         }
+        // masked basin: land mask, boundary points and inverse capacitance matrices
+        if (d.mask) {
+            std::vector<uint8_t> mk(d.mask, d.mask + (size_t)M.Ny * M.Nx);
+            uint8_t* dm;
+            if ((e = upload(p, &dm, mk))) break;
+            M.mask = dm;
+            const std::vector<int> B = land_boundary(d);
+            if ((int)B.size() > kMaxBoundary) {
+                e = cudaErrorInvalidValue;
+                too_large = true;
+                break;
+            }
+            if (!B.empty()) {
+                std::vector<double> cinv;
+                if (!capacitance_inverse(d, lam, n, B, cinv)) {
+                    e = cudaErrorInvalidValue;
+                    break;
+                }
+                int* db;
+                double* dc;
+                if ((e = upload(p, &db, B)) || (e = upload(p, &dc, cinv))) break;
+                M.nb = (int)B.size();
+                M.bidx = db;
+                M.cinv = dc;
+                for (int m = 0; m < n; ++m)
+                    for (int r0 = 0; r0 < M.nb; r0 += kCapRows) cap.push_back({i, m, r0});
+                p->cap_smem = std::max(p->cap_smem, (size_t)M.nb * sizeof(double));
+            }
+        }
         // column-sweep strips
         for (int v = 0; v < 3; ++v) {
             const int R = kSweepRows[v], W = sweep_columns();
@@ -830,6 +878,11 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
         for (int v = 0; v < 2 && !e; ++v) {
             p->n_st_v[v] = (int)st_v[v].size();
             e = upload(p, &p->st_tiles_v[v], st_v[v]);
+        }
+        if (!e && !cap.empty()) {
+            p->n_cap = (int)cap.size();
+            e = upload(p, &p->cap_items, cap);
+            if (!e) e = capacitance_init(p->cap_smem);
         }
         for (int v = 0; v < 3 && !e; ++v) {
             // group by layer count: one sweep launch per group
@@ -930,7 +983,7 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
         qg_plan_destroy(p);
-        return QG_ERR_CUDA;
+        return too_large ? QG_ERR_TOO_LARGE : QG_ERR_CUDA;
     }
     *out = p;
     return QG_OK;
@@ -972,7 +1025,7 @@ int qg_invert(qg_plan* p, const float* q, float* psi, void* stream) {
     if (!p || !q || !psi) return QG_ERR_NULL;
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = run_prep(p, q, nullptr, 0, 0, s);
-    if (!e) e = run_dst_solve(p, s);
+    if (!e) e = run_inversion(p, s);
     if (!e)
         e = timed(p, QG_K_OTHER, s, [&] {
             return launch_mode_to_layer(p->md, p->st_tiles, p->n_st, p->st_large, p->XC, psi, s, use_pdl(p));
@@ -987,7 +1040,7 @@ int qg_rhs(qg_plan* p, const float* q, float* dq, const float* params, int flags
     const int bc = (flags & QG_RHS_APPLY_BC) ? 1 : 0;
     // q is staged into the S1 plane (TMA-able pitch); the stencil applies the BC on read
     cudaError_t e = run_prep(p, q, p->S1, 0, bc, s);
-    if (!e) e = run_dst_solve(p, s);
+    if (!e) e = run_inversion(p, s);
     if (!e) {
         StencilArgs a = stencil_args(p, params);
         a.q_sel = 1;
@@ -1014,7 +1067,7 @@ int qg_step(qg_plan* p, float* q, const float* params, double dt, int n_steps, i
     if (e) return cuda_err(e);
     // while profiling, the multi-launch path runs so that every kernel class gets its events
     const bool persistent = p->opts.persistent && p->opts.dst_precision != QG_DST_FP32 &&
-                            p->opts.refine_sweeps == 0 && !p->profiling;
+                            p->opts.refine_sweeps == 0 && !p->profiling && p->n_cap == 0;
     const bool use_graph = p->opts.use_graphs && !p->profiling;
     if (persistent && n_steps > 0) {
         PersistArgs a = p->pa;
@@ -1066,6 +1119,7 @@ int qg_rhs_vjp(qg_plan* p, const float* q, const float* params, const float* dq_
                float* params_bar, int flags, void* stream) {
     if (!p || !q || !params || !dq_bar || !q_bar) return QG_ERR_NULL;
     if (flags & ~QG_RHS_APPLY_BC) return QG_ERR_ARG;
+    if (p->n_cap > 0) return QG_ERR_UNSUPPORTED;  // no adjoint of the masked inversion yet
     cudaStream_t s = (cudaStream_t)stream;
     const int bc = (flags & QG_RHS_APPLY_BC) ? 1 : 0;
     // forward psi (layer, caller packing) into the YA plane, which holds at least one field
@@ -1095,6 +1149,7 @@ int qg_rhs_vjp(qg_plan* p, const float* q, const float* params, const float* dq_
 
 int qg_invert_vjp(qg_plan* p, const float* psi_bar, float* q_bar, void* stream) {
     if (!p || !psi_bar || !q_bar) return QG_ERR_NULL;
+    if (p->n_cap > 0) return QG_ERR_UNSUPPORTED;
     cudaStream_t s = (cudaStream_t)stream;
     VjpArgs v = vjp_args(p);
     cudaError_t e = timed(p, QG_K_PREP, s, [&] { return launch_vjp_operand(v, psi_bar, s); });
@@ -1107,7 +1162,7 @@ int qg_diagnose(qg_plan* p, const float* q, float* ke, float* ens, void* stream)
     if (!p || !q || !ke || !ens) return QG_ERR_NULL;
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = run_prep(p, q, nullptr, 0, 0, s);
-    if (!e) e = run_dst_solve(p, s);
+    if (!e) e = run_inversion(p, s);
     if (!e) e = cudaMemsetAsync(p->diag_acc, 0, sizeof(double) * 2 * p->total_layers, s);
     if (!e)
         e = timed(p, QG_K_OTHER, s, [&] {

@@ -124,6 +124,7 @@ using namespace qg;
 extern "C" int qg_invert_static(const qg_member_desc* member, const float* q, float* psi, void* stream) {
     if (!member || !q || !psi) return QG_ERR_NULL;
     const qg_member_desc& d = *member;
+    if (d.mask) return QG_ERR_UNSUPPORTED;  // land needs the plan's capacitance matrices
     const int v = validate_member(d);
     if (v != QG_OK) return v;
     const int Ny = d.ny + 2, Nx = d.nx + 2, nl = d.n_layers;

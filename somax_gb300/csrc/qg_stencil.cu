@@ -34,11 +34,12 @@ __global__ void __launch_bounds__(NTHREADS) k_prep(PrepArgs a) {
         const int j = t.ty * TY + c / TX, i = t.tx * TX + c % TX;
         if (j >= M.Ny || i >= M.Nx) continue;
         const bool ring = on_ring(j, i, M.Ny, M.Nx);
+        const bool land = is_land(M, j, i);  // q reads as zero on land
         float v[kMaxLayers];
         for (int l = 0; l < nl; ++l) {
             const float x = a.q[caller_idx(M, l, j, i)];
-            if (a.copy) a.copy[xrow_idx(M, l, j, i)] = (a.zero_ring_copy && ring) ? 0.f : x;
-            v[l] = (a.bc_operand && ring) ? 0.f : x;
+            if (a.copy) a.copy[xrow_idx(M, l, j, i)] = (a.zero_ring_copy && (ring || land)) ? 0.f : x;
+            v[l] = ((a.bc_operand && ring) || land) ? 0.f : x;
         }
         if (!a.xa) continue;
         for (int m = 0; m < nl; ++m) {
@@ -84,7 +85,7 @@ __global__ void __launch_bounds__(NTHREADS) k_mode_to_layer(const MemberDev* __r
     for (int c = threadIdx.x; c < TX * TY; c += blockDim.x) {
         const int j = t.ty * TY + c / TX, i = t.tx * TX + c % TX;
         if (j >= M.Ny || i >= M.Nx) continue;
-        const bool zero = !M.barotropic && on_ring(j, i, M.Ny, M.Nx);
+        const bool zero = (!M.barotropic && on_ring(j, i, M.Ny, M.Nx)) || is_land(M, j, i);
         float ph[kMaxLayers];
         for (int m = 0; m < nl; ++m) ph[m] = psi_hat[xrow_idx(M, m, j, i)];
         for (int l = 0; l < nl; ++l) {
@@ -153,6 +154,7 @@ __global__ void __launch_bounds__(NTHREADS) k_diag(const MemberDev* __restrict__
         if (j <= 0 || i <= 0 || j >= Ny - 1 || i >= Nx - 1) {
             if (!M.barotropic || j < 0 || i < 0 || j >= Ny || i >= Nx) return 0.f;
         }
+        if (is_land(M, j, i)) return 0.f;
         float p = 0.f;
         for (int m = 0; m < nl; ++m) p = fmaf(M.Cm2l[l * kMaxLayers + m], psi_hat[xrow_idx(M, m, j, i)], p);
         return p;
@@ -172,7 +174,7 @@ __global__ void __launch_bounds__(NTHREADS) k_diag(const MemberDev* __restrict__
             const float uT = 0.5f * (uV(l, j, i) + uV(l, j - 1, i));
             const float vT = 0.5f * (vU(l, j, i) + vU(l, j, i - 1));
             ke[l] += (double)uT * uT + (double)vT * vT;
-            const float qv = q[caller_idx(M, l, j, i)];
+            const float qv = is_land(M, j, i) ? 0.f : q[caller_idx(M, l, j, i)];
             en[l] += (double)qv * qv;
         }
     }

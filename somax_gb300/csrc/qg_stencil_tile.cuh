@@ -107,13 +107,14 @@ __device__ __forceinline__ void stencil_fix_box(const MemberDev& M, float* sq, f
     for (int c = threadIdx.x; c < BOX; c += NTHREADS) {
         const int j = j0 + c / BX, i = i0 + c % BX;
         const bool ring = edge && j >= 0 && j < Ny && i >= 0 && i < Nx && on_ring(j, i, Ny, Nx);
-        if (apply_bc && ring)
+        const bool land = is_land(M, j, i);  // q and psi are zero on land
+        if ((apply_bc && ring) || land)
 #pragma unroll
             for (int l = 0; l < NL; ++l) sq[l * BOX + c] = 0.f;
         float ph[NL];
 #pragma unroll
         for (int m = 0; m < NL; ++m) ph[m] = sp[m * BOX + c];
-        const bool zero = ring && !M.barotropic;
+        const bool zero = (ring && !M.barotropic) || land;
 #pragma unroll
         for (int l = 0; l < NL; ++l) {
             float p = 0.f;
@@ -129,7 +130,7 @@ __device__ __forceinline__ void stencil_fix_box(const MemberDev& M, float* sq, f
     for (int c = threadIdx.x; c < LW * LH; c += NTHREADS) {
         const int sy = 1 + c / LW, sx = 3 + c % LW;  // box coordinates
         const int j = j0 + sy, i = i0 + sx;
-        const bool interior = j > 0 && i > 0 && j < Ny - 1 && i < Nx - 1;
+        const bool interior = j > 0 && i > 0 && j < Ny - 1 && i < Nx - 1 && !is_land(M, j, i);
         const int b = sy * BX + sx;
 #pragma unroll
         for (int l = 0; l < NL; ++l) {
@@ -172,13 +173,14 @@ __device__ __forceinline__ bool stencil_compute(const StencilArgs& a, const Memb
         const int j = t.ty * T::TY + ly;
         if (j >= Ny || i >= Nx) continue;
         const bool ring = on_ring(j, i, Ny, Nx);
+        const bool land = is_land(M, j, i);  // no dynamics on land
         const int s0 = (ly + 2) * BX + (lx + 4);  // box index of the cell
         const float wind = tau0 * Fj[r] * M.invH0;
         float d[NL];
 #pragma unroll
         for (int l = 0; l < NL; ++l) {
-            if (ring) {
-                d[l] = (l == 0) ? wind : 0.f;
+            if (ring || land) {
+                d[l] = (ring && l == 0) ? wind : 0.f;
                 continue;
             }
             const float* Q = sq + l * BOX + s0;
@@ -233,7 +235,7 @@ __device__ __forceinline__ bool stencil_compute(const StencilArgs& a, const Memb
 #pragma unroll
             for (int m = 0; m < NL; ++m) {
                 float s = 0.f;
-                if (!ring)
+                if (!ring && !land)
 #pragma unroll
                     for (int l = 0; l < NL; ++l) s = fmaf(M.Cl2m[m * kMaxLayers + l], yn[l], s);
                 store_plane(a.xa, a.xa_fmt, a.xplane, xrow_idx(M, m, j, i), s);

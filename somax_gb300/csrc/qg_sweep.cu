@@ -38,6 +38,7 @@ struct Win {
     // four-row windows indexed by row & 3 (east / west values come from the neighbouring
     // lanes when they are used, which keeps the windows small enough for 16 warps per SM)
     float q[NL][4], p[NL][4], lq[NL][4];
+    bool land[4];  // interior land cell of the row (masked members)
     // raw rows in flight, indexed by row & 1
     float rq[NL][2], rh[NL][2];
 };
@@ -62,20 +63,22 @@ __device__ __forceinline__ void fetch(Win<NL>& w, const float* __restrict__ qb, 
 // r - 1 (window slot (K + 3) & 3, needs rows r - 2 .. r).
 template <int NL, int S, int K>
 __device__ __forceinline__ void ingest(Win<NL>& w, const float (&cm)[NL][NL], const Coef& c, int r, int Ny, int x,
-                                       int Nx, bool apply_bc, bool zero_psi_ring) {
+                                       int Nx, bool apply_bc, bool zero_psi_ring, const uint8_t* mask) {
     const bool ring = r == 0 || r == Ny - 1 || x == 0 || x == Nx - 1;
+    const bool land = mask && r > 0 && r < Ny - 1 && x > 0 && x < Nx - 1 && mask[(int64_t)r * Nx + x] == 0;
+    w.land[K] = land;
 #pragma unroll
-    for (int l = 0; l < NL; ++l) w.q[l][K] = (apply_bc && ring) ? 0.f : w.rq[l][S];
+    for (int l = 0; l < NL; ++l) w.q[l][K] = ((apply_bc && ring) || land) ? 0.f : w.rq[l][S];
 #pragma unroll
     for (int l = 0; l < NL; ++l) {
         float p = 0.f;
 #pragma unroll
         for (int m = 0; m < NL; ++m) p = fmaf(cm[l][m], w.rh[m][S], p);
-        w.p[l][K] = (zero_psi_ring && ring) ? 0.f : p;
+        w.p[l][K] = ((zero_psi_ring && ring) || land) ? 0.f : p;
     }
     constexpr int K1 = (K + 3) & 3, K2 = (K + 2) & 3;
     const int r1 = r - 1;
-    const bool inter = r1 > 0 && r1 < Ny - 1 && x > 0 && x < Nx - 1;
+    const bool inter = r1 > 0 && r1 < Ny - 1 && x > 0 && x < Nx - 1 && !w.land[K1];
 #pragma unroll
     for (int l = 0; l < NL; ++l) {
         const float q1 = w.q[l][K1];
@@ -92,6 +95,7 @@ __device__ __forceinline__ bool output(const StencilArgs& a, const MemberDev& M,
     constexpr int N = (J + 1) & 3, S = (J + 3) & 3;  // rows j + 1 and j - 1
     const int Ny = M.Ny, Nx = M.Nx;
     const bool ring = j == 0 || j == Ny - 1 || x == 0 || x == Nx - 1;
+    const bool land = w.land[J];  // no dynamics on land
     const float wind = c.tau0 * Fj * c.invH0;
     // y0 of the row, loaded before the arithmetic that hides its latency
     float y0[NL];
@@ -121,7 +125,7 @@ __device__ __forceinline__ bool output(const StencilArgs& a, const MemberDev& M,
         const float L0 = w.lq[l][J];
         v += c.nu * L0;
         v -= c.nu4 * ((le - 2.f * L0 + lw) * c.idx2 + (w.lq[l][N] - 2.f * L0 + w.lq[l][S]) * c.idy2);
-        d[l] = ring ? (l == 0 ? wind : 0.f) : v;
+        d[l] = ring ? (l == 0 ? wind : 0.f) : (land ? 0.f : v);
     }
     bool bad = false;
 #pragma unroll
@@ -147,7 +151,7 @@ __device__ __forceinline__ bool output(const StencilArgs& a, const MemberDev& M,
             float s = 0.f;
 #pragma unroll
             for (int l = 0; l < NL; ++l) s = fmaf(cl[m][l], yn[l], s);
-            s = ring ? 0.f : s;
+            s = (ring || land) ? 0.f : s;
             const int64_t o = xo + m * lstride_x;
             if (a.xa_fmt == FMT_F32) {
                 static_cast<float*>(a.xa)[o] = s;
@@ -208,7 +212,7 @@ __device__ __forceinline__ bool sweep(const StencilArgs& a, const MemberDev& M, 
 #define QG_SWEEP_ROW(K)                                                                                 \
         {                                                                                               \
             const int r = rb + K;                                                                       \
-            ingest<NL, (K) & 1, K>(w, cm, c, r, Ny, x, Nx, apply_bc, zero_psi_ring);                    \
+            ingest<NL, (K) & 1, K>(w, cm, c, r, Ny, x, Nx, apply_bc, zero_psi_ring, M.mask);            \
             fetch<NL, (K) & 1>(w, qb, hb, lsx, r + 2, Ny, x, Nx, Px);                                   \
             const int j = r - 2;                                                                        \
             if (j >= jb && j < je) {                                                                    \

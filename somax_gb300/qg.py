@@ -349,6 +349,7 @@ class MemberSpec:
     wind_profile: str = "doublegyre"
     eigs: str = "consistent"
     modal: ModalTransform | None = None
+    mask: np.ndarray | None = None  # (ny + 2, nx + 2) land mask, 1 = ocean (extension)
 
     @property
     def n_layers(self) -> int:
@@ -367,6 +368,12 @@ class MemberSpec:
             d.g_prime[k] = float(self.g_prime[k]) if not self.barotropic else 1.0
         d.wind_profile = K["QG_WIND_SINGLE"] if self.wind_profile == "single" else K["QG_WIND_DOUBLEGYRE"]
         d.eigs_mode = K["QG_EIGS_REFERENCE"] if self.eigs == "reference" else K["QG_EIGS_CONSISTENT"]
+        if self.mask is not None:
+            m = np.ascontiguousarray(self.mask, dtype=np.uint8)
+            if m.shape != (self.ny + 2, self.nx + 2):
+                raise ValueError(f"mask must have shape {(self.ny + 2, self.nx + 2)}, got {m.shape}")
+            self._mask_c = m  # kept alive while qg_plan_create reads it
+            d.mask = m.ctypes.data_as(C.POINTER(C.c_ubyte))
         if self.modal is not None and not self.barotropic:
             d.has_modes = 1
             lam = self.f0**2 * np.asarray(self.modal.eigenvalues, float)
@@ -472,7 +479,16 @@ class _QGBase(SomaxModel):
         return self.state_cls(q=plan.rhs(q, pv, apply_bc=False))
 
     def apply_boundary_conditions(self, state):
-        return self.state_cls(q=_zero_ring(state.q))
+        """Zero ring (``baroclinic.py:192-195``); with a land mask, land cells are zeroed too."""
+        q = _zero_ring(state.q)
+        if self.spec.mask is not None:
+            ocean = torch.as_tensor(np.asarray(self.spec.mask) != 0, device=q.device)
+            ocean[0, :] = True
+            ocean[-1, :] = True
+            ocean[:, 0] = True
+            ocean[:, -1] = True
+            q = q * ocean.to(q.dtype)
+        return self.state_cls(q=q)
 
     def step(self, state, dt: float, n_steps: int = 1, solver="ssprk3", out: torch.Tensor | None = None,
              apply_bc: bool = True):
@@ -615,7 +631,7 @@ class BaroclinicQG(_QGBase):
                H=(400.0, 1100.0, 2600.0), g_prime=(9.81, 0.025, 0.0125), stratification=None,
                lateral_viscosity=0.0, bottom_drag=0.0, wind_amplitude=0.0, wind_profile="doublegyre",
                poisson_bc="dst", biharmonic_viscosity=0.0, precision="fp32", refine=0, eigs="consistent",
-               use_graphs=True, persistent=True, stencil=None, gemm_tile=None) -> "BaroclinicQG":
+               use_graphs=True, persistent=True, stencil=None, gemm_tile=None, mask=None) -> "BaroclinicQG":
         """``BaroclinicQG.create`` (``baroclinic.py:230-332``) with the same keyword arguments,
         plus ``biharmonic_viscosity`` (extension), ``precision`` of the DST-I GEMMs
         ("fp32", "tf32", "bf16x3"), ``refine`` sweeps, the ``eigs`` mode and whether ``step`` runs
@@ -631,7 +647,7 @@ class BaroclinicQG(_QGBase):
             strat = StratificationProfile.from_layers(H=list(H), g_prime=list(g_prime))
         modal = ModalTransform.from_stratification(strat, f0, eigs)
         spec = MemberSpec(nx, ny, Lx, Ly, f0, beta, list(strat.H), list(strat.g_prime), False, wind_profile,
-                          eigs, modal)
+                          eigs, modal, mask)
         params = QGParams(*(torch.tensor(float(v)) for v in (lateral_viscosity, bottom_drag, wind_amplitude,
                                                              biharmonic_viscosity)))
         return BaroclinicQG(spec, params, precision, refine, use_graphs, strat, modal, persistent, stencil, gemm_tile)
@@ -651,9 +667,9 @@ class BarotropicQG(_QGBase):
     def create(nx=64, ny=64, Lx=1e6, Ly=1e6, f0=1e-4, beta=1.6e-11, lateral_viscosity=0.0,
                bottom_drag=0.0, wind_amplitude=0.0, wind_profile="doublegyre", biharmonic_viscosity=0.0,
                precision="fp32", refine=0, use_graphs=True, persistent=True, stencil=None,
-               gemm_tile=None) -> "BarotropicQG":
+               gemm_tile=None, mask=None) -> "BarotropicQG":
         """``BarotropicQG.create`` (``barotropic.py:186-248``)."""
-        spec = MemberSpec(nx, ny, Lx, Ly, f0, beta, [1.0], [1.0], True, wind_profile)
+        spec = MemberSpec(nx, ny, Lx, Ly, f0, beta, [1.0], [1.0], True, wind_profile, mask=mask)
         params = QGParams(*(torch.tensor(float(v)) for v in (lateral_viscosity, bottom_drag, wind_amplitude,
                                                              biharmonic_viscosity)))
         return BarotropicQG(spec, params, precision, refine, use_graphs, persistent=persistent, stencil=stencil,

@@ -117,3 +117,37 @@ def initial_pv(cfg: QGConfig, seed: int = 0, rms_vorticity: float = 1e-6) -> np.
     for l in range(cfg.nl):
         f[l] *= scale * cfg.H[0] / cfg.H[l]
     return f
+
+
+def land_mask(ny: int, nx: int, frac: float = 0.15, seed: int = 0, n_blobs: int = 8) -> np.ndarray:
+    """(ny + 2, nx + 2) uint8 land mask of a masked basin (1 = ocean): the ring is land and
+    ``n_blobs`` connected land blobs grown from seeded centres cover ``frac`` of the interior
+    T-cells.  A blob is the set of cells within r(theta) = R (1 + 0.15 sin(3 theta + a) +
+    0.1 sin(5 theta + b)) of its centre (a wavy coastline); all blobs grow together (R scaled
+    by bisection) until the land fraction is reached."""
+    rng = np.random.default_rng(seed)
+    Ny, Nx = ny + 2, nx + 2
+    cy = rng.uniform(0.1, 0.9, n_blobs) * ny + 1
+    cx = rng.uniform(0.1, 0.9, n_blobs) * nx + 1
+    rel = rng.uniform(0.6, 1.4, n_blobs)
+    ph = rng.uniform(0, 2 * math.pi, (n_blobs, 2))
+    jj, ii = np.mgrid[0:Ny, 0:Nx]
+    dist = []
+    for b in range(n_blobs):
+        dy, dx = jj - cy[b], ii - cx[b]
+        th = np.arctan2(dy, dx)
+        shape = rel[b] * (1 + 0.15 * np.sin(3 * th + ph[b, 0]) + 0.1 * np.sin(5 * th + ph[b, 1]))
+        dist.append(np.hypot(dy, dx) / shape)
+    dmin = np.min(dist, axis=0)[1:-1, 1:-1]
+    target = frac * ny * nx
+    lo, hi = 0.0, float(max(ny, nx))
+    for _ in range(60):
+        mid = 0.5 * (lo + hi)
+        if (dmin <= mid).sum() < target:
+            lo = mid
+        else:
+            hi = mid
+    mask = np.ones((Ny, Nx), np.uint8)
+    mask[1:-1, 1:-1][dmin <= hi] = 0
+    mask[0, :] = mask[-1, :] = mask[:, 0] = mask[:, -1] = 0
+    return mask

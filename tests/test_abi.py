@@ -30,8 +30,9 @@ def test_strerror(L):
 
 
 def test_struct_layout_matches_header(L):
-    # 4 ints, 4 doubles, 2 x 8 doubles, 3 ints (+4 pad), 2 x 64 doubles, 8 doubles
-    assert C.sizeof(_lib.MemberDesc) == 16 + 32 + 128 + 16 + 1024 + 64
+    # 4 ints, 4 doubles, 2 x 8 doubles, 3 ints (+4 pad), 2 x 64 doubles, 8 doubles, mask pointer
+    assert C.sizeof(_lib.MemberDesc) == 16 + 32 + 128 + 16 + 1024 + 64 + 8
+    assert _lib.MemberDesc.mask.offset == 16 + 32 + 128 + 16 + 1024 + 64
     assert C.sizeof(_lib.Options) == 32
 
 
