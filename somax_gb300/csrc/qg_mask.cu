@@ -4,8 +4,9 @@
 // One CTA per (member, mode, block of kCapRows rows of C^-1): it gathers psi_hat of the first
 // solve at the member's boundary points B into shared memory (FP64), then each warp forms
 // sigma_r = -sum_j Cinv[r][j] psi_hat[B_j] for its rows with coalesced row reads and a warp
-// reduction in FP64, and writes sigma_r at B_r into the GEMM operand of the second solve (the
-// operand is zero there: B is land) and into its FP32 copy.  The C^-1 read dominates: 8 k^2
+// reduction in FP64, and adds sigma_r at B_r to the GEMM operand of the next solve (zero there
+// before the first correction: B is land) and to its FP32 copy.  A repeated correction
+// removes what the FP32 / split-BF16 solve leaves of psi on B after the first.  The C^-1 read dominates: 8 k^2
 // bytes per mode, the kernel's HBM roofline.
 #include <cuda_bf16.h>
 
@@ -42,18 +43,21 @@ __global__ void __launch_bounds__(NT) k_capacitance(const MemberDev* __restrict_
         for (int j = lane; j < k; j += 32) s = fma(row[j], v[j], s);
         for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
         if (lane == 0) {
-            const float sig = (float)(-s);
+            // accumulate: a repeated correction adds to the sources already at B
             const int b = M.bidx[r];
             const int64_t o = M.off_x + ((int64_t)m * M.Ny + b / Nx) * M.Px + (b % Nx);
             if (xa_fmt == FMT_F32) {
-                static_cast<float*>(xa)[o] = sig;
+                float* p = static_cast<float*>(xa);
+                p[o] = (float)((double)p[o] - s);
             } else {
                 __nv_bfloat16* p = static_cast<__nv_bfloat16*>(xa);
+                const double cur = (double)__bfloat162float(p[o]) + (double)__bfloat162float(p[xplane + o]);
+                const float sig = (float)(cur - s);
                 const __nv_bfloat16 hi = __float2bfloat16_rn(sig);
                 p[o] = hi;
                 p[xplane + o] = __float2bfloat16_rn(sig - __bfloat162float(hi));
             }
-            if (xq) xq[o] = sig;
+            if (xq) xq[o] = (float)((double)xq[o] - s);
         }
     }
 }

@@ -386,16 +386,46 @@ cudaError_t run_dst_solve(qg_plan* p, cudaStream_t s) {
     return cudaSuccess;
 }
 
+VjpArgs vjp_args(qg_plan* p) {
+    VjpArgs v{};
+    v.members = p->md;
+    v.tiles = p->st_tiles;
+    v.ntiles = p->n_st;
+    v.tile_x = p->st_large ? kTileLX : kTileSX;
+    v.tile_y = p->st_large ? kTileLY : kTileSY;
+    v.max_nl = p->max_nl;
+    v.n_members = p->n_members;
+    v.pacc = p->vjp_acc;
+    v.xa = p->XA;
+    v.xa_fmt = p->op_fmt;
+    v.xq = p->XQ;
+    v.xplane = p->xplane;
+    return v;
+}
+
 // psi_hat (XC) with the masked members' capacitance correction: solve, sigma at B into the
-// operand, solve again (the operand is otherwise unchanged: it is zero on land).
+// operand, solve again (the operand is otherwise unchanged: it is zero on land).  With
+// refinement the correction repeats once more, so that psi on B falls to the solve's
+// precision squared (the FP64 capacitance matrices are exact, the solves are not).
 cudaError_t run_inversion(qg_plan* p, cudaStream_t s) {
     cudaError_t e = run_dst_solve(p, s);
     if (e || p->n_cap == 0) return e;
-    e = timed(p, QG_K_OTHER, s, [&] {
-        return launch_capacitance(p->md, p->cap_items, p->n_cap, p->XC, p->XA, p->op_fmt, p->XQ, p->xplane,
-                                  p->cap_smem, s);
-    });
-    if (!e) e = run_dst_solve(p, s);
+    for (int c = 0; c < 1 + p->opts.refine_sweeps && !e; ++c) {
+        e = timed(p, QG_K_OTHER, s, [&] {
+            return launch_capacitance(p->md, p->cap_items, p->n_cap, p->XC, p->XA, p->op_fmt, p->XQ, p->xplane,
+                                      p->cap_smem, s);
+        });
+        // a refinement sweep leaves its residual in the operand: rebuild it from the FP32
+        // right-hand side (which holds the sources on B)
+        if (!e && p->opts.refine_sweeps > 0)
+            e = timed(p, QG_K_PREP, s, [&] {
+                VjpArgs v = vjp_args(p);
+                v.rhs = p->XQ;
+                v.xq = nullptr;
+                return launch_vjp_operand(v, nullptr, s);
+            });
+        if (!e) e = run_dst_solve(p, s);
+    }
     return e;
 }
 
@@ -658,27 +688,6 @@ cudaError_t tmap_encode(void* map, int bf16, int rank, const void* base, const u
 // =======================================================================================
 // C ABI
 // =======================================================================================
-namespace {
-
-VjpArgs vjp_args(qg_plan* p) {
-    VjpArgs v{};
-    v.members = p->md;
-    v.tiles = p->st_tiles;
-    v.ntiles = p->n_st;
-    v.tile_x = p->st_large ? kTileLX : kTileSX;
-    v.tile_y = p->st_large ? kTileLY : kTileSY;
-    v.max_nl = p->max_nl;
-    v.n_members = p->n_members;
-    v.pacc = p->vjp_acc;
-    v.xa = p->XA;
-    v.xa_fmt = p->op_fmt;
-    v.xq = p->XQ;
-    v.xplane = p->xplane;
-    return v;
-}
-
-}  // namespace
-
 extern "C" {
 
 const char* qg_strerror(int code) {
