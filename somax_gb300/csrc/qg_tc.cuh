@@ -176,8 +176,9 @@ __device__ __forceinline__ void tc_store_bf16x2(__nv_bfloat16* p, int64_t plane,
     p[plane + idx] = __float2bfloat16_rn(v - __bfloat162float(hi));
 }
 
-// Per-warp staging buffer of the epilogue: 32 rows x 32 columns, padded.
-constexpr int TC_STAGE_FLOATS = 32 * 33;
+// Per-warp staging buffer of the epilogue: 32 rows x 32 columns, padded, and a 32-float row
+// table (the spectral divide's row term).
+constexpr int TC_STAGE_FLOATS = 32 * 33 + 32;
 constexpr int TC_EPI_SMEM = 4 * TC_STAGE_FLOATS * 4;  // bytes, four epilogue warps
 
 // Epilogue of one 128 x width tile by one of four epilogue warps (TMEM lane quarter
@@ -223,28 +224,51 @@ __device__ __forceinline__ void tc_epilogue(const MemberDev& M, const TcGeom& g,
                     tc_store_bf16x2(Cb, cplane, o, x);
             }
         } else {
-            float eyv = 0.f;
-            if (PASS == G2_FWD_Y) eyv = (nb + lane < nend) ? ey[nb + lane] : 1.f;
+            // row-major store: stage the 32 x 32 block (row = lane), then every store writes
+            // two adjacent columns of two rows per warp instruction (lanes 0-15: row rr,
+            // lanes 16-31: row rr + 1), so a warp covers 2 x 64 contiguous bytes per plane
 #pragma unroll
-            for (int j = 0; j < 32; ++j) {
-                float x = __uint_as_float(v[j]);
-                // spectral divide: the fast division is exact to ~2 ulp, far inside the
-                // BF16x3 / TF32 error of the transform itself
-                if constexpr (PASS == G2_FWD_Y) x = __fdividef(x, exr + __shfl_sync(0xffffffffu, eyv, j) - laml);
-                stage[lane * 33 + j] = x;  // row = lane, column = j
-            }
+            for (int j = 0; j < 32; ++j) stage[lane * 33 + j] = __uint_as_float(v[j]);
+            if constexpr (PASS == G2_FWD_Y) stage[32 * 33 + lane] = exr - laml;  // row term of the divide
             __syncwarp();
-            const int n = nb + lane;
-            for (int rr = 0; rr < 32; ++rr) {
-                const int mm = m0 + quarter * 32 + rr;
-                if (mm >= Mtot) break;
-                if (n < nend) {
+            const int c2 = 2 * (lane & 15), half = lane >> 4;
+            const int n = nb + c2;
+            float ey0 = 1.f, ey1 = 1.f;
+            if constexpr (PASS == G2_FWD_Y) {
+                if (n < nend) ey0 = ey[n];
+                if (n + 1 < nend) ey1 = ey[n + 1];
+            }
+            for (int rr = 0; rr < 32; rr += 2) {
+                const int row = rr + half;
+                const int mm = m0 + quarter * 32 + row;
+                if (mm < Mtot && n < nend) {
+                    float x0 = stage[row * 33 + c2], x1 = stage[row * 33 + c2 + 1];
+                    // spectral divide: the fast division is exact to ~2 ulp, far inside the
+                    // BF16x3 / TF32 error of the transform itself
+                    if constexpr (PASS == G2_FWD_Y) {
+                        const float rt = stage[32 * 33 + row];
+                        x0 = __fdividef(x0, rt + ey0);
+                        x1 = __fdividef(x1, rt + ey1);
+                    }
                     const int64_t o = (int64_t)mm * ldo + n;
-                    const float x = stage[rr * 33 + lane];
-                    if (c_fmt == FMT_F32)
-                        Cf[o] = (PASS == G4_INV_X && accumulate) ? Cf[o] + x : x;
-                    else
-                        tc_store_bf16x2(Cb, cplane, o, x);
+                    const bool pair = n + 1 < nend;
+                    if (c_fmt == FMT_F32) {
+                        if (PASS == G4_INV_X && accumulate) {
+                            x0 += Cf[o];
+                            if (pair) x1 += Cf[o + 1];
+                        }
+                        if (pair)
+                            *reinterpret_cast<float2*>(Cf + o) = make_float2(x0, x1);
+                        else
+                            Cf[o] = x0;
+                    } else if (pair) {
+                        const __nv_bfloat162 hi = __floats2bfloat162_rn(x0, x1);
+                        const float2 hf = __bfloat1622float2(hi);
+                        *reinterpret_cast<__nv_bfloat162*>(Cb + o) = hi;
+                        *reinterpret_cast<__nv_bfloat162*>(Cb + cplane + o) = __floats2bfloat162_rn(x0 - hf.x, x1 - hf.y);
+                    } else {
+                        tc_store_bf16x2(Cb, cplane, o, x0);
+                    }
                 }
             }
             __syncwarp();
