@@ -16,7 +16,8 @@ the ring zeroing of the stage input (``core/model.py:47-49``); its adjoint for t
 ``g`` of ``y1`` is ``k_bar_i = dt b_i g``, then for the stages in reverse
 ``Y_bar_i = F_vjp(Y_i; k_bar_i)``, ``y0_bar += Y_bar_i``, ``k_bar_j += dt a_ij Y_bar_i``.
 The fused ``qg_step`` kernels produce the same ring (``y0 + dt * wind``) as this form, so the
-forward runs fused and only the recomputed stages of one step at a time run unfused.
+forward (every scheme) runs fused and only the recomputed stages of one step at a time run
+unfused.
 """
 
 from __future__ import annotations
@@ -73,26 +74,9 @@ class Invert(torch.autograd.Function):
 
 
 def _advance(plan, q, p, dt, n, scheme):
-    """q <- n steps of ``scheme`` (in place; the ring of q is taken as it is)."""
-    if n <= 0:
-        return q
-    if scheme in ("heun", "ssprk3"):
+    """q <- n fused steps of ``scheme`` (in place; the ring of q is taken as it is)."""
+    if n > 0:
         plan.step(q, p, dt, n, scheme, apply_bc=False)
-        return q
-    a, b = rk_tableau(scheme)
-    for _ in range(n):
-        ks = []
-        for s in range(len(b)):
-            ys = q
-            if s:
-                ys = q.clone()
-                for j, aij in enumerate(a[s]):
-                    if aij:
-                        ys.add_(ks[j], alpha=dt * aij)
-            ks.append(plan.rhs(ys, p, apply_bc=True))
-        for j, bj in enumerate(b):
-            if bj:
-                q.add_(ks[j], alpha=dt * bj)
     return q
 
 

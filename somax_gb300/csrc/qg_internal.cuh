@@ -109,6 +109,26 @@ struct PrepArgs {
     int tile_x, tile_y;    // cells per tile of the tile list
 };
 
+// Butcher-form stage combine: out = y0 + dt * sum_s coef[s] * k[s] and its modal operand.
+constexpr int kMaxStages = 8;
+struct RkCombineArgs {
+    const MemberDev* members;
+    const StencilTile* tiles;
+    int tile_x, tile_y;
+    const float* y0;       // x-row state plane
+    const float* k;        // stage derivatives, caller packing, plane s at s * kplane
+    int64_t kplane;
+    int n_k;
+    float coef[kMaxStages];
+    float dt;
+    float* out;            // x-row stage plane (the next stage input or the new state)
+    void* xa;              // modal operand of `out` (zero ring and land)
+    int xa_fmt;
+    float* xq;             // its FP32 copy (refinement), or null
+    int64_t xplane;
+};
+cudaError_t launch_rk_combine(const RkCombineArgs& a, int ntiles, cudaStream_t s, bool pdl);
+
 // TMA descriptors of one member for the stencil: the three stage planes and psi_hat,
 // 3-D boxes (x, y, layer) over the padded x-row planes.
 constexpr int kStencilMapsBytes = 4 * 128;

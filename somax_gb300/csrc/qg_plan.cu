@@ -241,6 +241,7 @@ struct qg_plan {
     std::vector<void*> allocs;
     float *XA = nullptr, *XB = nullptr, *XC = nullptr, *XQ = nullptr, *YA = nullptr, *YB = nullptr;
     float *S0 = nullptr, *S1 = nullptr, *S2 = nullptr;
+    float* K = nullptr;  // Butcher-form stage derivatives (kMaxStages caller-packed fields)
     float* params = nullptr;  // plan-owned copy of the params (graph-stable)
     // masked members: capacitance work items (one per mode and block of rows of C^-1)
     CapItem* cap_items = nullptr;
@@ -498,10 +499,69 @@ int scheme_stages(int scheme, Stage* st) {
     }
 }
 
+// Butcher tableaus of the schemes stepped in Butcher form: Euler and Tsit5 (Tsitouras 2011,
+// the coefficients diffrax.Tsit5 uses).  a[s][j] (j < s) and b[s].
+struct Tableau {
+    int n;
+    double a[6][6];
+    double b[6];
+};
+const Tableau* butcher(int scheme) {
+    static const Tableau euler = {1, {{0}}, {1.0}};
+    static const Tableau tsit5 = {
+        6,
+        {{0, 0, 0, 0, 0, 0},
+         {0.161, 0, 0, 0, 0, 0},
+         {-0.008480655492356989, 0.335480655492357, 0, 0, 0, 0},
+         {2.897153057105493, -6.359448489975075, 4.3622954328695815, 0, 0, 0},
+         {5.325864828439257, -11.748883564062828, 7.4955393428898365, -0.09249506636175525, 0, 0},
+         {5.86145544294642, -12.92096931784711, 8.159367898576159, -0.071584973281401, -0.028269050394068383, 0}},
+        {0.09646076681806523, 0.01, 0.4798896504144996, 1.379008574103742, -3.290069515436081, 2.324710524099774}};
+    if (scheme == QG_SCHEME_EULER) return &euler;
+    if (scheme == QG_SCHEME_TSIT5) return &tsit5;
+    return nullptr;
+}
+
+// One Butcher-form step of the state in S0 (XA holding Cl2m BC(S0)): per stage the DST solve,
+// the stencil in rhs mode writing k_s, and the combine into the next stage input (S1) or, at
+// the last stage, the new state (S0) with the next step's operand.
+cudaError_t run_one_step_butcher(qg_plan* p, const float* params, float dt, const Tableau& tb, cudaStream_t s) {
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < tb.n && !e; ++k) {
+        if ((e = run_inversion(p, s))) break;
+        StencilArgs a = stencil_args(p, params);
+        a.q_sel = k == 0 ? 0 : 1;
+        a.apply_bc = 1;
+        a.dq = p->K + (size_t)k * p->state_size;
+        e = timed(p, QG_K_STENCIL, s, [&] { return launch_stencil(p, a, s, use_pdl(p)); });
+        if (e) break;
+        RkCombineArgs c{};
+        c.members = p->md;
+        c.tiles = p->st_tiles;
+        c.tile_x = p->st_large ? kTileLX : kTileSX;
+        c.tile_y = p->st_large ? kTileLY : kTileSY;
+        c.y0 = p->S0;
+        c.k = p->K;
+        c.kplane = p->state_size;
+        const bool fin = k == tb.n - 1;
+        c.n_k = k + 1;
+        for (int j = 0; j <= k; ++j) c.coef[j] = (float)(fin ? tb.b[j] : tb.a[k + 1][j]);
+        c.dt = dt;
+        c.out = fin ? p->S0 : p->S1;
+        c.xa = p->XA;
+        c.xa_fmt = p->op_fmt;
+        c.xq = p->XQ;
+        c.xplane = p->xplane;
+        e = timed(p, QG_K_OTHER, s, [&] { return launch_rk_combine(c, p->n_st, s, use_pdl(p)); });
+    }
+    return e;
+}
+
 // One time step of the state in S0 (XA holding Cl2m BC(S0)).  Stage k reads stage plane k
 // (S0, S1, S2) and writes stage plane k + 1; the final stage updates S0 in place (it reads S0
 // only pointwise there) and leaves XA ready for the next step.
 cudaError_t run_one_step(qg_plan* p, const float* params, float dt, int scheme, cudaStream_t s) {
+    if (const Tableau* tb = butcher(scheme)) return run_one_step_butcher(p, params, dt, *tb, s);
     Stage st[4];
     const int ns = scheme_stages(scheme, st);
     float* stage_buf[3] = {p->S0, p->S1, p->S2};
@@ -927,6 +987,7 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
             e = dalloc(p, &p->diag_acc, (size_t)2 * p->total_layers * sizeof(double));
         if (!e) e = dalloc(p, &p->vjp_acc, (size_t)n_members * QG_NPARAMS * sizeof(double));
         if (!e && o.refine_sweeps > 0) e = dalloc(p, &p->XQ, xb);
+        if (!e) e = dalloc(p, &p->K, (size_t)6 * p->state_size * sizeof(float));  // Tsit5: 6 stages
     }
     if (e == cudaSuccess && tc) {
         // one set of TMA descriptors per (member, pass); the planes never move
@@ -1065,7 +1126,7 @@ int qg_step(qg_plan* p, float* q, const float* params, double dt, int n_steps, i
     if (!p || !q || !params) return QG_ERR_NULL;
     if (n_steps < 0 || (flags & ~QG_STEP_APPLY_BC)) return QG_ERR_ARG;
     Stage st[4];
-    if (scheme_stages(scheme, st) == 0) return QG_ERR_ARG;
+    if (scheme_stages(scheme, st) == 0 && !butcher(scheme)) return QG_ERR_ARG;
     if (!(dt == dt)) return QG_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = cudaMemcpyAsync(p->params, params, sizeof(float) * p->n_members * QG_NPARAMS,
@@ -1076,7 +1137,7 @@ int qg_step(qg_plan* p, float* q, const float* params, double dt, int n_steps, i
     if (e) return cuda_err(e);
     // while profiling, the multi-launch path runs so that every kernel class gets its events
     const bool persistent = p->opts.persistent && p->opts.dst_precision != QG_DST_FP32 &&
-                            p->opts.refine_sweeps == 0 && !p->profiling && p->n_cap == 0;
+                            p->opts.refine_sweeps == 0 && !p->profiling && p->n_cap == 0 && !butcher(scheme);
     const bool use_graph = p->opts.use_graphs && !p->profiling;
     if (persistent && n_steps > 0) {
         PersistArgs a = p->pa;

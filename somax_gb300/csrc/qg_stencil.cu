@@ -69,6 +69,45 @@ __global__ void __launch_bounds__(NTHREADS) k_unpack(const MemberDev* __restrict
 }
 
 // ---------------------------------------------------------------------------------------
+// Butcher-form stage combine (Euler, Tsit5): out = y0 + dt * sum_j c_j k_j over the stage
+// derivatives k_j (caller packing, one plane of `kplane` floats each), into an x-row stage
+// plane, plus the modal operand of that stage input (BC: zero ring and land) for the next DST
+// solve.  The ring is combined like every other cell; stage inputs are read with the BC, and
+// the final combination's ring is y0 + dt * wind as in the fused Shu-Osher stencil.
+// ---------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(NTHREADS) k_rk_combine(RkCombineArgs a) {
+    __shared__ MemberDev M;
+    const StencilTile t = a.tiles[blockIdx.x];
+    load_member(&M, a.members + t.member);
+    __syncthreads();
+    pdl_wait();
+    pdl_launch_dependents();
+    const int nl = M.nl, TX = a.tile_x, TY = a.tile_y;
+    for (int c = threadIdx.x; c < TX * TY; c += blockDim.x) {
+        const int j = t.ty * TY + c / TX, i = t.tx * TX + c % TX;
+        if (j >= M.Ny || i >= M.Nx) continue;
+        const bool zero = on_ring(j, i, M.Ny, M.Nx) || is_land(M, j, i);
+        float v[kMaxLayers];
+        for (int l = 0; l < nl; ++l) {
+            const int64_t ci = caller_idx(M, l, j, i);
+            float acc = 0.f;
+            for (int s = 0; s < a.n_k; ++s)
+                if (a.coef[s] != 0.f) acc = fmaf(a.coef[s], a.k[(int64_t)s * a.kplane + ci], acc);
+            const int64_t xi = xrow_idx(M, l, j, i);
+            v[l] = a.y0[xi] + a.dt * acc;
+            a.out[xi] = v[l];
+        }
+        for (int m = 0; m < nl; ++m) {
+            float sum = 0.f;
+            if (!zero)
+                for (int l = 0; l < nl; ++l) sum = fmaf(M.Cl2m[m * kMaxLayers + l], v[l], sum);
+            store_plane(a.xa, a.xa_fmt, a.xplane, xrow_idx(M, m, j, i), sum);
+            if (a.xq) a.xq[xrow_idx(M, m, j, i)] = sum;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------
 // Mode -> layer epilogue for qg_invert: psi = Cm2l psi_hat, ring zeroed (baroclinic).
 // ---------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(NTHREADS) k_mode_to_layer(const MemberDev* __restrict__ members,
@@ -236,6 +275,10 @@ cudaError_t stencil_encode_maps(const MemberDev& M, const float* const planes[4]
 
 cudaError_t launch_prep(const PrepArgs& a, int ntiles, cudaStream_t s, bool pdl) {
     return launch_k(k_prep, ntiles, NTHREADS, 0, s, pdl, a);
+}
+
+cudaError_t launch_rk_combine(const RkCombineArgs& a, int ntiles, cudaStream_t s, bool pdl) {
+    return launch_k(k_rk_combine, ntiles, NTHREADS, 0, s, pdl, a);
 }
 
 cudaError_t launch_unpack(const MemberDev* members, const StencilTile* tiles, int ntiles, int large,

@@ -297,13 +297,19 @@ class Plan:
 
     def launches_per_call(self, n_steps: int, scheme: str) -> int:
         """Kernels libqgcore launches for one ``step`` call of ``n_steps`` steps."""
-        stages = {"heun": 2, "ssprk3": 3}[scheme]
-        if self.persistent and self.precision != "fp32" and self.refine == 0:
+        stages = {"euler": 1, "heun": 2, "ssprk3": 3, "tsit5": 6}[scheme]
+        butcher = scheme in ("euler", "tsit5")
+        masked = any(m.mask is not None for m in self.members)
+        if self.persistent and self.precision != "fp32" and self.refine == 0 and not butcher and not masked:
             return 3  # pack, the persistent step kernel, unpack
         # the column-sweep stencil launches once per distinct layer count
         sweep = self.tuning()["stencil"].startswith("sweep")
         stencil = len({m.n_layers for m in self.members}) if sweep else 1
-        per_stage = 4 * (1 + self.refine) + self.refine + stencil
+        solve = 4 * (1 + self.refine) + self.refine
+        inversion = solve
+        if masked:  # capacitance correction(s), each followed by a solve
+            inversion += (1 + self.refine) * (1 + (1 if self.refine else 0) + solve)
+        per_stage = inversion + stencil + (1 if butcher else 0)
         return 2 + n_steps * stages * per_stage
 
     STENCIL_VARIANTS = ("tile32x8", "tile64x16", "sweep16", "sweep32", "sweep64")
@@ -508,42 +514,13 @@ class _QGBase(SomaxModel):
         else:
             q = self._field(q_in).clone()
         scheme = _solver_name(solver)
-        if scheme in ("heun", "ssprk3"):
-            self.plan(q.device).step(q, self._param_vector(q.device), dt, n_steps, scheme, apply_bc)
-        else:
-            q = self._host_rk(q, dt, n_steps, scheme, apply_bc)
+        self.plan(q.device).step(q, self._param_vector(q.device), dt, n_steps, scheme, apply_bc)
         if host:
             if out is None:
                 out = torch.empty(q.shape, dtype=torch.float32, pin_memory=True)
             out.copy_(q, non_blocking=True)
             return self.state_cls(q=out)
         return self.state_cls(q=q)
-
-    def _host_rk(self, q, dt, n_steps, scheme, apply_bc=True):
-        # Tableau schemes not yet fused into qg_step: stage loop over the fused RHS kernel.
-        from .tableaus import rk_tableau
-
-        plan = self.plan(q.device)
-        pv = self._param_vector(q.device)
-        a, b = rk_tableau(scheme)
-        y = _zero_ring(q) if apply_bc else q
-        for _ in range(n_steps):
-            ks = []
-            for s in range(len(b)):
-                ys = y
-                if s:
-                    acc = torch.zeros_like(y)
-                    for j, aj in enumerate(a[s]):
-                        if aj:
-                            acc.add_(ks[j], alpha=aj)
-                    ys = y + dt * acc
-                ks.append(plan.rhs(ys, pv, apply_bc=True))
-            acc = torch.zeros_like(y)
-            for j, bj in enumerate(b):
-                if bj:
-                    acc.add_(ks[j], alpha=bj)
-            y = y + dt * acc
-        return y
 
     def integrate(self, state0, t0: float, t1: float, dt: float, solver=None, saveat=None, **kw):
         """``SomaxModel.integrate`` with constant steps (``core/model.py:53-88``).
@@ -719,8 +696,6 @@ class QGEnsemble:
     def step(self, packed: torch.Tensor, dt: float, n_steps: int = 1, solver="ssprk3", apply_bc=True) -> torch.Tensor:
         """Advance every member in place by ``n_steps`` steps of ``dt``."""
         scheme = _solver_name(solver)
-        if scheme not in ("heun", "ssprk3"):
-            raise ValueError("ensembles step with heun or ssprk3")
         return self.plan.step(packed, self.params(packed.device), dt, n_steps, scheme, apply_bc)
 
     def step_host(self, packed_host: torch.Tensor, out: torch.Tensor, dt: float, n_steps: int = 1,

@@ -95,3 +95,18 @@ def test_gemm_tile_widths(precision, tile, nx, ny, nl):
     assert plan.tuning()["gemm_tile_n"] == tile
     psi = plan.invert(torch.tensor(q, dtype=torch.float32, device="cuda"))
     assert rel(psi, O.invert_pv(o, q)) < (3e-5 if precision == "bf16x3" else 6e-3)
+
+
+@pytest.mark.parametrize("scheme", ["euler", "tsit5"])
+@pytest.mark.parametrize("variant", ["tile32x8", "sweep16"])
+@pytest.mark.parametrize("precision", ["fp32", "bf16x3"])
+def test_butcher_schemes_fused(scheme, variant, precision):
+    """Euler and Tsit5 fused into qg_step (stencil in rhs mode + stage combine) against the
+    oracle's Butcher-form stepping."""
+    for nx, ny, nl in [(30, 24, 3), (17, 13, 1), (64, 40, 5)]:
+        m, o, q = pair(nx, ny, nl, 60 + nl)
+        plan = sg.Plan([m.spec], precision, stencil=variant)
+        pv = m._param_vector(torch.device("cuda"))
+        got = plan.step(torch.tensor(q, dtype=torch.float32, device="cuda"), pv, 1200.0, 3, scheme)
+        assert plan.status() == 0
+        assert rel(got, O.integrate(o, q, 1200.0, 3, scheme)) < RTOL_STEP
