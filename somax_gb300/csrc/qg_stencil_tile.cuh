@@ -89,10 +89,9 @@ __device__ __forceinline__ void tile_issue(const StencilMaps* maps, int q_sel, i
     tma_load_3d(sp, &maps->psi, bar, tx * T::TX - 4, ty * T::TY - 2, 0);
 }
 
-// After the TMA boxes landed: zero the q ring (BC on read) and land, mix psi_hat to layer psi
-// in place on the tile and one ring zeroing the baroclinic psi ring (baroclinic.py:155-158)
-// and land, and lap(q) of the cells one ring beyond the tile (zero on the ghost ring and on
-// land: the interior-only Laplacian).  NL = layers.
+// After the TMA boxes landed: zero the q ring (BC on read), mix psi_hat to layer psi in
+// place zeroing the baroclinic psi ring (baroclinic.py:155-158), and lap(q) of the cells one
+// ring beyond the tile (zero on the ghost ring: the interior-only Laplacian).  NL = layers.
 template <class T, int NL>
 __device__ __forceinline__ void stencil_fix_box(const MemberDev& M, float* sq, float* sp, float* sl, int ty, int tx,
                                                 int apply_bc, bool need_lap) {
@@ -105,34 +104,23 @@ __device__ __forceinline__ void stencil_fix_box(const MemberDev& M, float* sq, f
     for (int l = 0; l < NL; ++l)
 #pragma unroll
         for (int m = 0; m < NL; ++m) C[l][m] = M.Cm2l[l * kMaxLayers + m];
-    // q reads as zero on the ring (BC) and on land: only edge tiles and masked members have
-    // such cells, so interior tiles skip this pass
-    if (edge || M.mask) {
-        for (int c = threadIdx.x; c < BOX; c += NTHREADS) {
-            const int j = j0 + c / BX, i = i0 + c % BX;
-            const bool ring = edge && j >= 0 && j < Ny && i >= 0 && i < Nx && on_ring(j, i, Ny, Nx);
-            if ((apply_bc && ring) || is_land(M, j, i))
-#pragma unroll
-                for (int l = 0; l < NL; ++l) sq[l * BOX + c] = 0.f;
-        }
-    }
-    // psi_hat -> layer psi in place, on the cells the Jacobian reads (the tile and one ring)
-    constexpr int PW = T::TX + 2, PH = T::TY + 2;
-    for (int c = threadIdx.x; c < PW * PH; c += NTHREADS) {
-        const int sy = 1 + c / PW, sx = 3 + c % PW;  // box coordinates
-        const int j = j0 + sy, i = i0 + sx;
-        const int b = sy * BX + sx;
+    for (int c = threadIdx.x; c < BOX; c += NTHREADS) {
+        const int j = j0 + c / BX, i = i0 + c % BX;
         const bool ring = edge && j >= 0 && j < Ny && i >= 0 && i < Nx && on_ring(j, i, Ny, Nx);
-        const bool zero = (ring && !M.barotropic) || is_land(M, j, i);  // psi is zero on land
+        const bool land = is_land(M, j, i);  // q and psi are zero on land
+        if ((apply_bc && ring) || land)
+#pragma unroll
+            for (int l = 0; l < NL; ++l) sq[l * BOX + c] = 0.f;
         float ph[NL];
 #pragma unroll
-        for (int m = 0; m < NL; ++m) ph[m] = sp[m * BOX + b];
+        for (int m = 0; m < NL; ++m) ph[m] = sp[m * BOX + c];
+        const bool zero = (ring && !M.barotropic) || land;
 #pragma unroll
         for (int l = 0; l < NL; ++l) {
             float p = 0.f;
 #pragma unroll
             for (int m = 0; m < NL; ++m) p = fmaf(C[l][m], ph[m], p);
-            sp[l * BOX + b] = zero ? 0.f : p;
+            sp[l * BOX + c] = zero ? 0.f : p;
         }
     }
     if (!need_lap) return;
