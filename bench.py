@@ -106,6 +106,34 @@ def peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "src": "fallback"}
 
 
+def masked_cpu_baseline(threads: int, min_seconds: float = 10.0):
+    """The masked basin (3-layer 512^2, 15 % land) on the host: the float64 oracle with its
+    cached sparse LU per mode (no capacitance step), whole SSP-RK3 steps until at least
+    ``min_seconds``.  Returns (model-days/s, steps, seconds)."""
+    from oracle import masked as OM
+    from oracle import qg as O
+    from somax_gb300 import testcases as tc
+
+    O.set_workers(threads)
+    cfg = tc.CONFIGS["baroclinic3_512"]
+    kw = cfg.model_kwargs()
+    om = O.baroclinic_model(nx=cfg.n, ny=cfg.n, Lx=cfg.L, Ly=cfg.L, f0=kw["f0"], beta=kw["beta"], H=cfg.H,
+                            g_prime=cfg.g_prime, lateral_viscosity=cfg.lateral_viscosity,
+                            bottom_drag=cfg.bottom_drag, wind_amplitude=kw["wind_amplitude"],
+                            biharmonic_viscosity=cfg.biharmonic_viscosity)
+    mask = tc.land_mask(cfg.n, cfg.n, frac=0.15, seed=0)
+    q = tc.initial_pv(cfg, seed=0)
+    q = OM.integrate(om, q, mask, cfg.dt, 1, cfg.scheme)  # warm (factorisations)
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        q = OM.integrate(om, q, mask, cfg.dt, 1, cfg.scheme)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= min_seconds:
+            break
+    return steps * cfg.dt / 86400.0 / el, steps, el
+
+
 def cpu_baseline(cfg, threads: int, min_seconds: float = 10.0, chunk: int = 12):
     """Float32 oracle restatement of the RK step loop on the host cores: whole chunks of
     ``chunk`` steps until at least ``min_seconds`` have elapsed.  Returns (model-days/s,
@@ -155,6 +183,11 @@ def describe(name):
 
     if name == "ensemble256":
         return ENSEMBLE_METRIC, "member-days/s", ENSEMBLE_DESC + ", 72 steps = 1 model day per bench step"
+    if name == "masked3_512":
+        return ("QG model-days/sec per GB300 (3-layer 512^2 masked basin, SSP-RK3 dt=1200 s)", UNIT,
+                "masked3_512: 3-layer 512x512 double gyre (Lx=Ly=5120 km) with a seeded coastline (15 % of the "
+                "T-cells land, ring land), one FP32 refinement sweep, FP64 capacitance correction, ssprk3 "
+                "dt=1200s, 72 steps = 1 model day per bench step")
     cfg = tc.CONFIGS[name]
     metric = METRIC if name == "baroclinic3_128" else f"QG model-days/sec per GB300 ({name})"
     steps = int(round(86400.0 / cfg.dt))
@@ -177,6 +210,9 @@ def run_reference(args):
     for k in range(args.warmup + args.steps):
         if args.config == "ensemble256":
             v, desc = ensemble_cpu_rate(threads, per_step_s if k >= args.warmup else 1.0)
+        elif args.config == "masked3_512":
+            v, n, el = masked_cpu_baseline(threads, per_step_s if k >= args.warmup else 1.0)
+            desc = f"{n} ssprk3 steps of masked3_512 in float64 with cached sparse LU ({el:.1f} s)"
         else:
             cfg = tc.CONFIGS[args.config]
             v, n, el = cpu_baseline(cfg, threads, per_step_s if k >= args.warmup else 1.0)
@@ -229,12 +265,18 @@ class Workload:
             self.dt, self.scheme = cfgs[0].dt, cfgs[0].scheme
             self.model = None
         else:
-            cfg = tc.CONFIGS[name]
+            masked = name == "masked3_512"
+            cfg = tc.CONFIGS["baroclinic3_512" if masked else name]
+            mask = tc.land_mask(cfg.n, cfg.n, frac=0.15, seed=0) if masked else None
             self.model = sg.BaroclinicQG.create(**cfg.model_kwargs(), precision=precision, persistent=persistent,
-                                                stencil=stencil, gemm_tile=gemm_tile)
+                                                stencil=stencil, gemm_tile=gemm_tile, mask=mask,
+                                                refine=1 if masked else 0)
             self.plan = self.model.plan(dev)
             self.params = self.model._param_vector(dev)
-            self.q0 = tc.initial_pv(cfg, seed=seed).astype(np.float32)
+            q0 = tc.initial_pv(cfg, seed=seed)
+            if masked:
+                q0 = np.where(mask == 0, 0.0, q0)
+            self.q0 = q0.astype(np.float32)
             self.members = [(cfg.n + 2, cfg.nl)]
             self.dt, self.scheme = cfg.dt, cfg.scheme
             self.ens = None
@@ -436,7 +478,10 @@ def main():
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = len(os.sched_getaffinity(0))
-        if W.model is not None:
+        if args.config == "masked3_512":
+            v, n, el = masked_cpu_baseline(threads, 10.0)
+            sample = f"{n} ssprk3 steps of masked3_512, float64 NumPy/SciPy restatement with cached sparse LU ({el:.1f} s)"
+        elif W.model is not None:
             cfg = tc.CONFIGS[args.config]
             v, n, el = cpu_baseline(cfg, threads, 10.0)
             sample = f"{n} {cfg.scheme} steps of {cfg.name}, float32 NumPy/SciPy restatement ({el:.1f} s)"

@@ -61,16 +61,34 @@ def _operator(Ny: int, Nx: int, dx: float, dy: float, lam: float) -> sp.csr_matr
             - lam * sp.identity(Ny * Nx)).tocsr()
 
 
+_LU_CACHE: dict = {}
+
+
+def _factor(mask: np.ndarray, dx: float, dy: float, lam: float):
+    """Sparse LU of the masked operator (B rows replaced by the identity), cached per mask,
+    spacing and lambda (a time loop reuses it)."""
+    m = np.ascontiguousarray(mask, dtype=np.uint8)
+    key = (m.shape, hash(m.tobytes()), float(dx), float(dy), float(lam))
+    if key not in _LU_CACHE:
+        Ny, Nx = m.shape
+        A = _operator(Ny, Nx, dx, dy, lam).tolil()
+        B = boundary_points(m)
+        for k in B:
+            A.rows[k] = [k]
+            A.data[k] = [1.0]
+        if len(_LU_CACHE) > 16:
+            _LU_CACHE.clear()
+        _LU_CACHE[key] = (spla.splu(A.tocsc()), B)
+    return _LU_CACHE[key]
+
+
 def helmholtz_masked(rhs: np.ndarray, dx: float, dy: float, lam: float, mask: np.ndarray) -> np.ndarray:
     """Direct sparse solve: (lap - lam) psi = rhs off B, psi = 0 on B (float64)."""
     Ny, Nx = rhs.shape
-    A = _operator(Ny, Nx, dx, dy, lam).tolil()
+    lu, B = _factor(mask, dx, dy, lam)
     b = np.asarray(rhs, np.float64).reshape(-1).copy()
-    for k in boundary_points(mask):
-        A.rows[k] = [k]
-        A.data[k] = [1.0]
-        b[k] = 0.0
-    return spla.spsolve(A.tocsc(), b).reshape(Ny, Nx)
+    b[B] = 0.0
+    return lu.solve(b).reshape(Ny, Nx)
 
 
 def capacitance_matrix(Ny: int, Nx: int, dx: float, dy: float, lam: float, B: np.ndarray) -> np.ndarray:
