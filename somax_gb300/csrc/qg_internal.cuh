@@ -47,8 +47,11 @@ struct MemberDev {
 };
 
 // Interior land cell of a member (false without a mask).
+__host__ __device__ __forceinline__ bool is_land(const uint8_t* mask, int Ny, int Nx, int j, int i) {
+    return mask && j > 0 && i > 0 && j < Ny - 1 && i < Nx - 1 && mask[(int64_t)j * Nx + i] == 0;
+}
 __host__ __device__ __forceinline__ bool is_land(const MemberDev& M, int j, int i) {
-    return M.mask && j > 0 && i > 0 && j < M.Ny - 1 && i < M.Nx - 1 && M.mask[(int64_t)j * M.Nx + i] == 0;
+    return is_land(M.mask, M.Ny, M.Nx, j, i);
 }
 
 // Stencil work item: one 2-D tile of one member (all layers).

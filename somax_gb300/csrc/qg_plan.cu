@@ -668,6 +668,13 @@ cudaError_t autotune_stencil(qg_plan* p) {
     cudaError_t e = cudaEventCreate(&e0);
     if (!e) e = cudaEventCreate(&e1);
     if (e) return e;
+    // every parameter non-zero while timing, so that every term (the biharmonic's lap(q) pass
+    // included) runs as it will in the integration
+    {
+        std::vector<float> ones((size_t)p->n_members * QG_NPARAMS, 1.f);
+        e = cudaMemcpy(p->params, ones.data(), ones.size() * sizeof(float), cudaMemcpyHostToDevice);
+        if (e) return e;
+    }
     const int tile_default = p->st_large;
     for (int v = 0; v < QG_STENCIL_VARIANTS && !e; ++v) {
         if (v < 2) {
@@ -711,6 +718,7 @@ cudaError_t autotune_stencil(qg_plan* p) {
     select_tile(p, tile);
     select_sweep(p, best >= 2 ? best - 2 : -1);
     e = cudaMemsetAsync(p->S2, 0, sizeof(float) * p->xplane, s);
+    if (!e) e = cudaMemsetAsync(p->params, 0, sizeof(float) * p->n_members * QG_NPARAMS, s);
     if (!e) e = cudaMemsetAsync(p->XA, 0, sizeof(float) * p->xplane, s);
     if (!e) e = cudaStreamSynchronize(s);
     return e;

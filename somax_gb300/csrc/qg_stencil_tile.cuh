@@ -99,6 +99,7 @@ __device__ __forceinline__ void stencil_fix_box(const MemberDev& M, float* sq, f
     const int Ny = M.Ny, Nx = M.Nx;
     const int j0 = ty * T::TY - 2, i0 = tx * T::TX - 4;
     const bool edge = (j0 <= 0) || (i0 <= 0) || (j0 + T::BY >= Ny) || (i0 + BX >= Nx);
+    const uint8_t* mask = M.mask;  // in a register: the loops below store to shared memory
     float C[NL][NL];
 #pragma unroll
     for (int l = 0; l < NL; ++l)
@@ -107,7 +108,7 @@ __device__ __forceinline__ void stencil_fix_box(const MemberDev& M, float* sq, f
     for (int c = threadIdx.x; c < BOX; c += NTHREADS) {
         const int j = j0 + c / BX, i = i0 + c % BX;
         const bool ring = edge && j >= 0 && j < Ny && i >= 0 && i < Nx && on_ring(j, i, Ny, Nx);
-        const bool land = is_land(M, j, i);  // q and psi are zero on land
+        const bool land = is_land(mask, Ny, Nx, j, i);  // q and psi are zero on land
         if ((apply_bc && ring) || land)
 #pragma unroll
             for (int l = 0; l < NL; ++l) sq[l * BOX + c] = 0.f;
@@ -130,7 +131,7 @@ __device__ __forceinline__ void stencil_fix_box(const MemberDev& M, float* sq, f
     for (int c = threadIdx.x; c < LW * LH; c += NTHREADS) {
         const int sy = 1 + c / LW, sx = 3 + c % LW;  // box coordinates
         const int j = j0 + sy, i = i0 + sx;
-        const bool interior = j > 0 && i > 0 && j < Ny - 1 && i < Nx - 1 && !is_land(M, j, i);
+        const bool interior = j > 0 && i > 0 && j < Ny - 1 && i < Nx - 1 && !is_land(mask, Ny, Nx, j, i);
         const int b = sy * BX + sx;
 #pragma unroll
         for (int l = 0; l < NL; ++l) {
@@ -148,7 +149,13 @@ template <class T, int NL>
 __device__ __forceinline__ bool stencil_compute(const StencilArgs& a, const MemberDev& M, const StencilTile& t,
                                                 const float* sq, const float* sp, const float* sl) {
     constexpr int BX = T::BX, BOX = T::BOX, R = T::PER_THREAD;
-    const int Ny = M.Ny, Nx = M.Nx;
+    // member constants in registers: the stores below go through generic pointers, after which
+    // the compiler would otherwise reload every field of M from shared memory
+    const int Ny = M.Ny, Nx = M.Nx, Px = M.Px;
+    const uint8_t* mask = M.mask;
+    const float i12 = M.inv_12dxdy, b12 = M.beta_12dx, invH0 = M.invH0;
+    const int64_t off_x = M.off_x, off_c = M.off_state;
+    const int64_t lsx = (int64_t)Ny * Px, lsc = (int64_t)Ny * Nx;
     const float* P = a.params + (int64_t)t.member * QG_NPARAMS;
     const float nu = P[QG_P_NU], kappa = P[QG_P_KAPPA], tau0 = P[QG_P_TAU0], nu4 = P[QG_P_NU4];
     const float idx2 = M.inv_dx2, idy2 = M.inv_dy2;
@@ -164,7 +171,7 @@ __device__ __forceinline__ bool stencil_compute(const StencilArgs& a, const Memb
         const bool in = j < Ny && i < Nx;
         Fj[r] = in ? M.F[j] : 0.f;
 #pragma unroll
-        for (int l = 0; l < NL; ++l) y0r[r][l] = (step && in) ? a.y0[xrow_idx(M, l, j, i)] : 0.f;
+        for (int l = 0; l < NL; ++l) y0r[r][l] = (step && in) ? a.y0[off_x + l * lsx + (int64_t)j * Px + i] : 0.f;
     }
     bool bad = false;
 #pragma unroll
@@ -173,9 +180,10 @@ __device__ __forceinline__ bool stencil_compute(const StencilArgs& a, const Memb
         const int j = t.ty * T::TY + ly;
         if (j >= Ny || i >= Nx) continue;
         const bool ring = on_ring(j, i, Ny, Nx);
-        const bool land = is_land(M, j, i);  // no dynamics on land
+        const bool land = is_land(mask, Ny, Nx, j, i);  // no dynamics on land
         const int s0 = (ly + 2) * BX + (lx + 4);  // box index of the cell
-        const float wind = tau0 * Fj[r] * M.invH0;
+        const float wind = tau0 * Fj[r] * invH0;
+        const int64_t xo = off_x + (int64_t)j * Px + i, co = off_c + (int64_t)j * Nx + i;
         float d[NL];
 #pragma unroll
         for (int l = 0; l < NL; ++l) {
@@ -192,8 +200,8 @@ __device__ __forceinline__ bool stencil_compute(const StencilArgs& a, const Memb
             const float jpp = (fE - fW) * (gN - gS) - (fN - fS) * (gE - gW);
             const float jpx = fE * (gNE - gSE) - fW * (gNW - gSW) - fN * (gNE - gNW) + fS * (gSE - gSW);
             const float jxp = gN * (fNE - fNW) - gS * (fSE - fSW) - gE * (fNE - fSE) + gW * (fNW - fSW);
-            const float Jq = (jpp + jpx + jxp) * M.inv_12dxdy;
-            const float Jb = (4.f * (fE - fW) + (fNE - fNW) + (fSE - fSW)) * M.beta_12dx;
+            const float Jq = (jpp + jpx + jxp) * i12;
+            const float Jb = (4.f * (fE - fW) + (fNE - fNW) + (fSE - fSW)) * b12;
             float v = -(Jq + Jb);
             if (l == 0) v += wind;
             if (l == NL - 1) {
@@ -215,7 +223,7 @@ __device__ __forceinline__ bool stencil_compute(const StencilArgs& a, const Memb
 
         if (!step) {
 #pragma unroll
-            for (int l = 0; l < NL; ++l) a.dq[caller_idx(M, l, j, i)] = d[l];
+            for (int l = 0; l < NL; ++l) a.dq[co + l * lsc] = d[l];
             continue;
         }
         float yn[NL];
@@ -229,7 +237,7 @@ __device__ __forceinline__ bool stencil_compute(const StencilArgs& a, const Memb
                 yn[l] = a.a * y0r[r][l] + a.b * (sq[l * BOX + s0] + a.dt * d[l]);
             }
             bad |= !isfinite(yn[l]);
-            a.y_next[xrow_idx(M, l, j, i)] = yn[l];
+            a.y_next[xo + l * lsx] = yn[l];
         }
         if (a.xa) {
 #pragma unroll
@@ -238,8 +246,8 @@ __device__ __forceinline__ bool stencil_compute(const StencilArgs& a, const Memb
                 if (!ring && !land)
 #pragma unroll
                     for (int l = 0; l < NL; ++l) s = fmaf(M.Cl2m[m * kMaxLayers + l], yn[l], s);
-                store_plane(a.xa, a.xa_fmt, a.xplane, xrow_idx(M, m, j, i), s);
-                if (a.xq) a.xq[xrow_idx(M, m, j, i)] = s;
+                store_plane(a.xa, a.xa_fmt, a.xplane, xo + m * lsx, s);
+                if (a.xq) a.xq[xo + m * lsx] = s;
             }
         }
     }

@@ -89,11 +89,10 @@ __device__ __forceinline__ void ingest(Win<NL>& w, const float (&cm)[NL][NL], co
 
 // Output row j = r - 2 (window slot J = j & 3).  Returns true if a non-finite value was made.
 template <int NL, int J>
-__device__ __forceinline__ bool output(const StencilArgs& a, const MemberDev& M, Win<NL>& w, const float (&cl)[NL][NL],
+__device__ __forceinline__ bool output(const StencilArgs& a, int Ny, int Nx, Win<NL>& w, const float (&cl)[NL][NL],
                                        const Coef& c, int j, int x, bool write, float Fj, int64_t xo, int64_t co,
                                        int64_t lstride_x, int64_t lstride_c, bool step, bool need_y0) {
     constexpr int N = (J + 1) & 3, S = (J + 3) & 3;  // rows j + 1 and j - 1
-    const int Ny = M.Ny, Nx = M.Nx;
     const bool ring = j == 0 || j == Ny - 1 || x == 0 || x == Nx - 1;
     const bool land = w.land[J];  // no dynamics on land
     const float wind = c.tau0 * Fj * c.invH0;
@@ -198,6 +197,11 @@ __device__ __forceinline__ bool sweep(const StencilArgs& a, const MemberDev& M, 
         }
     const bool zero_psi_ring = !M.barotropic;
     const bool apply_bc = a.apply_bc != 0;
+    // member constants in registers (M is in global memory; stores through generic pointers
+    // would otherwise force reloads)
+    const uint8_t* mask = M.mask;
+    const float* Fp = M.F;
+    const int64_t off_x = M.off_x, off_c = M.off_state;
     const int64_t lsx = (int64_t)Ny * Px, lsc = (int64_t)Ny * Nx;
     const float* qb = a.qin + M.off_x;
     const float* hb = a.psi_hat + M.off_x;
@@ -212,14 +216,14 @@ __device__ __forceinline__ bool sweep(const StencilArgs& a, const MemberDev& M, 
 #define QG_SWEEP_ROW(K)                                                                                 \
         {                                                                                               \
             const int r = rb + K;                                                                       \
-            ingest<NL, (K) & 1, K>(w, cm, c, r, Ny, x, Nx, apply_bc, zero_psi_ring, M.mask);            \
+            ingest<NL, (K) & 1, K>(w, cm, c, r, Ny, x, Nx, apply_bc, zero_psi_ring, mask);              \
             fetch<NL, (K) & 1>(w, qb, hb, lsx, r + 2, Ny, x, Nx, Px);                                   \
             const int j = r - 2;                                                                        \
             if (j >= jb && j < je) {                                                                    \
-                const float Fj = M.F[j];                                                                \
-                bad |= output<NL, ((K) + 2) & 3>(a, M, w, cl, c, j, x, out_lane, Fj,                    \
-                                                 M.off_x + (int64_t)j * Px + x,                         \
-                                                 M.off_state + (int64_t)j * Nx + x, lsx, lsc, step,    \
+                const float Fj = Fp[j];                                                                 \
+                bad |= output<NL, ((K) + 2) & 3>(a, Ny, Nx, w, cl, c, j, x, out_lane, Fj,               \
+                                                 off_x + (int64_t)j * Px + x,                           \
+                                                 off_c + (int64_t)j * Nx + x, lsx, lsc, step,          \
                                                  need_y0);                                              \
             }                                                                                           \
         }
