@@ -20,8 +20,8 @@ struct PassGeom {
 
 __device__ __forceinline__ PassGeom pass_geom(const MemberDev& M, int pass, const void* A, void* C) {
     PassGeom g;
-    const bool xin = (pass == G1_FWD_X || pass == G4_INV_X);  // A in x-row planes
-    const bool xout = (pass == G3_INV_Y || pass == G4_INV_X); // C in x-row planes
+    const bool xin = pass_xin(pass);  // A in x-row planes, C (transposed) in y-row planes
+    const bool xout = !xin;
     g.Mb = xin ? M.Ny : M.Nx;
     g.K = xin ? M.Nx : M.Ny;
     g.Nn = g.K;
@@ -47,11 +47,10 @@ __global__ void __launch_bounds__(NT) k_gemm_simt(GemmArgs ga) {
     const int Mtot = nl * g.Mb;
     const int m0 = t.mt * BM, n0 = t.nt * BN;
     const int tid = threadIdx.x;
-    constexpr bool kTrans = (PASS == G1_FWD_X || PASS == G3_INV_Y);
-    // Interleaved ownership: rows mr + 16 i, columns nc + 16 j.  For transposed stores the
-    // row index runs along the warp so that the column-major writes coalesce.
-    const int mr = kTrans ? (tid & 15) : (tid >> 4);
-    const int nc = kTrans ? (tid >> 4) : (tid & 15);
+    // Interleaved ownership: rows mr + 16 i, columns nc + 16 j; the row index runs along the
+    // warp so that the transposed (column-major) stores coalesce.
+    const int mr = tid & 15;
+    const int nc = tid >> 4;
 
     float acc[4][4];
 #pragma unroll
@@ -103,14 +102,10 @@ __global__ void __launch_bounds__(NT) k_gemm_simt(GemmArgs ga) {
             const int n = n0 + nc + 16 * j;
             if (n >= g.Nn) continue;
             float v = acc[i][j];
-            if (kTrans) {
-                g.C[((int64_t)l * g.Nn + n) * g.ldo + r] = v;
-            } else {
-                const int64_t o = (int64_t)m * g.ldo + n;
-                if (PASS == G2_FWD_Y) v = v / (M.ex[r] + M.ey[n] - M.lam[l]);
-                if (PASS == G4_INV_X && ga.accumulate) v += g.C[o];
-                g.C[o] = v;
-            }
+            const int64_t o = ((int64_t)l * g.Nn + n) * g.ldo + r;
+            if (PASS == G2_FWD_Y) v = v / (M.ex[r] + M.ey[n] - M.lam[l]);
+            if (PASS == G4_INV_Y && ga.accumulate) v += g.C[o];
+            g.C[o] = v;
         }
     }
 }
@@ -121,8 +116,8 @@ cudaError_t launch_gemm_simt(const GemmArgs& g, int ntiles, cudaStream_t s, bool
     switch (g.pass) {
         case G1_FWD_X: return launch_k(k_gemm_simt<G1_FWD_X>, ntiles, NT, 0, s, pdl, g);
         case G2_FWD_Y: return launch_k(k_gemm_simt<G2_FWD_Y>, ntiles, NT, 0, s, pdl, g);
-        case G3_INV_Y: return launch_k(k_gemm_simt<G3_INV_Y>, ntiles, NT, 0, s, pdl, g);
-        case G4_INV_X: return launch_k(k_gemm_simt<G4_INV_X>, ntiles, NT, 0, s, pdl, g);
+        case G3_INV_X: return launch_k(k_gemm_simt<G3_INV_X>, ntiles, NT, 0, s, pdl, g);
+        case G4_INV_Y: return launch_k(k_gemm_simt<G4_INV_Y>, ntiles, NT, 0, s, pdl, g);
         default: return cudaErrorInvalidValue;
     }
 }

@@ -43,7 +43,7 @@ cudaError_t gemm_tc_encode(const MemberDev& M, int pass, const void* a_plane, in
                            void* out) {
     TcMaps tm;
     std::memset(&tm, 0, sizeof(tm));
-    const bool xin = (pass == G1_FWD_X || pass == G4_INV_X);
+    const bool xin = pass_xin(pass);
     const int Mb = xin ? M.Ny : M.Nx, K = xin ? M.Nx : M.Ny, pitch = xin ? M.Px : M.Py;
     const int64_t off = xin ? M.off_x : M.off_y;
     const int es = prec == QG_DST_BF16X3 ? 2 : 4;

@@ -65,13 +65,18 @@ struct GemmTile {
 };
 
 // The four DST-I GEMM passes of the inversion, psi_hat = S_y (S_y q S_x ./ L) S_x.
-// Each is C = A * S with A row-major (rows = (layer, r), K contiguous) and S symmetric.
+// Each is C = A * S with A row-major (rows = (layer, r), K contiguous) and S symmetric, stored
+// transposed (C^T = S A^T), so the contracted axis alternates x, y, x, y and the last pass
+// leaves psi_hat in the x-row layout of q.  Every store is column-major in C: the lanes of a
+// warp hold consecutive rows of the accumulator and write consecutive addresses.
 enum GemmPass : int {
-    G1_FWD_X = 0,  // A = q_modal rows (l, y), K = x  -> T1t[l][kx][y]   (transposed store)
-    G2_FWD_Y = 1,  // A = T1t rows (l, kx), K = y     -> U[l][kx][ky] / (ex+ey-lam)
-    G3_INV_Y = 2,  // A = U rows (l, kx), K = ky      -> Vt[l][y][kx]   (transposed store)
-    G4_INV_X = 3,  // A = Vt rows (l, y), K = kx      -> psi_hat[l][y][x]
+    G1_FWD_X = 0,  // A = q_modal rows (l, y), K = x  -> T1[l][kx][y]              (y-row plane)
+    G2_FWD_Y = 1,  // A = T1 rows (l, kx), K = y      -> U[l][ky][kx] / (ex+ey-lam) (x-row plane)
+    G3_INV_X = 2,  // A = U rows (l, ky), K = kx      -> V[l][x][ky]               (y-row plane)
+    G4_INV_Y = 3,  // A = V rows (l, x), K = ky       -> psi_hat[l][y][x]          (x-row plane)
 };
+// A of the pass is an x-row plane (rows (l, y), K = x); its output is then a y-row plane.
+__host__ __device__ constexpr bool pass_xin(int pass) { return pass == G1_FWD_X || pass == G3_INV_X; }
 
 // Operand / output formats of the internal planes.
 enum PlaneFmt : int {

@@ -90,11 +90,11 @@ struct Shared {
 template <int PREC, int PASS>
 __device__ void gemm_phase(const PersistArgs& a, uint8_t* smem, Shared& sh, uint32_t tmem, Counters& c) {
     using C = TcCfg<PREC>;
-    constexpr bool xin = (PASS == G1_FWD_X || PASS == G4_INV_X);
+    constexpr bool xin = pass_xin(PASS);
     const GemmTile* tiles = xin ? a.gx : a.gy;
     const int n = xin ? a.n_gx : a.n_gy;
-    void* Cv = PASS == G1_FWD_X ? a.YA : PASS == G2_FWD_Y ? a.YB : PASS == G3_INV_Y ? a.XB : (void*)a.XC;
-    const int c_fmt = PASS == G4_INV_X ? FMT_F32 : a.op_fmt;
+    void* Cv = PASS == G1_FWD_X ? a.YA : PASS == G2_FWD_Y ? a.XB : PASS == G3_INV_X ? a.YB : (void*)a.XC;
+    const int c_fmt = PASS == G4_INV_Y ? FMT_F32 : a.op_fmt;
     const TcMaps* maps = static_cast<const TcMaps*>(a.tc_maps);
     volatile int* abort = &sh.abort;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -151,10 +151,9 @@ __device__ void gemm_phase(const PersistArgs& a, uint8_t* smem, Shared& sh, uint
             const bool have = mbar_wait(&sh.tfull[buf], use & 1, abort);
             if (!have) break;
             tc_fence_after();
-            float* stage = reinterpret_cast<float*>(smem + C::STAGES * tc_stage_bytes<PREC>()) + (warp - 4) * TC_STAGE_FLOATS;
-            tc_epilogue<PASS>(M, g, Cv, c_fmt, PASS == G4_INV_X ? a.g4_accumulate : 0, tl.mt * TC_BM,
+            tc_epilogue<PASS>(M, g, Cv, c_fmt, PASS == G4_INV_Y ? a.g4_accumulate : 0, tl.mt * TC_BM,
                               tl.nt * a.tile_n, tc_tile_width(g.Nn, tl.nt, a.tile_n), tmem + buf * TC_TMEM_BUF,
-                              warp & 3, lane, true, stage);
+                              warp & 3, lane, true);
             tc_fence_before();
             mbar_arrive(&sh.tempty[buf]);
             ++c.epi_tiles;
@@ -331,9 +330,9 @@ __global__ void __launch_bounds__(PT, 1) k_persistent(PersistArgs a) {
             if (!grid_sync(a.bar_count, a.bar_gen, a.flags, abort)) goto done;
             gemm_phase<PREC, G2_FWD_Y>(a, smem, sh, tmem, c);
             if (!grid_sync(a.bar_count, a.bar_gen, a.flags, abort)) goto done;
-            gemm_phase<PREC, G3_INV_Y>(a, smem, sh, tmem, c);
+            gemm_phase<PREC, G3_INV_X>(a, smem, sh, tmem, c);
             if (!grid_sync(a.bar_count, a.bar_gen, a.flags, abort)) goto done;
-            gemm_phase<PREC, G4_INV_X>(a, smem, sh, tmem, c);
+            gemm_phase<PREC, G4_INV_Y>(a, smem, sh, tmem, c);
             if (!grid_sync(a.bar_count, a.bar_gen, a.flags, abort)) goto done;
             stencil_phase<T>(a, k, smem, sh, c);
             if (!grid_sync(a.bar_count, a.bar_gen, a.flags, abort)) goto done;
@@ -368,8 +367,7 @@ size_t stencil_layout(int max_nl, PersistArgs* a) {
 
 size_t persistent_smem_bytes(int precision, int max_nl, int large, PersistArgs* a) {
     const size_t gemm = (precision == QG_DST_TF32 ? (size_t)TcCfg<QG_DST_TF32>::STAGES * tc_stage_bytes<QG_DST_TF32>()
-                                                  : (size_t)TcCfg<QG_DST_BF16X3>::STAGES * tc_stage_bytes<QG_DST_BF16X3>()) +
-                        TC_EPI_SMEM;
+                                                  : (size_t)TcCfg<QG_DST_BF16X3>::STAGES * tc_stage_bytes<QG_DST_BF16X3>());
     const size_t sten = large ? stencil_layout<st::TileL>(max_nl, a) : stencil_layout<st::TileS>(max_nl, a);
     return std::max(gemm, sten) + 1024;
 }
@@ -404,7 +402,7 @@ cudaError_t launch_stencil_mt(const StencilArgs& sa, int n_st, int grid, int max
 
 template <int PREC>
 size_t gemm_mt_smem() {
-    return (size_t)TcCfg<PREC>::STAGES * tc_stage_bytes<PREC>() + TC_EPI_SMEM + 1024;
+    return (size_t)TcCfg<PREC>::STAGES * tc_stage_bytes<PREC>() + 1024;
 }
 
 cudaError_t launch_gemm_mt(const PersistArgs& a, int pass, int grid, int precision, cudaStream_t s, bool pdl) {
@@ -412,8 +410,8 @@ cudaError_t launch_gemm_mt(const PersistArgs& a, int pass, int grid, int precisi
     switch (pass) {                                                                                                \
         case G1_FWD_X: return launch_k(k_gemm_mt<P, G1_FWD_X>, grid, PT, gemm_mt_smem<P>(), s, pdl, a);          \
         case G2_FWD_Y: return launch_k(k_gemm_mt<P, G2_FWD_Y>, grid, PT, gemm_mt_smem<P>(), s, pdl, a);          \
-        case G3_INV_Y: return launch_k(k_gemm_mt<P, G3_INV_Y>, grid, PT, gemm_mt_smem<P>(), s, pdl, a);          \
-        case G4_INV_X: return launch_k(k_gemm_mt<P, G4_INV_X>, grid, PT, gemm_mt_smem<P>(), s, pdl, a);          \
+        case G3_INV_X: return launch_k(k_gemm_mt<P, G3_INV_X>, grid, PT, gemm_mt_smem<P>(), s, pdl, a);          \
+        case G4_INV_Y: return launch_k(k_gemm_mt<P, G4_INV_Y>, grid, PT, gemm_mt_smem<P>(), s, pdl, a);          \
         default: return cudaErrorInvalidValue;                                                                     \
     }
     if (precision == QG_DST_TF32) { QG_GMT(QG_DST_TF32) }
@@ -430,12 +428,12 @@ cudaError_t persistent_init() {
     QG_MTATTR(k_stencil_mt<st::TileL>, stencil_mt_smem_bytes(kMaxLayers, 1, nullptr, nullptr, nullptr))
     QG_MTATTR((k_gemm_mt<QG_DST_TF32, G1_FWD_X>), gemm_mt_smem<QG_DST_TF32>())
     QG_MTATTR((k_gemm_mt<QG_DST_TF32, G2_FWD_Y>), gemm_mt_smem<QG_DST_TF32>())
-    QG_MTATTR((k_gemm_mt<QG_DST_TF32, G3_INV_Y>), gemm_mt_smem<QG_DST_TF32>())
-    QG_MTATTR((k_gemm_mt<QG_DST_TF32, G4_INV_X>), gemm_mt_smem<QG_DST_TF32>())
+    QG_MTATTR((k_gemm_mt<QG_DST_TF32, G3_INV_X>), gemm_mt_smem<QG_DST_TF32>())
+    QG_MTATTR((k_gemm_mt<QG_DST_TF32, G4_INV_Y>), gemm_mt_smem<QG_DST_TF32>())
     QG_MTATTR((k_gemm_mt<QG_DST_BF16X3, G1_FWD_X>), gemm_mt_smem<QG_DST_BF16X3>())
     QG_MTATTR((k_gemm_mt<QG_DST_BF16X3, G2_FWD_Y>), gemm_mt_smem<QG_DST_BF16X3>())
-    QG_MTATTR((k_gemm_mt<QG_DST_BF16X3, G3_INV_Y>), gemm_mt_smem<QG_DST_BF16X3>())
-    QG_MTATTR((k_gemm_mt<QG_DST_BF16X3, G4_INV_X>), gemm_mt_smem<QG_DST_BF16X3>())
+    QG_MTATTR((k_gemm_mt<QG_DST_BF16X3, G3_INV_X>), gemm_mt_smem<QG_DST_BF16X3>())
+    QG_MTATTR((k_gemm_mt<QG_DST_BF16X3, G4_INV_Y>), gemm_mt_smem<QG_DST_BF16X3>())
 #undef QG_MTATTR
 #define QG_PATTR(P, T, L)                                                                                      \
     if (!e)                                                                                                    \

@@ -236,8 +236,9 @@ struct qg_plan {
     int n_gx_v[5] = {}, n_gy_v[5] = {};
     int n_bn = 1, bn_sel = 0;
     float tune_gemm_ms[5] = {-1.f, -1.f, -1.f, -1.f, -1.f};
-    // device memory: x-row planes XA (modal operand), XB (V^T), XC (psi_hat), XQ (FP32 modal
-    // rhs for refinement), S0 (state), S1/S2 (stage inputs); y-row planes YA (T1^T), YB (U)
+    // device memory: x-row planes XA (modal operand), XB (U, the divided spectrum), XC
+    // (psi_hat), XQ (FP32 modal rhs for refinement), S0 (state), S1/S2 (stage inputs); y-row
+    // planes YA (T1) and YB (V), the outputs of the x-contracting passes
     std::vector<void*> allocs;
     float *XA = nullptr, *XB = nullptr, *XC = nullptr, *XQ = nullptr, *YA = nullptr, *YB = nullptr;
     float *S0 = nullptr, *S1 = nullptr, *S2 = nullptr;
@@ -341,7 +342,7 @@ GemmArgs gemm_args(qg_plan* p, int pass, const void* A, void* C, int a_fmt, int 
     g.members = p->md;
     g.xplane = p->xplane;
     g.yplane = p->yplane;
-    g.tiles = (pass == G1_FWD_X || pass == G4_INV_X) ? p->gx_tiles : p->gy_tiles;
+    g.tiles = pass_xin(pass) ? p->gx_tiles : p->gy_tiles;
     g.pass = pass;
     g.A = A;
     g.C = C;
@@ -354,7 +355,7 @@ GemmArgs gemm_args(qg_plan* p, int pass, const void* A, void* C, int a_fmt, int 
 }
 
 cudaError_t run_gemm(qg_plan* p, const GemmArgs& g, cudaStream_t s) {
-    const int nt = (g.pass == G1_FWD_X || g.pass == G4_INV_X) ? p->n_gx : p->n_gy;
+    const int nt = pass_xin(g.pass) ? p->n_gx : p->n_gy;
     return timed(p, QG_K_GEMM, s, [&] {
         if (p->opts.dst_precision == QG_DST_FP32) return launch_gemm_simt(g, nt, s, use_pdl(p));
         PersistArgs a = p->pa;
@@ -370,9 +371,9 @@ cudaError_t run_dst_solve(qg_plan* p, cudaStream_t s) {
     cudaError_t e;
     // the last pass writes FP32 psi_hat; intermediate planes use the operand format
     if ((e = run_gemm(p, gemm_args(p, G1_FWD_X, p->XA, p->YA, f, f, 0), s))) return e;
-    if ((e = run_gemm(p, gemm_args(p, G2_FWD_Y, p->YA, p->YB, f, f, 0), s))) return e;
-    if ((e = run_gemm(p, gemm_args(p, G3_INV_Y, p->YB, p->XB, f, f, 0), s))) return e;
-    if ((e = run_gemm(p, gemm_args(p, G4_INV_X, p->XB, p->XC, f, FMT_F32, 0), s))) return e;
+    if ((e = run_gemm(p, gemm_args(p, G2_FWD_Y, p->YA, p->XB, f, f, 0), s))) return e;
+    if ((e = run_gemm(p, gemm_args(p, G3_INV_X, p->XB, p->YB, f, f, 0), s))) return e;
+    if ((e = run_gemm(p, gemm_args(p, G4_INV_Y, p->YB, p->XC, f, FMT_F32, 0), s))) return e;
     for (int r = 0; r < p->opts.refine_sweeps; ++r) {
         e = timed(p, QG_K_OTHER, s, [&] {
             return launch_residual(p->md, p->st_tiles, p->n_st, p->st_large, p->XQ, p->XC, p->XA, f, p->xplane, s,
@@ -380,9 +381,9 @@ cudaError_t run_dst_solve(qg_plan* p, cudaStream_t s) {
         });
         if (e) return e;
         if ((e = run_gemm(p, gemm_args(p, G1_FWD_X, p->XA, p->YA, f, f, 0), s))) return e;
-        if ((e = run_gemm(p, gemm_args(p, G2_FWD_Y, p->YA, p->YB, f, f, 0), s))) return e;
-        if ((e = run_gemm(p, gemm_args(p, G3_INV_Y, p->YB, p->XB, f, f, 0), s))) return e;
-        if ((e = run_gemm(p, gemm_args(p, G4_INV_X, p->XB, p->XC, f, FMT_F32, 1), s))) return e;
+        if ((e = run_gemm(p, gemm_args(p, G2_FWD_Y, p->YA, p->XB, f, f, 0), s))) return e;
+        if ((e = run_gemm(p, gemm_args(p, G3_INV_X, p->XB, p->YB, f, f, 0), s))) return e;
+        if ((e = run_gemm(p, gemm_args(p, G4_INV_Y, p->YB, p->XC, f, FMT_F32, 1), s))) return e;
     }
     return cudaSuccess;
 }
@@ -1000,8 +1001,8 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
     if (e == cudaSuccess && tc) {
         // one set of TMA descriptors per (member, pass); the planes never move
         std::vector<uint8_t> maps((size_t)n_members * 4 * kTcMapsBytes);
-        const void* in_plane[4] = {p->XA, p->YA, p->YB, p->XB};
-        const int64_t in_elems[4] = {p->xplane, p->yplane, p->yplane, p->xplane};
+        const void* in_plane[4] = {p->XA, p->YA, p->XB, p->YB};
+        const int64_t in_elems[4] = {p->xplane, p->yplane, p->xplane, p->yplane};
         for (int i = 0; i < n_members && !e; ++i)
             for (int pass = 0; pass < 4 && !e; ++pass)
                 e = gemm_tc_encode(p->mh[i], pass, in_plane[pass], in_elems[pass], o.dst_precision,

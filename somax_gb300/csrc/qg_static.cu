@@ -187,8 +187,8 @@ extern "C" int qg_invert_static(const qg_member_desc* member, const float* q, fl
     };
     if (!e) e = gemm(G1_FWD_X, P0, P1, gx, n_gx);
     if (!e) e = gemm(G2_FWD_Y, P1, P2, gy, n_gy);
-    if (!e) e = gemm(G3_INV_Y, P2, P0, gy, n_gy);
-    if (!e) e = gemm(G4_INV_X, P0, P1, gx, n_gx);
+    if (!e) e = gemm(G3_INV_X, P2, P0, gx, n_gx);
+    if (!e) e = gemm(G4_INV_Y, P0, P1, gy, n_gy);
     if (!e) e = launch_mode_to_layer(md, st, n_st, 0, P1, psi, s, false);
     return e == cudaSuccess ? QG_OK : QG_ERR_CUDA;
 }

@@ -206,18 +206,19 @@ __device__ __forceinline__ bool sweep(const StencilArgs& a, const MemberDev& M, 
     const float* qb = a.qin + M.off_x;
     const float* hb = a.psi_hat + M.off_x;
     Win<NL> w;
-    // rows are ingested from jb - 4 (a multiple of 4: static window slots); the output of
-    // row j follows the ingest of row j + 2
+    // rows are walked from jb - 4 (a multiple of 4: static window slots); the output of row j
+    // follows the ingest of row j + 2
     const int r0 = jb - 4;
-    fetch<NL, 0>(w, qb, hb, lsx, r0, Ny, x, Nx, Px);
-    fetch<NL, 1>(w, qb, hb, lsx, r0 + 1, Ny, x, Nx, Px);
+    // rows jb - 2 .. je + 1 are needed (outputs jb .. je - 1 read rows one beyond them, and the
+    // biharmonic's lap(q) one more); the two rows before and any after are skipped
     bool bad = false;
     for (int rb = r0; rb <= je + 1; rb += 4) {
 #define QG_SWEEP_ROW(K)                                                                                 \
         {                                                                                               \
             const int r = rb + K;                                                                       \
-            ingest<NL, (K) & 1, K>(w, cm, c, r, Ny, x, Nx, apply_bc, zero_psi_ring, mask);              \
-            fetch<NL, (K) & 1>(w, qb, hb, lsx, r + 2, Ny, x, Nx, Px);                                   \
+            if (r >= jb - 2 && r <= je + 1)                                                             \
+                ingest<NL, (K) & 1, K>(w, cm, c, r, Ny, x, Nx, apply_bc, zero_psi_ring, mask);          \
+            if (r + 2 <= je + 1) fetch<NL, (K) & 1>(w, qb, hb, lsx, r + 2, Ny, x, Nx, Px);              \
             const int j = r - 2;                                                                        \
             if (j >= jb && j < je) {                                                                    \
                 const float Fj = Fp[j];                                                                 \

