@@ -23,6 +23,11 @@ namespace qg {
 namespace {
 
 constexpr int PT = 256;  // threads per CTA (the stencil tile needs exactly 256)
+// The one-pass GEMM launch runs eight epilogue warps (warps 4-11, two per TMEM lane quarter,
+// each draining every other 32-column chunk): the drain of a tile, not its loads or MMAs,
+// bounds the pass when the stores split BF16 hi/lo or divide.
+constexpr int GEMM_EPI_WARPS = 8;
+constexpr int PT_GEMM = 128 + 32 * GEMM_EPI_WARPS;
 static_assert(st::NTHREADS == PT, "stencil tile thread count");
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
@@ -87,7 +92,7 @@ struct Shared {
     MemberDev M;                      // constants of the current stencil tile
 };
 
-template <int PREC, int PASS>
+template <int PREC, int PASS, int EPI = 4>
 __device__ void gemm_phase(const PersistArgs& a, uint8_t* smem, Shared& sh, uint32_t tmem, Counters& c) {
     using C = TcCfg<PREC>;
     constexpr bool xin = pass_xin(PASS);
@@ -142,7 +147,8 @@ __device__ void gemm_phase(const PersistArgs& a, uint8_t* smem, Shared& sh, uint
             tc_commit(&sh.tfull[buf]);
             sh.committed = (int)++c.mma_tiles;
         }
-    } else if (warp >= 4) {
+    } else if (warp >= 4 && warp < 4 + EPI) {
+        const int part = (warp - 4) >> 2;  // column chunks part, part + EPI / 4, ...
         for (int t = blockIdx.x; t < n; t += gridDim.x) {
             const GemmTile tl = tiles[t];
             const MemberDev& M = a.members[tl.member];
@@ -153,7 +159,7 @@ __device__ void gemm_phase(const PersistArgs& a, uint8_t* smem, Shared& sh, uint
             tc_fence_after();
             tc_epilogue<PASS>(M, g, Cv, c_fmt, PASS == G4_INV_Y ? a.g4_accumulate : 0, tl.mt * TC_BM,
                               tl.nt * a.tile_n, tc_tile_width(g.Nn, tl.nt, a.tile_n), tmem + buf * TC_TMEM_BUF,
-                              warp & 3, lane, true);
+                              warp & 3, lane, true, part, EPI / 4);
             tc_fence_before();
             mbar_arrive(&sh.tempty[buf]);
             ++c.epi_tiles;
@@ -233,7 +239,7 @@ __device__ void stencil_phase(const PersistArgs& a, int k, uint8_t* smem, Shared
     stencil_tiles<T>(sa, a.n_st, smem, a.slot_bytes, a.lap_offset, a.st_nbuf, sh, c);
 }
 
-__device__ void init_shared(Shared& sh, int stages) {
+__device__ void init_shared(Shared& sh, int stages, int epi_warps = 4) {
     if (threadIdx.x == 0) {
         for (int s = 0; s < stages; ++s) {
             mbar_init(&sh.full[s], 1);
@@ -241,7 +247,7 @@ __device__ void init_shared(Shared& sh, int stages) {
         }
         for (int b = 0; b < 2; ++b) {
             mbar_init(&sh.tfull[b], 1);
-            mbar_init(&sh.tempty[b], 4 * 32);  // every epilogue thread arrives
+            mbar_init(&sh.tempty[b], epi_warps * 32);  // every epilogue thread arrives
             mbar_init(&sh.sbar[b], 1);
         }
         sh.abort = 0;
@@ -267,12 +273,12 @@ __device__ void drain_after_abort(Shared& sh) {
 // min(tiles, SMs) CTAs, two TMEM accumulators so a tile's epilogue overlaps the next
 // tile's MMAs.
 template <int PREC, int PASS>
-__global__ void __launch_bounds__(PT, 1) k_gemm_mt(PersistArgs a) {
+__global__ void __launch_bounds__(PT_GEMM, 1) k_gemm_mt(PersistArgs a) {
     using C = TcCfg<PREC>;
     extern __shared__ uint8_t smem_raw[];
     __shared__ Shared sh;
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    init_shared(sh, C::STAGES);
+    init_shared(sh, C::STAGES, GEMM_EPI_WARPS);
     if ((threadIdx.x >> 5) == 1) tc_alloc(&sh.tmem_slot, TC_TMEM_COLS);
     tc_fence_before();
     __syncthreads();
@@ -281,7 +287,7 @@ __global__ void __launch_bounds__(PT, 1) k_gemm_mt(PersistArgs a) {
     pdl_wait();
     pdl_launch_dependents();
     Counters c;
-    gemm_phase<PREC, PASS>(a, smem, sh, tmem, c);
+    gemm_phase<PREC, PASS, GEMM_EPI_WARPS>(a, smem, sh, tmem, c);
     __syncthreads();
     drain_after_abort<C::STAGES>(sh);
     tc_fence_before();
@@ -408,10 +414,10 @@ size_t gemm_mt_smem() {
 cudaError_t launch_gemm_mt(const PersistArgs& a, int pass, int grid, int precision, cudaStream_t s, bool pdl) {
 #define QG_GMT(P)                                                                                                  \
     switch (pass) {                                                                                                \
-        case G1_FWD_X: return launch_k(k_gemm_mt<P, G1_FWD_X>, grid, PT, gemm_mt_smem<P>(), s, pdl, a);          \
-        case G2_FWD_Y: return launch_k(k_gemm_mt<P, G2_FWD_Y>, grid, PT, gemm_mt_smem<P>(), s, pdl, a);          \
-        case G3_INV_X: return launch_k(k_gemm_mt<P, G3_INV_X>, grid, PT, gemm_mt_smem<P>(), s, pdl, a);          \
-        case G4_INV_Y: return launch_k(k_gemm_mt<P, G4_INV_Y>, grid, PT, gemm_mt_smem<P>(), s, pdl, a);          \
+        case G1_FWD_X: return launch_k(k_gemm_mt<P, G1_FWD_X>, grid, PT_GEMM, gemm_mt_smem<P>(), s, pdl, a);          \
+        case G2_FWD_Y: return launch_k(k_gemm_mt<P, G2_FWD_Y>, grid, PT_GEMM, gemm_mt_smem<P>(), s, pdl, a);          \
+        case G3_INV_X: return launch_k(k_gemm_mt<P, G3_INV_X>, grid, PT_GEMM, gemm_mt_smem<P>(), s, pdl, a);          \
+        case G4_INV_Y: return launch_k(k_gemm_mt<P, G4_INV_Y>, grid, PT_GEMM, gemm_mt_smem<P>(), s, pdl, a);          \
         default: return cudaErrorInvalidValue;                                                                     \
     }
     if (precision == QG_DST_TF32) { QG_GMT(QG_DST_TF32) }

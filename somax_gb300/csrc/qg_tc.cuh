@@ -176,17 +176,17 @@ __device__ __forceinline__ void tc_store_bf16x2(__nv_bfloat16* p, int64_t plane,
     p[plane + idx] = __float2bfloat16_rn(v - __bfloat162float(hi));
 }
 
-// Epilogue of one 128 x width tile by one of four epilogue warps (TMEM lane quarter
-// `quarter`): read the accumulator 32 columns at a time and store it transposed,
+// Epilogue of one 128 x width tile by the epilogue warp(s) of TMEM lane quarter `quarter`
+// (chunks c0, c0 + cstep, ... of 32 columns each): read the accumulator and store it transposed,
 // out[(l, n)][r], straight from the registers: lane = accumulator row r, so each store
-// instruction writes 32 consecutive elements of one output row.  All four warps must call it
-// (tcgen05.ld is warp-collective); `valid` false skips the stores.  G2 divides by
+// instruction writes 32 consecutive elements of one output row.  Every lane of the warp calls
+// it (tcgen05.ld is warp-collective); `valid` false skips the stores.  G2 divides by
 // ex[r] + ey[n] - lam[l] (row term per lane, column term shuffled from the lane that loaded
 // it); G4 adds to psi_hat when `accumulate` is set (refinement).
 template <int PASS>
 __device__ __forceinline__ void tc_epilogue(const MemberDev& M, const TcGeom& g, void* Cv, int c_fmt, int accumulate,
                                             int m0, int n0, int width, uint32_t tmem_acc, int quarter, int lane,
-                                            bool valid) {
+                                            bool valid, int c0 = 0, int cstep = 1) {
     const int Mtot = g.Mtot, Mb = g.Mb, ldo = g.ldo;
     const int Nn = g.Nn;                    // columns of the pass (layer stride of the output)
     const int nend = min(Nn, n0 + width);   // this tile's columns end here
@@ -200,7 +200,7 @@ __device__ __forceinline__ void tc_epilogue(const MemberDev& M, const TcGeom& g,
     float* Cf = static_cast<float*>(Cv) + g.cbase;
     __nv_bfloat16* Cb = static_cast<__nv_bfloat16*>(Cv) + g.cbase;
     const int64_t obase = (int64_t)l * Nn * ldo + r;
-    for (int c = 0; c < (TC_BN + 31) / 32; ++c) {
+    for (int c = c0; c < (TC_BN + 31) / 32; c += cstep) {
         const int nb = n0 + c * 32;
         if (!valid || nb >= nend) break;  // warp-uniform (and the same for all four warps)
         uint32_t v[32];
