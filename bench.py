@@ -379,7 +379,7 @@ def main():
     ap.add_argument("--gemm-tile", type=int, default=None,
                     help="force the tensor-core DST tile width (144 | 80 | 48 | 32 | 16); default: autotuned")
     ap.add_argument("--stencil", default=None,
-                    help="force a stencil variant (tile32x8 | tile64x16 | sweep16 | sweep32 | sweep64); "
+                    help="force a stencil variant (tile32x8 | tile64x16 | sweep16 | sweep32 | sweep64 | lsweep16 | lsweep32 | lsweep64); "
                          "default: the autotuner's pick")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

@@ -204,7 +204,10 @@ int qg_kernel_stats(qg_plan* plan, int kclass, double* total_ms, int64_t* launch
 #define QG_STENCIL_SWEEP_16 2
 #define QG_STENCIL_SWEEP_32 3
 #define QG_STENCIL_SWEEP_64 4
-#define QG_STENCIL_VARIANTS 5
+#define QG_STENCIL_LSWEEP_16 5 /* layer-per-warp column sweep, two columns per lane */
+#define QG_STENCIL_LSWEEP_32 6
+#define QG_STENCIL_LSWEEP_64 7
+#define QG_STENCIL_VARIANTS 8
 /* The plan's tuned choice: *variant = the stencil the multi-launch path runs; ms[k] (k < n)
    the autotuner's time of one stage with variant k in ms (-1 when not measured). */
 int qg_plan_tuning(const qg_plan* plan, int* variant, float* ms, int n);

@@ -176,6 +176,13 @@ int sweep_blocks_per_sm(int nl);
 // one launch per layer count k + 1 with n_items[k] > 0 (items grouped by layer count)
 cudaError_t launch_sweep(const StencilArgs& a, const SweepItem* const* items, const int* n_items, int R,
                          const int* grid, cudaStream_t s, bool pdl);
+// The layer-per-warp sweep (two columns per lane, one warp per layer of a strip): items are
+// strips of lsweep_columns() output columns, lsweep_strips_per_block(nl) strips per CTA.
+int lsweep_columns();
+int lsweep_strips_per_block(int nl);
+int lsweep_blocks_per_sm(int nl);
+cudaError_t launch_lsweep(const StencilArgs& a, const SweepItem* const* items, const int* n_items, int R,
+                          const int* grid, cudaStream_t s, bool pdl);
 
 // launchers (return cudaError_t of the launch)
 cudaError_t launch_prep(const PrepArgs& a, int ntiles, cudaStream_t s, bool pdl);

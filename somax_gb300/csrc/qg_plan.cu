@@ -23,6 +23,10 @@ using namespace qg;
 
 namespace {
 
+// sweep item lists: strip heights 16, 32, 64 of the one-layer-per-lane sweep, then of the
+// layer-per-warp sweep
+constexpr int kSweepLists = 6;
+
 // ---------------------------------------------------------------------------------------
 // Small dense linear algebra in double (nl <= 8)
 // ---------------------------------------------------------------------------------------
@@ -262,14 +266,15 @@ struct qg_plan {
     StencilTile* st_tiles_v[2] = {nullptr, nullptr};
     int n_st_v[2] = {0, 0};
     void* st_maps_v[2] = {nullptr, nullptr};
-    float tune_ms[QG_STENCIL_VARIANTS] = {-1.f, -1.f, -1.f, -1.f, -1.f};
-    // column-sweep stencil: item lists for 16-, 32- and 64-row strips; sw_sel = the one the
+    float tune_ms[QG_STENCIL_VARIANTS] = {-1.f, -1.f, -1.f, -1.f, -1.f, -1.f, -1.f, -1.f};
+    // column-sweep stencils: item lists of the one-layer-per-lane sweep (v = 0, 1, 2) and the
+    // layer-per-warp sweep (v = 3, 4, 5) for 16-, 32- and 64-row strips; sw_sel = the one the
     // multi-launch path runs (-1: the tile stencil)
-    SweepItem* sw_items_v[3] = {nullptr, nullptr, nullptr};
-    int n_sw_v[3] = {0, 0, 0};
+    SweepItem* sw_items_v[kSweepLists] = {};
+    int n_sw_v[kSweepLists] = {};
     // items of each list grouped by layer count: group k (k + 1 layers) at offset sw_off
-    int sw_off[3][kMaxLayers] = {};
-    int sw_cnt[3][kMaxLayers] = {};
+    int sw_off[kSweepLists][kMaxLayers] = {};
+    int sw_cnt[kSweepLists][kMaxLayers] = {};
     int sw_sel = -1;
     int sw_grid[kMaxLayers] = {};
     PersistArgs pa{};         // constant part of the tensor-core launches' arguments
@@ -462,7 +467,7 @@ StencilArgs stencil_args(qg_plan* p, const float* params) {
     return a;
 }
 
-constexpr int kSweepRows[3] = {16, 32, 64};
+constexpr int kSweepRows[3] = {16, 32, 64};  // strip heights of sweep list v: kSweepRows[v % 3]
 constexpr int kNumBN = 5;
 constexpr int kGemmBN[kNumBN] = {144, 80, 48, 32, 16};  // tensor-core output tile widths the autotuner tries
 
@@ -475,6 +480,7 @@ cudaError_t launch_stencil(qg_plan* p, StencilArgs a, cudaStream_t s, bool pdl) 
         const int v = p->sw_sel;
         const SweepItem* items[kMaxLayers];
         for (int k = 0; k < kMaxLayers; ++k) items[k] = p->sw_items_v[v] + p->sw_off[v][k];
+        if (v >= 3) return launch_lsweep(a, items, p->sw_cnt[v], kSweepRows[v % 3], p->sw_grid, s, pdl);
         return launch_sweep(a, items, p->sw_cnt[v], kSweepRows[v], p->sw_grid, s, pdl);
     }
     return launch_stencil_mt(a, p->n_st, p->st_grid, p->max_nl, p->st_large, s, pdl);
@@ -592,10 +598,13 @@ int cuda_err(cudaError_t e) { return e == cudaSuccess ? QG_OK : QG_ERR_CUDA; }
 void select_sweep(qg_plan* p, int v) {
     p->sw_sel = v;
     if (v < 0) return;
-    const int per_cta = sweep_warps_per_block();  // one strip per warp
     for (int k = 0; k < kMaxLayers; ++k) {
+        // strips per CTA: one per warp (one-layer-per-lane sweep) or one per group of k + 1
+        // warps (layer-per-warp sweep)
+        const int per_cta = v >= 3 ? lsweep_strips_per_block(k + 1) : sweep_warps_per_block();
+        const int per_sm = v >= 3 ? lsweep_blocks_per_sm(k + 1) : sweep_blocks_per_sm(k + 1);
         const int ctas = (p->sw_cnt[v][k] + per_cta - 1) / per_cta;
-        p->sw_grid[k] = std::max(1, std::min(ctas, sweep_blocks_per_sm(k + 1) * std::max(p->n_sm, 1)));
+        p->sw_grid[k] = std::max(1, std::min(ctas, per_sm * std::max(p->n_sm, 1)));
     }
 }
 
@@ -813,7 +822,7 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
         p->st_large = large_tiles >= 2 * (int64_t)std::max(p->n_sm, 1);
     }
     std::vector<StencilTile> st_v[2];
-    std::vector<SweepItem> sw_v[3];
+    std::vector<SweepItem> sw_v[kSweepLists];
     std::vector<CapItem> cap;
     bool too_large = false;
     // geometry and offsets
@@ -924,8 +933,8 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
             }
         }
         // column-sweep strips
-        for (int v = 0; v < 3; ++v) {
-            const int R = kSweepRows[v], W = sweep_columns();
+        for (int v = 0; v < kSweepLists; ++v) {
+            const int R = kSweepRows[v % 3], W = v >= 3 ? lsweep_columns() : sweep_columns();
             for (int sy = 0; sy < (M.Ny + R - 1) / R; ++sy)
                 for (int sx = 0; sx < (M.Nx + W - 1) / W; ++sx) sw_v[v].push_back({i, sx, sy});
         }
@@ -962,7 +971,7 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
             e = upload(p, &p->cap_items, cap);
             if (!e) e = capacitance_init(p->cap_smem);
         }
-        for (int v = 0; v < 3 && !e; ++v) {
+        for (int v = 0; v < kSweepLists && !e; ++v) {
             // group by layer count: one sweep launch per group
             std::vector<SweepItem> g;
             for (int k = 0; k < kMaxLayers; ++k) {

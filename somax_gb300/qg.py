@@ -302,8 +302,8 @@ class Plan:
         masked = any(m.mask is not None for m in self.members)
         if self.persistent and self.precision != "fp32" and self.refine == 0 and not butcher and not masked:
             return 3  # pack, the persistent step kernel, unpack
-        # the column-sweep stencil launches once per distinct layer count
-        sweep = self.tuning()["stencil"].startswith("sweep")
+        # the column-sweep stencils launch once per distinct layer count
+        sweep = "sweep" in self.tuning()["stencil"]
         stencil = len({m.n_layers for m in self.members}) if sweep else 1
         solve = 4 * (1 + self.refine) + self.refine
         inversion = solve
@@ -312,7 +312,7 @@ class Plan:
         per_stage = inversion + stencil + (1 if butcher else 0)
         return 2 + n_steps * stages * per_stage
 
-    STENCIL_VARIANTS = ("tile32x8", "tile64x16", "sweep16", "sweep32", "sweep64")
+    STENCIL_VARIANTS = ("tile32x8", "tile64x16", "sweep16", "sweep32", "sweep64", "lsweep16", "lsweep32", "lsweep64")
 
     def tuning(self) -> dict:
         """The autotuner's stencil choice and the time (ms) of one RK stage (four DST passes

@@ -73,7 +73,7 @@ def test_masked_barotropic_inversion_and_rhs():
     assert rel(dq, OM.vector_field(o, q, mask)) < RTOL_MASK
 
 
-@pytest.mark.parametrize("stencil", ["tile32x8", "tile64x16", "sweep16"])
+@pytest.mark.parametrize("stencil", ["tile32x8", "tile64x16", "sweep16", "lsweep16"])
 def test_masked_rhs_and_steps(stencil):
     nx, ny, nl = 70, 54, 3
     mask = tc.land_mask(ny, nx, frac=0.15, seed=3)

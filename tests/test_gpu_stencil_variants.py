@@ -56,7 +56,7 @@ def test_variant_rhs_and_steps(variant, nx, ny, nl):
         assert rel(got, O.integrate(o, q, 1200.0, 3, scheme)) < RTOL_STEP
 
 
-@pytest.mark.parametrize("variant", ["sweep16", "sweep32", "sweep64"])
+@pytest.mark.parametrize("variant", ["sweep16", "sweep32", "sweep64", "lsweep16", "lsweep32", "lsweep64"])
 def test_sweep_ensemble_mixed_layers(variant):
     specs = [((30, 30), 1, 3), ((40, 33), 3, 4), ((24, 24), 5, 5), ((130, 66), 2, 6), ((17, 13), 3, 7)]
     ms, os, qs = [], [], []
@@ -78,12 +78,13 @@ def test_sweep_ensemble_mixed_layers(variant):
         assert rel(got, O.integrate(o, q, 1200.0, 3, "ssprk3")) < RTOL_STEP
 
 
-def test_sweep_equals_tile_stencil():
+@pytest.mark.parametrize("variant", ["sweep32", "lsweep32"])
+def test_sweep_equals_tile_stencil(variant):
     m, _, q = pair(130, 98, 3, 9)
     pv = m._param_vector(torch.device("cuda"))
     qd = torch.tensor(q, dtype=torch.float32, device="cuda")
     a = sg.Plan([m.spec], "fp32", stencil="tile32x8").step(qd.clone(), pv, 1200.0, 5, "ssprk3")
-    b = sg.Plan([m.spec], "fp32", stencil="sweep32").step(qd.clone(), pv, 1200.0, 5, "ssprk3")
+    b = sg.Plan([m.spec], "fp32", stencil=variant).step(qd.clone(), pv, 1200.0, 5, "ssprk3")
     assert rel(b, a) < 1e-6
 
 
@@ -101,7 +102,7 @@ def test_gemm_tile_widths(precision, tile, nx, ny, nl):
 
 
 @pytest.mark.parametrize("scheme", ["euler", "tsit5"])
-@pytest.mark.parametrize("variant", ["tile32x8", "sweep16"])
+@pytest.mark.parametrize("variant", ["tile32x8", "sweep16", "lsweep16"])
 @pytest.mark.parametrize("precision", ["fp32", "bf16x3"])
 def test_butcher_schemes_fused(scheme, variant, precision):
     """Euler and Tsit5 fused into qg_step (stencil in rhs mode + stage combine) against the
