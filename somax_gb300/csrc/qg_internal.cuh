@@ -177,10 +177,22 @@ int sweep_blocks_per_sm(int nl);
 cudaError_t launch_sweep(const StencilArgs& a, const SweepItem* const* items, const int* n_items, int R,
                          const int* grid, cudaStream_t s, bool pdl);
 // The layer-per-warp sweep (two columns per lane, one warp per layer of a strip): items are
-// strips of lsweep_columns() output columns, lsweep_strips_per_block(nl) strips per CTA.
+// strips of kLSweepOut output columns, lsweep_strips_per_block(nl) strips per CTA.  Each strip
+// class has its own kernel: 0 = every column and row the strip reads is strictly inside the
+// member (no ring, member-edge or store predicates), 1 = the strip touches the ring or the
+// member's edge, 2 = masked member (land rules).
+constexpr int kLSweepOut = 60;
+constexpr int kLSweepClasses = 3;
+__host__ __device__ inline int lsweep_item_class(int Ny, int Nx, bool masked, int sx, int sy, int R) {
+    if (masked) return 2;
+    const int x0 = sx * kLSweepOut, jb = sy * R, rhi = (jb + R < Ny ? jb + R : Ny) + 1;
+    // columns x0 - 2 .. x0 + 61 and rows jb - 2 .. rhi are read
+    return (x0 - 2 >= 1 && x0 + 61 <= Nx - 2 && jb - 2 >= 1 && rhi <= Ny - 2) ? 0 : 1;
+}
 int lsweep_columns();
 int lsweep_strips_per_block(int nl);
-int lsweep_blocks_per_sm(int nl);
+int lsweep_blocks_per_sm(int nl, int cls);
+// items / n_items / grid: kMaxLayers * kLSweepClasses groups, group (nl - 1) * kLSweepClasses + class
 cudaError_t launch_lsweep(const StencilArgs& a, const SweepItem* const* items, const int* n_items, int R,
                           const int* grid, cudaStream_t s, bool pdl);
 

@@ -26,6 +26,7 @@ namespace {
 // sweep item lists: strip heights 16, 32, 64 of the one-layer-per-lane sweep, then of the
 // layer-per-warp sweep
 constexpr int kSweepLists = 6;
+constexpr int kSweepGroups = kMaxLayers * kLSweepClasses;
 
 // ---------------------------------------------------------------------------------------
 // Small dense linear algebra in double (nl <= 8)
@@ -272,11 +273,12 @@ struct qg_plan {
     // multi-launch path runs (-1: the tile stencil)
     SweepItem* sw_items_v[kSweepLists] = {};
     int n_sw_v[kSweepLists] = {};
-    // items of each list grouped by layer count: group k (k + 1 layers) at offset sw_off
-    int sw_off[kSweepLists][kMaxLayers] = {};
-    int sw_cnt[kSweepLists][kMaxLayers] = {};
+    // items of each list grouped by layer count and strip class: group k * kLSweepClasses + c
+    // (k + 1 layers, class c; always class 0 for the one-layer-per-lane sweep) at offset sw_off
+    int sw_off[kSweepLists][kSweepGroups] = {};
+    int sw_cnt[kSweepLists][kSweepGroups] = {};
     int sw_sel = -1;
-    int sw_grid[kMaxLayers] = {};
+    int sw_grid[kSweepGroups] = {};
     PersistArgs pa{};         // constant part of the tensor-core launches' arguments
     // graphs
     cudaStream_t cap = nullptr;
@@ -478,10 +480,18 @@ cudaError_t launch_stencil(qg_plan* p, StencilArgs a, cudaStream_t s, bool pdl) 
     a.psi_hat = p->XC;
     if (p->sw_sel >= 0) {
         const int v = p->sw_sel;
-        const SweepItem* items[kMaxLayers];
-        for (int k = 0; k < kMaxLayers; ++k) items[k] = p->sw_items_v[v] + p->sw_off[v][k];
+        const SweepItem* items[kSweepGroups];
+        for (int k = 0; k < kSweepGroups; ++k) items[k] = p->sw_items_v[v] + p->sw_off[v][k];
         if (v >= 3) return launch_lsweep(a, items, p->sw_cnt[v], kSweepRows[v % 3], p->sw_grid, s, pdl);
-        return launch_sweep(a, items, p->sw_cnt[v], kSweepRows[v], p->sw_grid, s, pdl);
+        // the one-layer-per-lane sweep: class 0 of each layer count
+        const SweepItem* it1[kMaxLayers];
+        int cnt1[kMaxLayers], grid1[kMaxLayers];
+        for (int k = 0; k < kMaxLayers; ++k) {
+            it1[k] = items[k * kLSweepClasses];
+            cnt1[k] = p->sw_cnt[v][k * kLSweepClasses];
+            grid1[k] = p->sw_grid[k * kLSweepClasses];
+        }
+        return launch_sweep(a, it1, cnt1, kSweepRows[v], grid1, s, pdl);
     }
     return launch_stencil_mt(a, p->n_st, p->st_grid, p->max_nl, p->st_large, s, pdl);
 }
@@ -598,13 +608,14 @@ int cuda_err(cudaError_t e) { return e == cudaSuccess ? QG_OK : QG_ERR_CUDA; }
 void select_sweep(qg_plan* p, int v) {
     p->sw_sel = v;
     if (v < 0) return;
-    for (int k = 0; k < kMaxLayers; ++k) {
+    for (int g = 0; g < kSweepGroups; ++g) {
+        const int k = g / kLSweepClasses, c = g % kLSweepClasses;
         // strips per CTA: one per warp (one-layer-per-lane sweep) or one per group of k + 1
         // warps (layer-per-warp sweep)
         const int per_cta = v >= 3 ? lsweep_strips_per_block(k + 1) : sweep_warps_per_block();
-        const int per_sm = v >= 3 ? lsweep_blocks_per_sm(k + 1) : sweep_blocks_per_sm(k + 1);
-        const int ctas = (p->sw_cnt[v][k] + per_cta - 1) / per_cta;
-        p->sw_grid[k] = std::max(1, std::min(ctas, per_sm * std::max(p->n_sm, 1)));
+        const int per_sm = v >= 3 ? lsweep_blocks_per_sm(k + 1, c) : sweep_blocks_per_sm(k + 1);
+        const int ctas = (p->sw_cnt[v][g] + per_cta - 1) / per_cta;
+        p->sw_grid[g] = std::max(1, std::min(ctas, per_sm * std::max(p->n_sm, 1)));
     }
 }
 
@@ -972,12 +983,17 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
             if (!e) e = capacitance_init(p->cap_smem);
         }
         for (int v = 0; v < kSweepLists && !e; ++v) {
-            // group by layer count: one sweep launch per group
+            // group by layer count and strip class: one sweep launch per group
             std::vector<SweepItem> g;
-            for (int k = 0; k < kMaxLayers; ++k) {
+            for (int k = 0; k < kSweepGroups; ++k) {
                 p->sw_off[v][k] = (int)g.size();
-                for (const SweepItem& it : sw_v[v])
-                    if (members[it.member].n_layers == k + 1) g.push_back(it);
+                for (const SweepItem& it : sw_v[v]) {
+                    const qg_member_desc& d = members[it.member];
+                    const int cls = v >= 3 ? lsweep_item_class(d.ny + 2, d.nx + 2, d.mask != nullptr, it.sx, it.sy,
+                                                               kSweepRows[v % 3])
+                                           : 0;
+                    if (d.n_layers * kLSweepClasses + cls == k + kLSweepClasses) g.push_back(it);
+                }
                 p->sw_cnt[v][k] = (int)g.size() - p->sw_off[v][k];
             }
             p->n_sw_v[v] = (int)g.size();
@@ -1271,6 +1287,7 @@ int qg_status(qg_plan* p, int* flags, void* stream) {
     if (e) return QG_ERR_CUDA;
     if (flags) *flags = h;
     if (h & 2) return QG_ERR_TIMEOUT;
+    if (h & 4) return QG_ERR_CUDA;  // a kernel met a work item it was not built for and skipped it
     if (h & 1) return QG_ERR_NONFINITE;
     return QG_OK;
 }
