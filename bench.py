@@ -237,7 +237,7 @@ def run_reference(args):
 class Workload:
     """One bench step = one model day of every member, on one device."""
 
-    def __init__(self, name, precision, persistent, dev, seed, stencil=None, gemm_tile=None):
+    def __init__(self, name, precision, persistent, dev, seed, stencil=None, gemm_tile=None, cluster=None):
         import torch
 
         import somax_gb300 as sg
@@ -252,12 +252,13 @@ class Workload:
                 for _ in range(count):
                     kw = cfg.model_kwargs()
                     kw["wind_amplitude"] = tc.wind_amplitude(float(rng.uniform(0.05, 0.12)), cfg.L)
-                    models.append(sg.BaroclinicQG.create(**kw, precision=precision, persistent=persistent))
+                    models.append(sg.BaroclinicQG.create(**kw, precision=precision, persistent=persistent,
+                                                         cluster=cluster))
                     q0s.append(tc.initial_pv(cfg, seed=10000 * seed + k).astype(np.float32))
                     cfgs.append(cfg)
                     k += 1
             self.ens = sg.QGEnsemble(models, precision=precision, persistent=persistent, device=dev, stencil=stencil,
-                                     gemm_tile=gemm_tile)
+                                     gemm_tile=gemm_tile, cluster=cluster)
             self.plan = self.ens.plan
             self.params = self.ens.params(dev)
             self.q0 = np.concatenate([q.reshape(-1) for q in q0s])
@@ -270,7 +271,7 @@ class Workload:
             mask = tc.land_mask(cfg.n, cfg.n, frac=0.15, seed=0) if masked else None
             self.model = sg.BaroclinicQG.create(**cfg.model_kwargs(), precision=precision, persistent=persistent,
                                                 stencil=stencil, gemm_tile=gemm_tile, mask=mask,
-                                                refine=1 if masked else 0)
+                                                refine=1 if masked else 0, cluster=cluster)
             self.plan = self.model.plan(dev)
             self.params = self.model._param_vector(dev)
             q0 = tc.initial_pv(cfg, seed=seed)
@@ -318,7 +319,7 @@ def traffic_table():
         return json.load(f).get("bytes_per_launch", {})
 
 
-def roofline(W, stats, precision, name):
+def roofline(W, stats, precision, name, cluster=False):
     """Roofline of every kernel class from the profiled pass's per-launch event times.
 
     Algorithmic HBM bytes per launch, per layer-cell of every member (lc = sum nl Ny Nx):
@@ -326,12 +327,17 @@ def roofline(W, stats, precision, name):
       rhs_stencil  step mode: q of the stage, psi_hat, y0 in (12 B); y_next and the next
                    stage's modal operand out (8 B)
       prep / other pack q (4 B in, 8 B out) / unpack (4 B in, 4 B out)
+      cluster      the cluster-resident step kernel (class 4 when the plan steps with it): the
+                   state in (4 B) and out (4 B) once per launch; everything else lives in shared
+                   memory, so the kernel is bound by its SMs' FP32 work and barriers, not HBM
     Issued tensor flops of a DST-I pass: 2 N per element (three products for BF16x3).  A
     kernel is HBM-bound when its bytes / peak bandwidth exceed its flops / peak throughput.
     The dominant class (largest total time) is the headline."""
     pk = peaks()
     lc = W.cells()
     bytes_per = {0: 12.0 * lc, 1: 8.0 * lc, 2: 20.0 * lc, 3: 8.0 * lc}
+    if cluster:
+        bytes_per[4] = 8.0 * lc
     flops_per = {1: W.gemm_flops_per_pass() * (3.0 if precision == "bf16x3" else 1.0)}
     traffic = traffic_table().get(name, {})
     kernels = {}
@@ -352,15 +358,19 @@ def roofline(W, stats, precision, name):
             ent["bound"] = "hbm"
         ent["traffic"] = traffic.get(KERNEL_CLASSES[k])
         kernels[KERNEL_CLASSES[k]] = ent
-    dom = max((k for k in (1, 2) if KERNEL_CLASSES[k] in kernels), key=lambda k: stats[k][0])
-    d = kernels[KERNEL_CLASSES[dom]]
+    if cluster and "persistent" in kernels:
+        kernels["cluster"] = kernels.pop("persistent")
+        dom_name = "cluster"
+    else:
+        dom_name = KERNEL_CLASSES[max((k for k in (1, 2) if KERNEL_CLASSES[k] in kernels), key=lambda k: stats[k][0])]
+    d = kernels[dom_name]
     if d["bound"] == "tensor":
         roof = {"bound": "tensor", "achieved": d["issued_tflops"], "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
                 "frac": d["tensor_frac"]}
     else:
         roof = {"bound": "hbm", "achieved": d["achieved_gbs"], "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": d["hbm_frac"]}
-    roof.update({"kernel": KERNEL_CLASSES[dom], "traffic": d["traffic"], "peak_src": pk["src"],
+    roof.update({"kernel": dom_name, "traffic": d["traffic"], "peak_src": pk["src"],
                  "algorithmic_bytes_per_launch": d["bytes_per_launch"], "avg_launch_us": d["avg_us"],
                  "kernels": kernels})
     return roof
@@ -382,6 +392,8 @@ def main():
                     help="force a stencil variant (tile32x8 | tile64x16 | sweep16 | sweep32 | sweep64 | lsweep16 | lsweep32 | lsweep64); "
                          "default: the autotuner's pick")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cluster", default="auto", choices=["auto", "on", "off"],
+                    help="cluster-resident stepping of small members: autotuned, forced on, or off")
     args = ap.parse_args()
 
     from somax_gb300 import testcases as tc
@@ -401,7 +413,8 @@ def main():
     if world > 1:
         dist.init_process_group("nccl", device_id=dev)
 
-    W = Workload(args.config, args.precision, bool(args.persistent), dev, rank, args.stencil, args.gemm_tile)
+    W = Workload(args.config, args.precision, bool(args.persistent), dev, rank, args.stencil, args.gemm_tile,
+                 {"auto": None, "on": True, "off": False}[args.cluster])
     plan = W.plan
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
 
@@ -459,7 +472,7 @@ def main():
     torch.cuda.synchronize()
     stats = {k: plan.kernel_stats(k) for k in range(5)}
     plan.set_profiling(False)
-    roof = roofline(W, stats, args.precision, args.config)
+    roof = roofline(W, stats, args.precision, args.config, plan.engine()["cluster_ctas"] > 0)
 
     line = {
         "metric": W.metric, "value": value, "unit": W.unit, "n_gpus": world, "steps": args.steps,
@@ -469,7 +482,7 @@ def main():
                    "precision": args.precision, "persistent": bool(args.persistent),
                    "l2": "flushed between timed steps (256 MB write)",
                    "replicas": "independent basins per rank" if world > 1 else "one device",
-                   "tuning": plan.tuning(), "status": status},
+                   "tuning": dict(plan.tuning(), engine=plan.engine()), "status": status},
         "e2e": {"value": e2e_value, "unit": W.unit, "h2d_bytes_per_step": qbytes, "d2h_bytes_per_step": qbytes,
                 "api": "BaroclinicQG.step / QGEnsemble.step_host with pinned host q -> qg_step"},
         "roofline": roof,

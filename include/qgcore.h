@@ -118,7 +118,11 @@ typedef struct qg_options {
     int autotune;       /* 1: qg_plan_create times the stencil variants and keeps the fastest */
     int stencil;        /* 0: autotuner's choice; QG_STENCIL_* + 1: run that variant */
     int gemm_tile;      /* 0: autotuner's choice; 144, 80, 48, 32 or 16: that tensor-core tile width */
-    int reserved[1];
+    int cluster;        /* cluster-resident stepping of small members (qg_step with Heun / SSP-RK3:
+                           one thread-block cluster per member runs every stage of every step in
+                           one launch, FP32 DST passes on the CUDA cores, state in shared memory):
+                           0: used when the autotuner times it faster than the multi-launch path,
+                           1: used whenever the members allow it, 2: never */
 } qg_options;
 
 typedef struct qg_plan qg_plan;
@@ -215,6 +219,12 @@ int qg_plan_tuning(const qg_plan* plan, int* variant, float* ms, int n);
    columns; 64 for the FP32 CUDA-core passes) and the time of the four passes it measured
    with each width in ms (ms[0..4] in that order; -1 when not measured). */
 int qg_plan_gemm_tuning(const qg_plan* plan, int* tile_n, float* ms, int n);
+/* The stepping engine qg_step uses for Heun / SSP-RK3: *cluster_ctas = the CTAs of one
+   member's cluster when the cluster-resident engine runs (all members alike in layers and
+   grid, unmasked, small enough for one cluster's shared memory), else 0; ms[0], ms[1] (n >= 2)
+   the autotuner's time of four SSP-RK3 steps with the multi-launch path and with the cluster
+   engine (-1 when not measured). */
+int qg_plan_engine(const qg_plan* plan, int* cluster_ctas, float* ms, int n);
 
 #ifdef __cplusplus
 }

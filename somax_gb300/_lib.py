@@ -53,7 +53,7 @@ class MemberDesc(C.Structure):
 class Options(C.Structure):
     _fields_ = [("dst_precision", C.c_int), ("refine_sweeps", C.c_int), ("use_graphs", C.c_int),
                 ("persistent", C.c_int), ("autotune", C.c_int), ("stencil", C.c_int),
-                ("gemm_tile", C.c_int), ("reserved", C.c_int * 1)]
+                ("gemm_tile", C.c_int), ("cluster", C.c_int)]
 
 
 _lib = None
@@ -89,6 +89,7 @@ def lib() -> C.CDLL:
         "qg_kernel_stats": (C.c_int, [vp, C.c_int, C.POINTER(C.c_double), C.POINTER(i64)]),
         "qg_plan_tuning": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_float), C.c_int]),
         "qg_plan_gemm_tuning": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_float), C.c_int]),
+        "qg_plan_engine": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_float), C.c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

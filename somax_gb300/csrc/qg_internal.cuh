@@ -304,6 +304,66 @@ cudaError_t launch_capacitance(const MemberDev* members, const CapItem* items, i
 cudaError_t capacitance_init(size_t max_smem);
 constexpr int kMaxBoundary = 28000;  // boundary points per member (FP64 gather in shared memory)
 
+// Cluster-resident stepping of small members (qg_cluster.cu): shared-memory layout of one
+// CTA of a cluster of C CTAs for a member of nl layers on an Ny x Nx grid (float offsets).
+struct ClGeom {
+    int C, By, Bx;         // row / column block of a CTA
+    int BPy, BPx;          // blocks padded to a multiple of 4
+    int BPe, BPq;          // row block + 1-row halos (psi, lap q), + 2-row halos (stage input)
+    int Hx, Hy, NPx, NPy;  // folded DST-I matrices: ceil(N / 2) rows, pitch round_up(N, 4)
+    int share_s;           // Nx == Ny: one matrix for both axes
+    int o_sx, o_sy, o_ra, o_rb, o_psi, o_fold, o_q0, o_q1, o_y0, o_stg, o_const, total;
+};
+__host__ __device__ inline int round4(int v) { return (v + 3) & ~3; }
+__host__ __device__ inline ClGeom cl_geom(int nl, int Ny, int Nx, int C) {
+    ClGeom g;
+    g.C = C;
+    g.By = (Ny + C - 1) / C;
+    g.Bx = (Nx + C - 1) / C;
+    g.BPy = round4(g.By);
+    g.BPx = round4(g.Bx);
+    g.BPe = round4(g.By + 2);
+    g.BPq = round4(g.By + 4);
+    g.Hx = (Nx + 1) / 2;
+    g.Hy = (Ny + 1) / 2;
+    g.NPx = round4(Nx);
+    g.NPy = round4(Ny);
+    g.share_s = Nx == Ny;
+    int o = 0;
+    g.o_sx = o;
+    o += g.Hx * g.NPx;
+    g.o_sy = g.share_s ? g.o_sx : o;
+    if (!g.share_s) o += g.Hy * g.NPy;
+    g.o_ra = o;  // x-owned planes [nl][Ny][BPx]
+    o += nl * Ny * g.BPx;
+    g.o_rb = o;  // y-owned planes [nl][Nx][BPy] (also the operand of the first pass)
+    o += nl * Nx * g.BPy;
+    g.o_psi = o;  // psi_hat / psi with 1-row halos [nl][Nx][BPe]
+    o += nl * Nx * g.BPe;
+    const int Hm = g.Hx > g.Hy ? g.Hx : g.Hy, BPm = g.BPx > g.BPy ? g.BPx : g.BPy;
+    const int fold = nl * Hm * 2 * BPm, lap = nl * Nx * g.BPe;
+    g.o_fold = o;  // folded pass input; lap q during the stencil
+    o += fold > lap ? fold : lap;
+    g.o_q0 = o;  // stage inputs with 2-row halos [nl][Nx][BPq], two
+    o += nl * Nx * g.BPq;
+    g.o_q1 = o;
+    o += nl * Nx * g.BPq;
+    g.o_y0 = o;  // state [nl][Nx][BPy]
+    o += nl * Nx * g.BPy;
+    const int Bm = g.By > g.Bx ? g.By : g.Bx;
+    const int BPo = BPm > g.BPe ? BPm : g.BPe;
+    g.o_stg = o;  // outgoing chunks [C][nl][rows][BPo]
+    o += C * nl * Bm * BPo;
+    g.o_const = o;  // Cm2l, Cl2m (nl x nl), lambda (nl), F (Ny), ex (Nx), ey (Ny)
+    o += round4(2 * nl * nl + nl + 2 * Ny + Nx);
+    g.total = o;
+    return g;
+}
+int cluster_size_for(int nl, int Ny, int Nx, size_t* smem_bytes);
+cudaError_t launch_cluster(const MemberDev* members, int n_members, int nl, int C, size_t smem, float* q,
+                           const float* params, int apply_bc, int n_steps, int n_stages, const float* sa,
+                           const float* sb, float dt, int* flags, cudaStream_t s);
+
 // host helpers shared by the plan and the plan-free entry points
 int validate_member(const qg_member_desc& d);
 void member_constants(const qg_member_desc& d, MemberDev& M, double* Cl2m, double* Cm2l, double* lam);

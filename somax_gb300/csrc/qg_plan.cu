@@ -241,6 +241,14 @@ struct qg_plan {
     int n_gx_v[5] = {}, n_gy_v[5] = {};
     int n_bn = 1, bn_sel = 0;
     float tune_gemm_ms[5] = {-1.f, -1.f, -1.f, -1.f, -1.f};
+    // cluster-resident stepping (qg_cluster.cu): CTAs per member's cluster (0: not possible),
+    // its dynamic shared memory, the members' layer count, whether qg_step uses it, and the
+    // autotuner's times of four SSP-RK3 steps (multi-launch, cluster)
+    int cl_C = 0;
+    size_t cl_smem = 0;
+    int cl_nl = 0;
+    bool cl_use = false;
+    float tune_engine_ms[2] = {-1.f, -1.f};
     // device memory: x-row planes XA (modal operand), XB (U, the divided spectrum), XC
     // (psi_hat), XQ (FP32 modal rhs for refinement), S0 (state), S1/S2 (stage inputs); y-row
     // planes YA (T1) and YB (V), the outputs of the x-contracting passes
@@ -677,6 +685,8 @@ cudaError_t autotune_gemm(qg_plan* p) {
     return e;
 }
 
+int autotune_engine(qg_plan* p);
+
 // Autotuner: time every stencil variant (tile shapes, sweep strip heights) in its setting,
 // one RK stage (the four DST passes, then the step-mode stencil) on the plan's own planes
 // (zero state, zero parameters), with CUDA events; the passes are common to all variants,
@@ -798,6 +808,7 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
     if (opts) o = *opts;
     if (o.dst_precision < QG_DST_FP32 || o.dst_precision > QG_DST_BF16X3) return QG_ERR_ARG;
     if (o.refine_sweeps < 0 || o.refine_sweeps > 1) return QG_ERR_ARG;
+    if (o.cluster < 0 || o.cluster > 2) return QG_ERR_ARG;
     if (o.stencil < 0 || o.stencil > QG_STENCIL_VARIANTS) return QG_ERR_ARG;
     if (o.gemm_tile != 0 && std::find(kGemmBN, kGemmBN + kNumBN, o.gemm_tile) == kGemmBN + kNumBN)
         return QG_ERR_ARG;
@@ -1085,6 +1096,24 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
     }
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess && o.cluster != 2) {
+        // cluster-resident stepping: every member alike in layers and grid, no land
+        bool alike = true;
+        for (int i = 0; i < n_members; ++i)
+            alike = alike && !members[i].mask && members[i].n_layers == members[0].n_layers &&
+                    members[i].nx == members[0].nx && members[i].ny == members[0].ny;
+        if (alike) {
+            p->cl_nl = members[0].n_layers;
+            p->cl_C = cluster_size_for(p->cl_nl, members[0].ny + 2, members[0].nx + 2, &p->cl_smem);
+        }
+        if (p->cl_C > 0 && o.cluster == 1) p->cl_use = true;
+        // the autotuner weighs it only when no stencil variant or tile width is forced (a
+        // forced choice asks for the multi-launch path)
+        if (p->cl_C > 0 && o.cluster == 0 && o.autotune && !o.stencil && !o.gemm_tile) {
+            const int r = autotune_engine(p);
+            if (r != QG_OK) e = cudaErrorUnknown;
+        }
+    }
     if (e != cudaSuccess) {
         qg_plan_destroy(p);
         return too_large ? QG_ERR_TOO_LARGE : QG_ERR_CUDA;
@@ -1163,6 +1192,20 @@ int qg_step(qg_plan* p, float* q, const float* params, double dt, int n_steps, i
     if (scheme_stages(scheme, st) == 0 && !butcher(scheme)) return QG_ERR_ARG;
     if (!(dt == dt)) return QG_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
+    if (p->cl_use && n_steps > 0 && !butcher(scheme)) {
+        // one launch: every stage of every step, q and params read in the caller's packing
+        const int ns = scheme_stages(scheme, st);
+        float sa[4], sb[4];
+        for (int k = 0; k < ns; ++k) {
+            sa[k] = st[k].a;
+            sb[k] = st[k].b;
+        }
+        const cudaError_t ec = timed(p, QG_K_PERSISTENT, s, [&] {
+            return launch_cluster(p->md, p->n_members, p->cl_nl, p->cl_C, p->cl_smem, q, params,
+                                  (flags & QG_STEP_APPLY_BC) ? 1 : 0, n_steps, ns, sa, sb, (float)dt, p->flags, s);
+        });
+        return cuda_err(ec);
+    }
     cudaError_t e = cudaMemcpyAsync(p->params, params, sizeof(float) * p->n_members * QG_NPARAMS,
                                     cudaMemcpyDeviceToDevice, s);
     // the state lives in S0 for the whole call; its ring is zeroed only for a new
@@ -1306,6 +1349,13 @@ int qg_plan_gemm_tuning(const qg_plan* p, int* tile_n, float* ms, int n) {
     return QG_OK;
 }
 
+int qg_plan_engine(const qg_plan* p, int* cluster_ctas, float* ms, int n) {
+    if (!p) return QG_ERR_NULL;
+    if (cluster_ctas) *cluster_ctas = p->cl_use ? p->cl_C : 0;
+    for (int k = 0; ms && k < n && k < 2; ++k) ms[k] = p->tune_engine_ms[k];
+    return QG_OK;
+}
+
 int qg_set_profiling(qg_plan* p, int enable) {
     if (!p) return QG_ERR_NULL;
     cudaDeviceSynchronize();
@@ -1329,3 +1379,45 @@ int qg_kernel_stats(qg_plan* p, int k, double* total_ms, int64_t* launches) {
 }
 
 }  // extern "C"
+
+namespace {
+
+// Autotuner: time four SSP-RK3 steps of a zero state through qg_step with the multi-launch
+// path (graph replay) and with the cluster engine, after one warm-up call each, and keep the
+// faster.  The state is the YA plane (it holds at least one packed field), the parameters
+// ones in the K planes.
+int autotune_engine(qg_plan* p) {
+    cudaStream_t s = p->cap;
+    float* qd = p->YA;
+    float* prm = p->K;
+    std::vector<float> ones((size_t)p->n_members * QG_NPARAMS, 1.f);
+    if (cudaMemsetAsync(qd, 0, sizeof(float) * p->state_size, s) ||
+        cudaMemcpyAsync(prm, ones.data(), ones.size() * sizeof(float), cudaMemcpyHostToDevice, s) ||
+        cudaStreamSynchronize(s))
+        return QG_ERR_CUDA;
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0)) return QG_ERR_CUDA;
+    if (cudaEventCreate(&e1)) {
+        cudaEventDestroy(e0);
+        return QG_ERR_CUDA;
+    }
+    int r = QG_OK;
+    for (int use = 0; use < 2 && r == QG_OK; ++use) {
+        p->cl_use = use != 0;
+        r = qg_step(p, qd, prm, 1200.0, 1, QG_SCHEME_SSPRK3, 0, s);
+        if (r == QG_OK && cudaEventRecord(e0, s)) r = QG_ERR_CUDA;
+        if (r == QG_OK) r = qg_step(p, qd, prm, 1200.0, 4, QG_SCHEME_SSPRK3, 0, s);
+        float ms = -1.f;
+        if (r == QG_OK && (cudaEventRecord(e1, s) || cudaEventSynchronize(e1) || cudaEventElapsedTime(&ms, e0, e1)))
+            r = QG_ERR_CUDA;
+        p->tune_engine_ms[use] = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    p->cl_use = r == QG_OK && p->tune_engine_ms[1] >= 0.f && p->tune_engine_ms[1] < p->tune_engine_ms[0];
+    int flags = 0;
+    if (r == QG_OK) qg_status(p, &flags, s);  // clear what the timing runs left
+    return r;
+}
+
+}  // namespace

@@ -162,11 +162,30 @@ def _stream_handle(device) -> C.c_void_p:
     return C.c_void_p(torch.cuda.current_stream(device).cuda_stream)
 
 
+def lsweep_classes(spec, rows: int) -> set:
+    """Strip classes of a member's layer-per-warp sweep items with ``rows``-row strips: 0 =
+    every column and row the strip reads strictly inside the member, 1 = edge strip, 2 =
+    masked member (one kernel launch per class and layer count present)."""
+    if spec.mask is not None:
+        return {2}
+    Ny, Nx = spec.ny + 2, spec.nx + 2
+    out = set()
+    for sy in range((Ny + rows - 1) // rows):
+        for sx in range((Nx + 59) // 60):
+            x0, jb = 60 * sx, rows * sy
+            rhi = min(jb + rows, Ny) + 1
+            out.add(0 if (x0 - 2 >= 1 and x0 + 61 <= Nx - 2 and jb - 2 >= 1 and rhi <= Ny - 2) else 1)
+    return out
+
+
 class Plan:
     """Owns a ``qg_plan`` (device constants + workspace) on one CUDA device."""
 
     def __init__(self, members: Sequence["MemberSpec"], precision="fp32", refine=0, use_graphs=True,
-                 device=None, persistent=True, autotune=True, stencil=None, gemm_tile=None):
+                 device=None, persistent=True, autotune=True, stencil=None, gemm_tile=None, cluster=None):
+        """``cluster``: cluster-resident stepping of small members (``step`` with Heun / SSP-RK3 in
+        one launch per call): None = when the autotuner times it faster, True = whenever the
+        members allow it, False = never."""
         if not torch.cuda.is_available():
             raise RuntimeError("somax_gb300 needs a CUDA device (no CPU fallback)")
         self.device = torch.device(device or "cuda", torch.cuda.current_device()) if device is None \
@@ -177,7 +196,7 @@ class Plan:
             m.fill(arr[i])
         forced = 0 if stencil is None else 1 + self.STENCIL_VARIANTS.index(stencil)
         opts = Options(PRECISIONS[precision], int(refine), int(bool(use_graphs)), int(bool(persistent)),
-                       int(bool(autotune)), forced, int(gemm_tile or 0))
+                       int(bool(autotune)), forced, int(gemm_tile or 0), 0 if cluster is None else (1 if cluster else 2))
         handle = C.c_void_p()
         with torch.cuda.device(self.device):
             check(L.qg_plan_create(arr, len(members), C.byref(opts), C.byref(handle)), "qg_plan_create")
@@ -300,11 +319,20 @@ class Plan:
         stages = {"euler": 1, "heun": 2, "ssprk3": 3, "tsit5": 6}[scheme]
         butcher = scheme in ("euler", "tsit5")
         masked = any(m.mask is not None for m in self.members)
+        if self.engine()["cluster_ctas"] and not butcher:
+            return 1  # the cluster-resident step kernel, every stage of every step
         if self.persistent and self.precision != "fp32" and self.refine == 0 and not butcher and not masked:
             return 3  # pack, the persistent step kernel, unpack
-        # the column-sweep stencils launch once per distinct layer count
-        sweep = "sweep" in self.tuning()["stencil"]
-        stencil = len({m.n_layers for m in self.members}) if sweep else 1
+        # the column-sweep stencils launch once per distinct layer count, the layer-per-warp
+        # sweep once per distinct (layer count, strip class)
+        variant = self.tuning()["stencil"]
+        if variant.startswith("lsweep"):
+            rows = int(variant[len("lsweep"):])
+            stencil = len({(m.n_layers, c) for m in self.members for c in lsweep_classes(m, rows)})
+        elif "sweep" in variant:
+            stencil = len({m.n_layers for m in self.members})
+        else:
+            stencil = 1
         solve = 4 * (1 + self.refine) + self.refine
         inversion = solve
         if masked:  # capacitance correction(s), each followed by a solve
@@ -328,6 +356,16 @@ class Plan:
                 "ms": {name: round(float(t), 5) for name, t in zip(self.STENCIL_VARIANTS, ms)},
                 "gemm_tile_n": bn.value,
                 "gemm_ms": {w: round(float(t), 5) for w, t in zip((144, 80, 48, 32, 16), gms)}}
+
+    def engine(self) -> dict:
+        """The stepping engine of ``step`` (Heun / SSP-RK3): the cluster size of the cluster-
+        resident engine (0: the multi-launch path) and the autotuner's time (ms) of four SSP-RK3
+        steps with each."""
+        n = C.c_int()
+        ms = (C.c_float * 2)()
+        check(self._L.qg_plan_engine(self._h, C.byref(n), ms, 2), "qg_plan_engine")
+        return {"cluster_ctas": n.value, "ms": {"multi_launch": round(float(ms[0]), 5),
+                                                "cluster": round(float(ms[1]), 5)}}
 
     def set_profiling(self, on: bool):
         check(self._L.qg_set_profiling(self._h, int(on)), "qg_set_profiling")
@@ -417,7 +455,7 @@ class _QGBase(SomaxModel):
     barotropic = False
 
     def __init__(self, spec: MemberSpec, params: QGParams, precision="fp32", refine=0, use_graphs=True,
-                 strat=None, modal=None, persistent=True, stencil=None, gemm_tile=None):
+                 strat=None, modal=None, persistent=True, stencil=None, gemm_tile=None, cluster=None):
         self.spec = spec
         self.params = params
         self.precision = precision
@@ -426,6 +464,7 @@ class _QGBase(SomaxModel):
         self.persistent = persistent
         self.stencil = stencil
         self.gemm_tile = gemm_tile
+        self.cluster = cluster
         self.strat = strat
         self.modal = modal
         self.grid = Grid(spec.nx, spec.ny, spec.Lx, spec.Ly)
@@ -439,7 +478,7 @@ class _QGBase(SomaxModel):
         key = device.index
         if key not in self._plans:
             self._plans[key] = Plan([self.spec], self.precision, self.refine, self.use_graphs, device, self.persistent,
-                                    stencil=self.stencil, gemm_tile=self.gemm_tile)
+                                    stencil=self.stencil, gemm_tile=self.gemm_tile, cluster=self.cluster)
         return self._plans[key]
 
     @property
@@ -608,7 +647,8 @@ class BaroclinicQG(_QGBase):
                H=(400.0, 1100.0, 2600.0), g_prime=(9.81, 0.025, 0.0125), stratification=None,
                lateral_viscosity=0.0, bottom_drag=0.0, wind_amplitude=0.0, wind_profile="doublegyre",
                poisson_bc="dst", biharmonic_viscosity=0.0, precision="fp32", refine=0, eigs="consistent",
-               use_graphs=True, persistent=True, stencil=None, gemm_tile=None, mask=None) -> "BaroclinicQG":
+               use_graphs=True, persistent=True, stencil=None, gemm_tile=None, mask=None,
+               cluster=None) -> "BaroclinicQG":
         """``BaroclinicQG.create`` (``baroclinic.py:230-332``) with the same keyword arguments,
         plus ``biharmonic_viscosity`` (extension), ``precision`` of the DST-I GEMMs
         ("fp32", "tf32", "bf16x3"), ``refine`` sweeps, the ``eigs`` mode and whether ``step`` runs
@@ -627,7 +667,8 @@ class BaroclinicQG(_QGBase):
                           eigs, modal, mask)
         params = QGParams(*(torch.tensor(float(v)) for v in (lateral_viscosity, bottom_drag, wind_amplitude,
                                                              biharmonic_viscosity)))
-        return BaroclinicQG(spec, params, precision, refine, use_graphs, strat, modal, persistent, stencil, gemm_tile)
+        return BaroclinicQG(spec, params, precision, refine, use_graphs, strat, modal, persistent, stencil, gemm_tile,
+                            cluster)
 
     @property
     def n_layers(self):
@@ -644,13 +685,13 @@ class BarotropicQG(_QGBase):
     def create(nx=64, ny=64, Lx=1e6, Ly=1e6, f0=1e-4, beta=1.6e-11, lateral_viscosity=0.0,
                bottom_drag=0.0, wind_amplitude=0.0, wind_profile="doublegyre", biharmonic_viscosity=0.0,
                precision="fp32", refine=0, use_graphs=True, persistent=True, stencil=None,
-               gemm_tile=None, mask=None) -> "BarotropicQG":
+               gemm_tile=None, mask=None, cluster=None) -> "BarotropicQG":
         """``BarotropicQG.create`` (``barotropic.py:186-248``)."""
         spec = MemberSpec(nx, ny, Lx, Ly, f0, beta, [1.0], [1.0], True, wind_profile, mask=mask)
         params = QGParams(*(torch.tensor(float(v)) for v in (lateral_viscosity, bottom_drag, wind_amplitude,
                                                              biharmonic_viscosity)))
         return BarotropicQG(spec, params, precision, refine, use_graphs, persistent=persistent, stencil=stencil,
-                            gemm_tile=gemm_tile)
+                            gemm_tile=gemm_tile, cluster=cluster)
 
 
 class QGEnsemble:
@@ -659,12 +700,12 @@ class QGEnsemble:
     tensor-core precisions).  States are packed member after member in the reference layout."""
 
     def __init__(self, models: Sequence[_QGBase], precision="bf16x3", refine=0, use_graphs=True, persistent=True,
-                 device=None, stencil=None, gemm_tile=None):
+                 device=None, stencil=None, gemm_tile=None, cluster=None):
         if not models:
             raise ValueError("an ensemble needs at least one member")
         self.models = list(models)
         self.plan = Plan([m.spec for m in self.models], precision, refine, use_graphs, device, persistent,
-                         stencil=stencil, gemm_tile=gemm_tile)
+                         stencil=stencil, gemm_tile=gemm_tile, cluster=cluster)
         self.offsets = self.plan.offsets
         self.sizes = [int(np.prod(m.shape)) for m in self.models]
 

@@ -25,7 +25,8 @@ def member(n, nl, seed, precision="bf16x3", persistent=True, nu4=1e9, tau=1e-10)
     g = (9.81, 0.025, 0.0125, 0.01, 0.008)[:nl] if nl > 1 else (0.0055,)
     m = sg.BaroclinicQG.create(nx=n[0], ny=n[1], Lx=2e6, Ly=1.8e6, n_layers=nl, H=H, g_prime=g,
                                lateral_viscosity=50.0, bottom_drag=1e-7, wind_amplitude=tau,
-                               biharmonic_viscosity=nu4, precision=precision, persistent=persistent)
+                               biharmonic_viscosity=nu4, precision=precision, persistent=persistent,
+                               cluster=False)
     o = O.baroclinic_model(nx=n[0], ny=n[1], Lx=2e6, Ly=1.8e6, H=H, g_prime=g, lateral_viscosity=50.0,
                            bottom_drag=1e-7, wind_amplitude=tau, biharmonic_viscosity=nu4)
     k = tc.kminus3_field(max(n), seed, nl)[:, : n[1] + 2, : n[0] + 2] * 1e-6

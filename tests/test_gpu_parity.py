@@ -133,10 +133,11 @@ def test_step(scheme, nx, ny, nl):
 
 def test_step_graph_and_eager_agree():
     m, _ = pair(30, 30, 3, nu=100.0, tau=1e-10)
+    m.cluster = False  # both through the multi-launch path
     q = cuda(field((3, 32, 32), 7))
     a = m.step(sg.BaroclinicQGState(q=q), 1200.0, 4, "ssprk3").q
     m2 = sg.BaroclinicQG.create(nx=30, ny=30, Lx=2e6, Ly=1.6e6, n_layers=3, lateral_viscosity=100.0,
-                                wind_amplitude=1e-10, use_graphs=False)
+                                wind_amplitude=1e-10, use_graphs=False, cluster=False)
     b = m2.step(sg.BaroclinicQGState(q=q), 1200.0, 4, "ssprk3").q
     assert torch.equal(a, b)
 
@@ -267,7 +268,7 @@ def test_invert_tensor_cores(precision, refine, nx, ny, nl):
 def test_config2_tensor_cores_10_steps(precision, refine):
     cfg = tc.C2
     kw = cfg.model_kwargs()
-    m = sg.BaroclinicQG.create(**kw, precision=precision, refine=refine)
+    m = sg.BaroclinicQG.create(**kw, precision=precision, refine=refine, cluster=False)
     _, o = _config_pair(cfg)
     q0 = tc.initial_pv(cfg, seed=0)
     q10 = m.step(sg.BaroclinicQGState(q=cuda(q0)), cfg.dt, 10, cfg.scheme).q
