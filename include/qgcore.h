@@ -167,6 +167,17 @@ int qg_rhs_vjp(qg_plan* plan, const float* q, const float* params, const float* 
                float* params_bar, int flags, void* stream);
 int qg_invert_vjp(qg_plan* plan, const float* psi_bar, float* q_bar, void* stream);
 
+/* Geostrophic projection P = G (Q G)^-1 Q of a multilayer shallow-water state (h, u, v), each a
+   packed field like q (device pointers): ReparameterizedQG.project
+   (somax/_src/models/qg/reparameterized.py:142-178).  Q: q = curl(u, v) - f0 (h - H) / H with
+   the vorticity at the C-grid corner points; (Q G)^-1: the plan's modal Helmholtz inversion
+   (as qg_invert); G: (u_g, v_g) = grad_perp(psi) at the u / v points and
+   h_g = H (1 + f0 Cm2l diag(eig) Cl2m psi) with eig = lambda / f0^2.  psi (may be NULL)
+   receives the streamfunction.  Baroclinic unmasked members (QG_ERR_UNSUPPORTED otherwise);
+   the plan's stage planes serve as scratch, so calls on one plan are not concurrent. */
+int qg_project(qg_plan* plan, const float* h, const float* u, const float* v, float* h_g, float* u_g,
+               float* v_g, float* psi, void* stream);
+
 /* Kinetic energy and enstrophy per layer: ke, ens each sum(n_layers) floats (device). */
 int qg_diagnose(qg_plan* plan, const float* q, float* ke, float* ens, void* stream);
 

@@ -7,4 +7,5 @@ from .qg import (  # noqa: F401
     BarotropicQG, BarotropicQGDiagnostics, BarotropicQGParams, BarotropicQGState, Euler, Heun,
     MemberSpec, Plan, QGDiagnostics, QGEnsemble, QGParams, SaveAt, Solution, SomaxModel, State, Tsit5,
 )
+from .reparameterized import MultilayerSW2DState, ReparameterizedQG, ReparamQGGeostrophy  # noqa: F401
 from .transforms import ModalTransform, StratificationProfile  # noqa: F401

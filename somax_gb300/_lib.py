@@ -90,6 +90,7 @@ def lib() -> C.CDLL:
         "qg_plan_tuning": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_float), C.c_int]),
         "qg_plan_gemm_tuning": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_float), C.c_int]),
         "qg_plan_engine": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_float), C.c_int]),
+        "qg_project": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -24,6 +24,8 @@ struct MemberDev {
     float inv_12dxdy;  // 1 / (12 dx dy): Arakawa normalisation
     float beta_12dx;   // beta / (12 dx): the beta-term of J(psi, beta y) for a linear beta y
     float invH0;       // 1 / H[0] (1 for barotropic)
+    float f0;          // Coriolis parameter
+    float H[kMaxLayers];  // layer thicknesses (the geostrophic projection)
     float Cl2m[kMaxLayers * kMaxLayers];
     float Cm2l[kMaxLayers * kMaxLayers];
     float lam[kMaxLayers];  // f0^2 * eig
@@ -206,6 +208,12 @@ cudaError_t launch_diag_acc(const MemberDev* members, const StencilTile* tiles, 
                             const float* q, const float* psi_hat, double* acc, cudaStream_t s);
 cudaError_t launch_diag_finish(const double* acc, int64_t n_layers, float* ke, float* ens,
                                cudaStream_t s);
+// geostrophic projection of a shallow-water state (h, u, v): the PV q in front of the
+// inversion, then (h_g, u_g, v_g) from psi
+cudaError_t launch_project_q(const MemberDev* members, const StencilTile* tiles, int ntiles, int large,
+                             const float* h, const float* u, const float* v, float* q, cudaStream_t s);
+cudaError_t launch_project_g(const MemberDev* members, const StencilTile* tiles, int ntiles, int large,
+                             const float* psi, float* hg, float* ug, float* vg, cudaStream_t s);
 cudaError_t launch_residual(const MemberDev* members, const StencilTile* tiles, int ntiles, int large,
                             const float* qm, const float* psi_hat, void* out, int out_fmt,
                             int64_t xplane, cudaStream_t s, bool pdl);

@@ -158,6 +158,8 @@ void member_constants(const qg_member_desc& d, MemberDev& M, double* Cl2m, doubl
     M.inv_12dxdy = (float)(1.0 / (12.0 * dx * dy));
     M.beta_12dx = (float)(d.beta / (12.0 * dx));
     M.invH0 = d.barotropic ? 1.f : (float)(1.0 / d.H[0]);
+    M.f0 = (float)d.f0;
+    for (int l = 0; l < d.n_layers && !d.barotropic; ++l) M.H[l] = (float)d.H[l];
     const int n = d.n_layers;
     if (d.barotropic) {
         Cl2m[0] = Cm2l[0] = 1.0;
@@ -1163,6 +1165,28 @@ int qg_invert(qg_plan* p, const float* q, float* psi, void* stream) {
         e = timed(p, QG_K_OTHER, s, [&] {
             return launch_mode_to_layer(p->md, p->st_tiles, p->n_st, p->st_large, p->XC, psi, s, use_pdl(p));
         });
+    return cuda_err(e);
+}
+
+int qg_project(qg_plan* p, const float* h, const float* u, const float* v, float* h_g, float* u_g, float* v_g,
+               float* psi, void* stream) {
+    if (!p || !h || !u || !v || !h_g || !u_g || !v_g) return QG_ERR_NULL;
+    if (p->n_cap > 0) return QG_ERR_UNSUPPORTED;
+    for (const MemberDev& M : p->mh)
+        if (M.barotropic) return QG_ERR_UNSUPPORTED;
+    cudaStream_t s = (cudaStream_t)stream;
+    // the PV and psi in two of the Butcher stage planes (caller packing)
+    float* q = p->K;
+    float* ps = psi ? psi : p->K + p->state_size;
+    cudaError_t e = timed(p, QG_K_OTHER, s, [&] {
+        return launch_project_q(p->md, p->st_tiles, p->n_st, p->st_large, h, u, v, q, s);
+    });
+    if (e) return cuda_err(e);
+    const int r = qg_invert(p, q, ps, stream);
+    if (r != QG_OK) return r;
+    e = timed(p, QG_K_OTHER, s, [&] {
+        return launch_project_g(p->md, p->st_tiles, p->n_st, p->st_large, ps, h_g, u_g, v_g, s);
+    });
     return cuda_err(e);
 }
 

@@ -136,6 +136,78 @@ __global__ void __launch_bounds__(NTHREADS) k_mode_to_layer(const MemberDev* __r
 }
 
 // ---------------------------------------------------------------------------------------
+// Geostrophic projection of a multilayer shallow-water state (h, u, v) around one modal
+// Helmholtz inversion (ReparameterizedQG.project, reparameterized.py:142-178), all fields in
+// the caller's packing on the Arakawa C-grid of the arrays (u at the east faces, v at the
+// north faces, vorticity and the streamfunction's corner points at index (j, i) of the
+// north-east corner of T-cell (j, i)):
+//   k_project_q: q = zeta - f0 (h - H_l) / H_l with zeta = (v[j][i+1] - v[j][i]) / dx
+//                - (u[j+1][i] - u[j][i]) / dy on interior cells, 0 on the ring
+//   k_project_g: u_g = -(psi[j][i] - psi[j-1][i]) / dy, v_g = (psi[j][i] - psi[j][i-1]) / dx
+//                on interior cells (0 on the ring), h_g = H_l (1 + f0 (Cm2l diag(eig) Cl2m
+//                psi)_l) with eig_m = lambda_m / f0^2 everywhere
+// The curl of grad_perp is then the 5-point Laplacian, so Q G is the Helmholtz operator the
+// inversion solves and the projection is idempotent up to the ring.
+// ---------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(NTHREADS) k_project_q(const MemberDev* __restrict__ members,
+                                                        const StencilTile* __restrict__ tiles, int TX, int TY,
+                                                        const float* __restrict__ h, const float* __restrict__ u,
+                                                        const float* __restrict__ v, float* __restrict__ q) {
+    __shared__ MemberDev M;
+    const StencilTile t = tiles[blockIdx.x];
+    load_member(&M, members + t.member);
+    __syncthreads();
+    pdl_wait();
+    pdl_launch_dependents();
+    const float idx = 1.f / M.dx, idy = 1.f / M.dy;
+    for (int c = threadIdx.x; c < TX * TY; c += blockDim.x) {
+        const int j = t.ty * TY + c / TX, i = t.tx * TX + c % TX;
+        if (j >= M.Ny || i >= M.Nx) continue;
+        const bool ring = on_ring(j, i, M.Ny, M.Nx);
+        for (int l = 0; l < M.nl; ++l) {
+            const int64_t o = caller_idx(M, l, j, i);
+            float zeta = 0.f;
+            if (!ring) zeta = (v[o + 1] - v[o]) * idx - (u[o + M.Nx] - u[o]) * idy;
+            q[o] = zeta - M.f0 * ((h[o] - M.H[l]) / M.H[l]);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(NTHREADS) k_project_g(const MemberDev* __restrict__ members,
+                                                        const StencilTile* __restrict__ tiles, int TX, int TY,
+                                                        const float* __restrict__ psi, float* __restrict__ hg,
+                                                        float* __restrict__ ug, float* __restrict__ vg) {
+    __shared__ MemberDev M;
+    const StencilTile t = tiles[blockIdx.x];
+    load_member(&M, members + t.member);
+    __syncthreads();
+    pdl_wait();
+    pdl_launch_dependents();
+    const int nl = M.nl;
+    const float idx = 1.f / M.dx, idy = 1.f / M.dy, if0 = 1.f / M.f0;
+    for (int c = threadIdx.x; c < TX * TY; c += blockDim.x) {
+        const int j = t.ty * TY + c / TX, i = t.tx * TX + c % TX;
+        if (j >= M.Ny || i >= M.Nx) continue;
+        const bool ring = on_ring(j, i, M.Ny, M.Nx);
+        float p[kMaxLayers], pm[kMaxLayers];
+        for (int l = 0; l < nl; ++l) p[l] = psi[caller_idx(M, l, j, i)];
+        for (int m = 0; m < nl; ++m) {
+            float s = 0.f;
+            for (int k = 0; k < nl; ++k) s = fmaf(M.Cl2m[m * kMaxLayers + k], p[k], s);
+            pm[m] = s * (M.lam[m] * if0);  // f0 eig_m (Cl2m psi)_m
+        }
+        for (int l = 0; l < nl; ++l) {
+            const int64_t o = caller_idx(M, l, j, i);
+            float a = 0.f;
+            for (int m = 0; m < nl; ++m) a = fmaf(M.Cm2l[l * kMaxLayers + m], pm[m], a);
+            hg[o] = fmaf(M.H[l], a, M.H[l]);  // H + H a: the anomaly rounds once
+            ug[o] = ring ? 0.f : -(p[l] - psi[o - M.Nx]) * idy;
+            vg[o] = ring ? 0.f : (p[l] - psi[o - 1]) * idx;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------
 // Helmholtz residual in modal space for one refinement sweep:
 //   r_m = qm_m - (lap_full psi_hat_m - lam_m psi_hat_m)
 // where lap_full is the full-array 5-point operator with zeros outside the array (the
@@ -291,6 +363,18 @@ cudaError_t launch_mode_to_layer(const MemberDev* members, const StencilTile* ti
                                  const float* psi_hat, float* psi, cudaStream_t s, bool pdl) {
     return launch_k(k_mode_to_layer, ntiles, NTHREADS, 0, s, pdl, members, tiles, large ? TileL::TX : TileS::TX,
                     large ? TileL::TY : TileS::TY, psi_hat, psi);
+}
+
+cudaError_t launch_project_q(const MemberDev* members, const StencilTile* tiles, int ntiles, int large,
+                             const float* h, const float* u, const float* v, float* q, cudaStream_t s) {
+    return launch_k(k_project_q, ntiles, NTHREADS, 0, s, false, members, tiles, large ? TileL::TX : TileS::TX,
+                    large ? TileL::TY : TileS::TY, h, u, v, q);
+}
+
+cudaError_t launch_project_g(const MemberDev* members, const StencilTile* tiles, int ntiles, int large,
+                             const float* psi, float* hg, float* ug, float* vg, cudaStream_t s) {
+    return launch_k(k_project_g, ntiles, NTHREADS, 0, s, false, members, tiles, large ? TileL::TX : TileS::TX,
+                    large ? TileL::TY : TileS::TY, psi, hg, ug, vg);
 }
 
 cudaError_t launch_residual(const MemberDev* members, const StencilTile* tiles, int ntiles, int large,
