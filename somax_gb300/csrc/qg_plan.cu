@@ -215,8 +215,13 @@ const char* kErrStr[] = {"ok", "null pointer", "bad shape", "CUDA error", "non-f
 
 }  // namespace
 
+// Captured steps of qg_step: one step, and kGraphSteps steps in one graph, so that the
+// kernels of consecutive steps chain with programmatic dependent launch instead of draining
+// the GPU at every graph boundary.
+constexpr int kGraphSteps = 8;
 struct StepGraph {
-    cudaGraphExec_t exec = nullptr;
+    cudaGraphExec_t exec = nullptr;    // one step
+    cudaGraphExec_t exec_k = nullptr;  // kGraphSteps steps
     double dt = 0.0;
     int scheme = -1;
 };
@@ -1128,6 +1133,7 @@ void qg_plan_destroy(qg_plan* p) {
     if (!p) return;
     cudaDeviceSynchronize();
     if (p->graph.exec) cudaGraphExecDestroy(p->graph.exec);
+    if (p->graph.exec_k) cudaGraphExecDestroy(p->graph.exec_k);
     for (auto& v : p->ev)
         for (auto& pr : v) {
             cudaEventDestroy(pr.first);
@@ -1256,28 +1262,36 @@ int qg_step(qg_plan* p, float* q, const float* params, double dt, int n_steps, i
         for (int k = 0; k < n_steps && !e; ++k) e = run_one_step(p, p->params, (float)dt, scheme, s);
     } else if (n_steps > 0) {
         StepGraph& g = p->graph;
-        if (!g.exec || g.dt != dt || g.scheme != scheme) {
-            if (g.exec) {
-                cudaGraphExecDestroy(g.exec);
-                g.exec = nullptr;
-            }
-            cudaGraph_t graph = nullptr;
-            e = cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal);
-            if (!e) {
-                cudaError_t e1 = run_one_step(p, p->params, (float)dt, scheme, p->cap);
-                e = cudaStreamEndCapture(p->cap, &graph);
-                if (!e) e = e1;
-            }
-            if (!e) e = cudaGraphInstantiate(&g.exec, graph, 0);
-            if (graph) cudaGraphDestroy(graph);
-            if (e) {
-                g.exec = nullptr;
-                return cuda_err(e);
-            }
+        if (g.dt != dt || g.scheme != scheme) {
+            for (cudaGraphExec_t* x : {&g.exec, &g.exec_k})
+                if (*x) {
+                    cudaGraphExecDestroy(*x);
+                    *x = nullptr;
+                }
             g.dt = dt;
             g.scheme = scheme;
         }
-        for (int k = 0; k < n_steps && !e; ++k) e = cudaGraphLaunch(g.exec, s);
+        // capture `steps` consecutive steps into *out
+        auto capture = [&](int steps, cudaGraphExec_t* out) {
+            cudaGraph_t graph = nullptr;
+            cudaError_t ec = cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal);
+            if (!ec) {
+                cudaError_t e1 = cudaSuccess;
+                for (int k = 0; k < steps && !e1; ++k) e1 = run_one_step(p, p->params, (float)dt, scheme, p->cap);
+                ec = cudaStreamEndCapture(p->cap, &graph);
+                if (!ec) ec = e1;
+            }
+            if (!ec) ec = cudaGraphInstantiate(out, graph, 0);
+            if (graph) cudaGraphDestroy(graph);
+            if (ec) *out = nullptr;
+            return ec;
+        };
+        int left = n_steps;
+        if (left >= kGraphSteps && !g.exec_k) e = capture(kGraphSteps, &g.exec_k);
+        for (; left >= kGraphSteps && !e; left -= kGraphSteps) e = cudaGraphLaunch(g.exec_k, s);
+        if (!e && left > 0 && !g.exec) e = capture(1, &g.exec);
+        for (; left > 0 && !e; --left) e = cudaGraphLaunch(g.exec, s);
+        if (e) return cuda_err(e);
     }
     if (!e)
         e = timed(p, QG_K_OTHER, s, [&] {
