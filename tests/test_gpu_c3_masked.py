@@ -6,7 +6,7 @@ the float64 direct sparse solve and the Helmholtz relative residual over the oce
 The residual of any psi stored in FP32 has a floor: rounding psi to FP32 perturbs lap(psi) by
 ~1e-7 |psi| / dx^2, which for the barotropic mode (lam = 0, psi ~ q (L / pi)^2) is ~1e-2 of
 |q| at N = 514.  The floor is measured here as the residual of the float64 solution rounded to
-FP32, and the GPU's residual is judged against it.
+FP32, and the GPU's residual is compared with it.
 
 Measured on GB300 (modes 0, 1, 2): split-BF16x3 + refinement: error 5.2e-7, 1.3e-6, 3.8e-6,
 residual 2.5x, 1.7x, 1.7x the floor; TF32 + refinement: error 4.1e-4, 8.4e-6, 8.1e-6.

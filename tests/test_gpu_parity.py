@@ -3,7 +3,7 @@
 Tolerances (relative L2 against float64):
   * PV inversion psi and single-step RHS: RTOL_INV / RTOL_RHS (FP32 arithmetic; the RHS
     differences amplify the inversion's rounding by the stencil's cancellation)
-  * state after 1 and 10 steps: RTOL_STEP = 1e-5, the benchmark spec's bound on q after 10 steps
+  * state after 1 and 10 steps: RTOL_STEP = 1e-5, the accuracy target for q after 10 steps
 """
 
 import numpy as np
