@@ -103,9 +103,11 @@ class QGParams:
     biharmonic_viscosity: torch.Tensor
 
     def vector(self, device) -> torch.Tensor:
-        return torch.stack([torch.as_tensor(v, dtype=torch.float32, device=device).reshape(())
-                            for v in (self.lateral_viscosity, self.bottom_drag, self.wind_amplitude,
-                                      self.biharmonic_viscosity)])
+        vals = (self.lateral_viscosity, self.bottom_drag, self.wind_amplitude, self.biharmonic_viscosity)
+        if any(isinstance(v, torch.Tensor) and v.requires_grad for v in vals):
+            # keep the autograd connection to the parameters
+            return torch.stack([torch.as_tensor(v, dtype=torch.float32, device=device).reshape(()) for v in vals])
+        return torch.tensor([float(v) for v in vals], dtype=torch.float32).to(device)  # one copy
 
 
 BaroclinicQGParams = QGParams
@@ -715,7 +717,11 @@ class QGEnsemble:
 
     def params(self, device=None) -> torch.Tensor:
         device = device or self.plan.device
-        return torch.cat([m._param_vector(device) for m in self.models])
+        ts = [t for m in self.models for t in m._param_tensors()]
+        if any(isinstance(t, torch.Tensor) and t.requires_grad for t in ts):
+            return torch.cat([m._param_vector(device) for m in self.models])
+        # every member's parameters in one host-to-device copy
+        return torch.tensor([float(t) for t in ts], dtype=torch.float32).to(device)
 
     def pack(self, qs: Sequence[torch.Tensor]) -> torch.Tensor:
         if len(qs) != len(self.models):
