@@ -195,6 +195,24 @@ def describe(name):
                           f"{cfg.scheme} dt={cfg.dt:g}s, {steps} steps = 1 model day per bench step")
 
 
+def max_over_ranks(x: float, world: int, device) -> float:
+    """The largest of every rank's x: a multi-rank job takes as long as its slowest rank."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world: int, n_members: int, steps: int, seconds: float) -> float:
+    """Member-days per second of the whole job: every rank advances its own replica of
+    n_members members by one model day per bench step."""
+    return world * n_members * steps / seconds
+
+
 def run_reference(args):
     """The reference's CPU path (its JAX code cannot be installed here): the float32
     NumPy/SciPy restatement on every host core, each bench step a bounded time sample."""
@@ -436,13 +454,9 @@ def main():
         torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
-    dev_ms = sum(a.elapsed_time(b) for a, b in ev)
-    t = torch.tensor([dev_ms], device=dev, dtype=torch.float64)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    dev_ms = float(t.item())
+    dev_ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in ev), world, dev)
     ms_per_step = dev_ms / args.steps
-    value = world * W.n_members * args.steps / (dev_ms / 1000.0)
+    value = whole_job_rate(world, W.n_members, args.steps, dev_ms / 1000.0)
     status = plan.status(dev)
 
     # ---- e2e: public API with pinned host buffers --------------------------------------
@@ -456,11 +470,8 @@ def main():
     for _ in range(args.steps):
         W.host_step(qh, out)
         torch.cuda.current_stream(dev).synchronize()
-    e2e_s = time.perf_counter() - t0
-    t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    e2e_value = world * W.n_members * args.steps / float(t.item())
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world, dev)
+    e2e_value = whole_job_rate(world, W.n_members, args.steps, e2e_s)
     qbytes = qh.numel() * 4
 
     # ---- launches per bench step (graph / persistent replay counts every kernel) ---------
