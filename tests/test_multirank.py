@@ -37,7 +37,7 @@ def _rank(rank, world, port, out):
 
 def test_two_gloo_ranks_time_is_the_slowest_rank():
     port = _free_port()
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:  # no fork from a threaded process
         out = m.dict()
         mp.spawn(_rank, args=(2, port, out), nprocs=2, join=True)
         res = dict(out)
