@@ -1,0 +1,67 @@
+"""Host logic of the benchmark and of the launch accounting, on CPU: the roofline of every
+kernel class (the multi-launch classes, and the cluster engine's single launch) from
+synthetic per-class timings, and the layer-per-warp sweep's strip classes that decide how
+many kernels a step launches."""
+
+import os
+import sys
+import types
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+import bench  # noqa: E402
+from somax_gb300.qg import lsweep_classes  # noqa: E402
+
+
+def workload(members):
+    w = types.SimpleNamespace(members=members)
+    w.cells = lambda: sum(nl * N * N for N, nl in members)
+    w.gemm_flops_per_pass = lambda: sum(2.0 * nl * N ** 3 for N, nl in members)
+    return w
+
+
+def test_roofline_multi_launch_classes():
+    W = workload([(130, 3)])
+    lc = 3 * 130 * 130
+    # class: (total ms, launches); the DST passes dominate
+    stats = {0: (0.01, 1), 1: (8.0, 800), 2: (2.0, 200), 3: (0.01, 1), 4: (0.0, 0)}
+    r = bench.roofline(W, stats, "bf16x3", "baroclinic3_128")
+    assert r["kernel"] == "dst_gemm" and r["bound"] == "hbm"
+    assert r["algorithmic_bytes_per_launch"] == 8.0 * lc
+    assert r["avg_launch_us"] == pytest.approx(10.0)
+    assert r["achieved"] == pytest.approx(8.0 * lc / 10e-6 / 1e9)
+    assert r["frac"] == pytest.approx(r["achieved"] / bench.peaks()["hbm_gbs"])
+    assert set(r["kernels"]) == {"prep", "dst_gemm", "rhs_stencil", "other"}
+
+
+def test_roofline_cluster_engine_single_launch():
+    """With the cluster engine only class 4 has timings: it is reported as the cluster
+    kernel with the state in and out once per launch (8 B per layer-cell)."""
+    W = workload([(66, 1)])
+    stats = {k: (0.0, 0) for k in range(4)}
+    stats[4] = (0.7, 1)
+    r = bench.roofline(W, stats, "bf16x3", "barotropic_64", cluster=True)
+    assert r["kernel"] == "cluster"
+    assert r["algorithmic_bytes_per_launch"] == 8.0 * 66 * 66
+    assert set(r["kernels"]) == {"cluster"}
+
+
+class Spec(types.SimpleNamespace):
+    pass
+
+
+@pytest.mark.parametrize("nx,ny,rows,expected", [
+    (128, 128, 16, {0, 1}),   # 130 wide: strips 0, 1 (interior rows), 2 (10 columns)
+    (64, 64, 16, {1}),        # 66 wide: both strips touch the edge
+    (256, 256, 64, {0, 1}),
+    (3, 5, 16, {1}),
+])
+def test_lsweep_strip_classes(nx, ny, rows, expected):
+    assert lsweep_classes(Spec(nx=nx, ny=ny, mask=None), rows) == expected
+
+
+def test_lsweep_masked_member_is_its_own_class():
+    assert lsweep_classes(Spec(nx=30, ny=30, mask=object()), 16) == {2}
