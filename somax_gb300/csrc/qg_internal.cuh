@@ -197,6 +197,9 @@ int lsweep_blocks_per_sm(int nl, int cls);
 // items / n_items / grid: kMaxLayers * kLSweepClasses groups, group (nl - 1) * kLSweepClasses + class
 cudaError_t launch_lsweep(const StencilArgs& a, const SweepItem* const* items, const int* n_items, int R,
                           const int* grid, cudaStream_t s, bool pdl);
+// one (layer count, strip class) group g of launch_lsweep
+cudaError_t launch_lsweep_group(const StencilArgs& a, const SweepItem* items, int n_items, int R, int grid, int g,
+                                cudaStream_t s, bool pdl);
 
 // launchers (return cudaError_t of the launch)
 cudaError_t launch_prep(const PrepArgs& a, int ntiles, cudaStream_t s, bool pdl);

@@ -575,17 +575,21 @@ int lsweep_blocks_per_sm(int nl, int cls) {
 // with g / kLSweepClasses + 1 layers.  Strip heights must be multiples of 16 (the walk's
 // compile-time ring slots assume the first ingested row is 6 mod 8) and at most 64 (the wind
 // profile of a strip is held in two registers per lane).
+cudaError_t launch_lsweep_group(const StencilArgs& a, const SweepItem* items, int n_items, int R, int grid, int g,
+                                cudaStream_t s, bool pdl) {
+    if (R <= 0 || R % 16 != 0 || R > 64 || g < 0 || g >= kMaxLayers * kLSweepClasses) return cudaErrorInvalidValue;
+    if (!lsweep_init()) return cudaErrorInvalidValue;
+    if (n_items <= 0) return cudaSuccess;
+    const int n = g / kLSweepClasses;
+    return launch_k(kLSweep[g], grid, lsweep_groups(n + 1) * (n + 1) * 32, kLSweepSmem[n], s, pdl, a, items, n_items,
+                    R);
+}
+
 cudaError_t launch_lsweep(const StencilArgs& a, const SweepItem* const* items, const int* n_items, int R,
                           const int* grid, cudaStream_t s, bool pdl) {
-    if (R <= 0 || R % 16 != 0 || R > 64) return cudaErrorInvalidValue;
-    if (!lsweep_init()) return cudaErrorInvalidValue;
     cudaError_t e = cudaSuccess;
     for (int g = 0; g < kMaxLayers * kLSweepClasses && !e; ++g)
-        if (n_items[g] > 0) {
-            const int n = g / kLSweepClasses;
-            e = launch_k(kLSweep[g], grid[g], lsweep_groups(n + 1) * (n + 1) * 32, kLSweepSmem[n], s, pdl, a,
-                         items[g], n_items[g], R);
-        }
+        if (n_items[g] > 0) e = launch_lsweep_group(a, items[g], n_items[g], R, grid[g], g, s, pdl);
     return e;
 }
 

@@ -297,6 +297,12 @@ struct qg_plan {
     PersistArgs pa{};         // constant part of the tensor-core launches' arguments
     // graphs
     cudaStream_t cap = nullptr;
+    // the layer-per-warp sweep's (layer count, strip class) launches are independent: they run
+    // as parallel branches on these streams (forked from and joined into the stage's stream)
+    static constexpr int kSide = 4;
+    cudaStream_t side[kSide] = {};
+    cudaEvent_t fork_ev = nullptr;
+    cudaEvent_t join_ev[kSweepGroups] = {};
     StepGraph graph;
     // profiling
     bool profiling = false;
@@ -497,7 +503,28 @@ cudaError_t launch_stencil(qg_plan* p, StencilArgs a, cudaStream_t s, bool pdl) 
         const int v = p->sw_sel;
         const SweepItem* items[kSweepGroups];
         for (int k = 0; k < kSweepGroups; ++k) items[k] = p->sw_items_v[v] + p->sw_off[v][k];
-        if (v >= 3) return launch_lsweep(a, items, p->sw_cnt[v], kSweepRows[v % 3], p->sw_grid, s, pdl);
+        if (v >= 3) {
+            int groups[kSweepGroups], n = 0;
+            for (int g = 0; g < kSweepGroups; ++g)
+                if (p->sw_cnt[v][g] > 0) groups[n++] = g;
+            if (n <= 1 || !p->fork_ev)
+                return launch_lsweep(a, items, p->sw_cnt[v], kSweepRows[v % 3], p->sw_grid, s, pdl);
+            // fork: the first group on the stage's stream (after the last DST pass, with
+            // programmatic dependent launch), the others on side streams after an event; join
+            // them all back before the stage's next launch
+            cudaError_t e = cudaEventRecord(p->fork_ev, s);
+            for (int i = 0; i < n && !e; ++i) {
+                const int g = groups[i];
+                cudaStream_t ss = i == 0 ? s : p->side[(i - 1) % qg_plan::kSide];
+                if (i > 0) e = cudaStreamWaitEvent(ss, p->fork_ev, 0);
+                if (!e)
+                    e = launch_lsweep_group(a, items[g], p->sw_cnt[v][g], kSweepRows[v % 3], p->sw_grid[g], g, ss,
+                                            i == 0 && pdl);
+                if (!e && i > 0) e = cudaEventRecord(p->join_ev[i], ss);
+            }
+            for (int i = 1; i < n && !e; ++i) e = cudaStreamWaitEvent(s, p->join_ev[i], 0);
+            return e;
+        }
         // the one-layer-per-lane sweep: class 0 of each layer count
         const SweepItem* it1[kMaxLayers];
         int cnt1[kMaxLayers], grid1[kMaxLayers];
@@ -1102,6 +1129,12 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
         }
     }
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);
+    for (int i = 0; i < qg_plan::kSide && e == cudaSuccess; ++i)
+        e = cudaStreamCreateWithFlags(&p->side[i], cudaStreamNonBlocking);
+    for (int i = 0; i < kSweepGroups && e == cudaSuccess; ++i)
+        e = cudaEventCreateWithFlags(&p->join_ev[i], cudaEventDisableTiming);
+    // the fork event last: its presence switches the sweep's groups to parallel branches
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->fork_ev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e == cudaSuccess && o.cluster != 2) {
         // cluster-resident stepping: every member alike in layers and grid, no land
@@ -1140,6 +1173,11 @@ void qg_plan_destroy(qg_plan* p) {
             cudaEventDestroy(pr.second);
         }
     if (p->cap) cudaStreamDestroy(p->cap);
+    for (cudaStream_t x : p->side)
+        if (x) cudaStreamDestroy(x);
+    if (p->fork_ev) cudaEventDestroy(p->fork_ev);
+    for (cudaEvent_t x : p->join_ev)
+        if (x) cudaEventDestroy(x);
     for (void* a : p->allocs) cudaFree(a);
     delete p;
 }
