@@ -1115,8 +1115,15 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
         a.bar_count = p->bar;
         a.bar_gen = p->bar + 1;
         select_tile(p, p->st_large);
+        // side streams for the sweep's parallel branches, before the autotuner times them
+        for (int i = 0; i < qg_plan::kSide && e == cudaSuccess; ++i)
+            e = cudaStreamCreateWithFlags(&p->side[i], cudaStreamNonBlocking);
+        for (int i = 0; i < kSweepGroups && e == cudaSuccess; ++i)
+            e = cudaEventCreateWithFlags(&p->join_ev[i], cudaEventDisableTiming);
+        // the fork event last: its presence switches the sweep's groups to parallel branches
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->fork_ev, cudaEventDisableTiming);
         // a forced choice (qg_options.gemm_tile / .stencil) skips that half of the autotuner
-        if (o.autotune && tc && !o.gemm_tile) e = autotune_gemm(p);
+        if (!e && o.autotune && tc && !o.gemm_tile) e = autotune_gemm(p);
         if (!e && tc && o.gemm_tile)
             for (int v = 0; v < kNumBN; ++v)
                 if (kGemmBN[v] == o.gemm_tile) select_gemm(p, v);
@@ -1129,12 +1136,6 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
         }
     }
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);
-    for (int i = 0; i < qg_plan::kSide && e == cudaSuccess; ++i)
-        e = cudaStreamCreateWithFlags(&p->side[i], cudaStreamNonBlocking);
-    for (int i = 0; i < kSweepGroups && e == cudaSuccess; ++i)
-        e = cudaEventCreateWithFlags(&p->join_ev[i], cudaEventDisableTiming);
-    // the fork event last: its presence switches the sweep's groups to parallel branches
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->fork_ev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e == cudaSuccess && o.cluster != 2) {
         // cluster-resident stepping: every member alike in layers and grid, no land
