@@ -189,14 +189,36 @@ int qg_diagnose(qg_plan* plan, const float* q, float* ke, float* ens, void* stre
    (ny+2) * round_up(nx+2, 32) <= 2^20 (and the same with x and y swapped); larger members
    return QG_ERR_TOO_LARGE.  All calls on a device share that scratch, so calls that
    overlap on the GPU race; serialise them.  The first call on each device looks up the
-   scratch address (cudaGetSymbolAddress); make it before any stream capture. */
+   scratch address (cudaGetSymbolAddress), and so does the first call in a new context of
+   that device (after cudaDeviceReset); make those calls before any stream capture. */
 int qg_invert_static(const qg_member_desc* member, const float* q, float* psi, void* stream);
+
+/* State statistics of the runner's chunk log (somax/_src/cli/_run.py:408-432,
+   _state_diagnostics): stats[0..3] = min, mean and max over the finite entries of the packed
+   field q and the number of non-finite entries (device pointer, 4 doubles; NaN for min /
+   mean / max when no entry is finite).  Reduced on the device, no host scan. */
+int qg_state_stats(qg_plan* plan, const float* q, double* stats, void* stream);
 
 /* Device-side status: synchronises the stream, returns QG_OK or QG_ERR_NONFINITE /
    QG_ERR_TIMEOUT, writes the raw flag word to *flags (may be NULL) and clears it. */
 int qg_status(qg_plan* plan, int* flags, void* stream);
 
 const char* qg_strerror(int code);
+
+/* Clock64 cycles that a CTA of the persistent step kernel waits at its grid barrier before it
+   gives up (the launch then sets the time-out flag that qg_status reports as QG_ERR_TIMEOUT,
+   and every CTA drains its copies in flight and returns).  0 restores the default of about
+   2 s; the waits on TMA and tensor-core completions keep that default.  Counterpart of the
+   runner's divergence guard (somax/_src/cli/_run.py:671-686): a wait that cannot end is
+   reported, never left to hang the device.  Takes effect on the next qg_step. */
+int qg_plan_set_wait_limit(qg_plan* plan, int64_t cycles);
+
+/* The layer-per-warp sweep launches one kernel per (layer count, strip class) group; by
+   default (on = 1) a stage forks them onto plan-owned side streams as parallel branches and
+   joins them before the next DST pass.  on = 0 launches them one after another on the call's
+   stream (same arithmetic, same result bit for bit).  Discards the captured step graphs.
+   No reference counterpart: a switch of this library's launch schedule. */
+int qg_plan_set_parallel_sweep(qg_plan* plan, int on);
 
 /* Per-kernel-class timing with CUDA events recorded on the launch stream around every
    launch while profiling is on (graphs are bypassed then).  Used by the benchmark to turn

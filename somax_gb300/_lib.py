@@ -91,6 +91,9 @@ def lib() -> C.CDLL:
         "qg_plan_gemm_tuning": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_float), C.c_int]),
         "qg_plan_engine": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_float), C.c_int]),
         "qg_project": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+        "qg_plan_set_wait_limit": (C.c_int, [vp, i64]),
+        "qg_state_stats": (C.c_int, [vp, vp, vp, vp]),
+        "qg_plan_set_parallel_sweep": (C.c_int, [vp, C.c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

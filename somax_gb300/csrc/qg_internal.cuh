@@ -209,6 +209,9 @@ cudaError_t launch_mode_to_layer(const MemberDev* members, const StencilTile* ti
                                  const float* psi_hat, float* psi, cudaStream_t s, bool pdl);
 cudaError_t launch_diag_acc(const MemberDev* members, const StencilTile* tiles, int ntiles, int large,
                             const float* q, const float* psi_hat, double* acc, cudaStream_t s);
+// min / mean / max of the finite entries and the non-finite count of n floats into out[0..3]
+// (device doubles); acc: 32 bytes of device scratch
+cudaError_t launch_state_stats(const float* q, int64_t n, void* acc, double* out, int grid, cudaStream_t s);
 cudaError_t launch_diag_finish(const double* acc, int64_t n_layers, float* ke, float* ens,
                                cudaStream_t s);
 // geostrophic projection of a shallow-water state (h, u, v): the PV q in front of the
@@ -285,8 +288,9 @@ struct PersistArgs {
     int n_stages, n_steps;
     float sa[4], sb[4], dt;   // Shu-Osher stage coefficients
     int* flags;
-    unsigned* bar_count;      // grid barrier: arrivals, generation
+    unsigned* bar_count;      // grid barrier: arrivals, generation (zeroed before every launch)
     unsigned* bar_gen;
+    long long bar_wait;       // clock64 cycles a CTA waits at the grid barrier before giving up
 };
 size_t persistent_smem_bytes(int precision, int max_nl, int large, PersistArgs* a);
 cudaError_t persistent_init();

@@ -41,9 +41,10 @@ __device__ __forceinline__ void red_release_add(unsigned* p, unsigned v) {
 __device__ __forceinline__ void proxy_fence_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
 __device__ __forceinline__ void proxy_fence_shared() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-// Grid-wide barrier with a bounded spin.  Returns false (and flags the abort) on timeout or
-// when this CTA already aborted.
-__device__ bool grid_sync(unsigned* count, unsigned* gen, int* flags, volatile int* abort) {
+// Grid-wide barrier with a spin bounded by `wait` clock64 cycles.  Returns false (and flags the
+// abort) on timeout or when this CTA already aborted.  A CTA that gives up leaves its arrival
+// in *count, so the host zeroes both words before the next launch.
+__device__ bool grid_sync(unsigned* count, unsigned* gen, int* flags, volatile int* abort, long long wait) {
     __syncthreads();
     if (threadIdx.x == 0) {
         bool ok = !*abort;
@@ -58,7 +59,7 @@ __device__ bool grid_sync(unsigned* count, unsigned* gen, int* flags, volatile i
             } else {
                 const long long t0 = clock64();
                 while (ld_acquire(gen) == g) {
-                    if (clock64() - t0 > kTimeoutCycles) {
+                    if (clock64() - t0 > wait) {
                         ok = false;
                         break;
                     }
@@ -333,15 +334,15 @@ __global__ void __launch_bounds__(PT, 1) k_persistent(PersistArgs a) {
     for (int step = 0; step < a.n_steps; ++step) {
         for (int k = 0; k < a.n_stages; ++k) {
             gemm_phase<PREC, G1_FWD_X>(a, smem, sh, tmem, c);
-            if (!grid_sync(a.bar_count, a.bar_gen, a.flags, abort)) goto done;
+            if (!grid_sync(a.bar_count, a.bar_gen, a.flags, abort, a.bar_wait)) goto done;
             gemm_phase<PREC, G2_FWD_Y>(a, smem, sh, tmem, c);
-            if (!grid_sync(a.bar_count, a.bar_gen, a.flags, abort)) goto done;
+            if (!grid_sync(a.bar_count, a.bar_gen, a.flags, abort, a.bar_wait)) goto done;
             gemm_phase<PREC, G3_INV_X>(a, smem, sh, tmem, c);
-            if (!grid_sync(a.bar_count, a.bar_gen, a.flags, abort)) goto done;
+            if (!grid_sync(a.bar_count, a.bar_gen, a.flags, abort, a.bar_wait)) goto done;
             gemm_phase<PREC, G4_INV_Y>(a, smem, sh, tmem, c);
-            if (!grid_sync(a.bar_count, a.bar_gen, a.flags, abort)) goto done;
+            if (!grid_sync(a.bar_count, a.bar_gen, a.flags, abort, a.bar_wait)) goto done;
             stencil_phase<T>(a, k, smem, sh, c);
-            if (!grid_sync(a.bar_count, a.bar_gen, a.flags, abort)) goto done;
+            if (!grid_sync(a.bar_count, a.bar_gen, a.flags, abort, a.bar_wait)) goto done;
         }
     }
 done:

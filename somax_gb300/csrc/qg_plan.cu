@@ -12,6 +12,7 @@
 #include <new>
 #include <vector>
 
+#include "qg_device.cuh"
 #include "qg_internal.cuh"
 
 namespace qg {
@@ -270,6 +271,7 @@ struct qg_plan {
     size_t cap_smem = 0;
     int* flags = nullptr;
     double* diag_acc = nullptr;
+    void* stats_acc = nullptr;  // qg_state_stats accumulators (32 bytes)
     double* vjp_acc = nullptr;  // parameter cotangents of qg_rhs_vjp (QG_NPARAMS per member)
     int op_fmt = FMT_F32;
     void* tc_maps = nullptr;  // TMA descriptors of the tensor-core GEMMs
@@ -303,6 +305,7 @@ struct qg_plan {
     cudaStream_t side[kSide] = {};
     cudaEvent_t fork_ev = nullptr;
     cudaEvent_t join_ev[kSweepGroups] = {};
+    bool fork_on = true;  // qg_plan_set_parallel_sweep: 0 launches the groups one after another
     StepGraph graph;
     // profiling
     bool profiling = false;
@@ -507,7 +510,7 @@ cudaError_t launch_stencil(qg_plan* p, StencilArgs a, cudaStream_t s, bool pdl) 
             int groups[kSweepGroups], n = 0;
             for (int g = 0; g < kSweepGroups; ++g)
                 if (p->sw_cnt[v][g] > 0) groups[n++] = g;
-            if (n <= 1 || !p->fork_ev)
+            if (n <= 1 || !p->fork_ev || !p->fork_on)
                 return launch_lsweep(a, items, p->sw_cnt[v], kSweepRows[v % 3], p->sw_grid, s, pdl);
             // fork: the first group on the stage's stream (after the last DST pass, with
             // programmatic dependent launch), the others on side streams after an event; join
@@ -1065,6 +1068,7 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
             !(e = dalloc(p, &p->flags, 16)) && !(e = dalloc(p, &p->bar, 16)))
             e = dalloc(p, &p->diag_acc, (size_t)2 * p->total_layers * sizeof(double));
         if (!e) e = dalloc(p, &p->vjp_acc, (size_t)n_members * QG_NPARAMS * sizeof(double));
+        if (!e) e = dalloc(p, (uint8_t**)&p->stats_acc, 64);
         if (!e && o.refine_sweeps > 0) e = dalloc(p, &p->XQ, xb);
         if (!e) e = dalloc(p, &p->K, (size_t)6 * p->state_size * sizeof(float));  // Tsit5: 6 stages
     }
@@ -1114,6 +1118,7 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
         a.flags = p->flags;
         a.bar_count = p->bar;
         a.bar_gen = p->bar + 1;
+        a.bar_wait = kTimeoutCycles;
         select_tile(p, p->st_large);
         // side streams for the sweep's parallel branches, before the autotuner times them
         for (int i = 0; i < qg_plan::kSide && e == cudaSuccess; ++i)
@@ -1296,7 +1301,10 @@ int qg_step(qg_plan* p, float* q, const float* params, double dt, int n_steps, i
         a.n_steps = n_steps;
         a.g4_accumulate = 0;
         const int grid = std::max(1, std::min(p->n_sm, std::max(p->n_st, std::max(p->n_gx, p->n_gy))));
-        e = timed(p, QG_K_PERSISTENT, s, [&] { return launch_persistent(a, grid, p->opts.dst_precision, s); });
+        // a launch that gave up at a grid barrier leaves arrivals behind: start from zero
+        e = cudaMemsetAsync(p->bar, 0, 2 * sizeof(unsigned), s);
+        if (!e)
+            e = timed(p, QG_K_PERSISTENT, s, [&] { return launch_persistent(a, grid, p->opts.dst_precision, s); });
     } else if (!use_graph) {
         for (int k = 0; k < n_steps && !e; ++k) e = run_one_step(p, p->params, (float)dt, scheme, s);
     } else if (n_steps > 0) {
@@ -1396,6 +1404,14 @@ int qg_diagnose(qg_plan* p, const float* q, float* ke, float* ens, void* stream)
     return cuda_err(e);
 }
 
+int qg_state_stats(qg_plan* p, const float* q, double* stats, void* stream) {
+    if (!p || !q || !stats) return QG_ERR_NULL;
+    const int grid = std::max(1, std::min(p->n_sm * 4, (int)((p->state_size / 4 + 255) / 256)));
+    return cuda_err(timed(p, QG_K_OTHER, (cudaStream_t)stream, [&] {
+        return launch_state_stats(q, p->state_size, p->stats_acc, stats, grid, (cudaStream_t)stream);
+    }));
+}
+
 int qg_status(qg_plan* p, int* flags, void* stream) {
     if (!p) return QG_ERR_NULL;
     cudaStream_t s = (cudaStream_t)stream;
@@ -1409,6 +1425,29 @@ int qg_status(qg_plan* p, int* flags, void* stream) {
     if (h & 2) return QG_ERR_TIMEOUT;
     if (h & 4) return QG_ERR_CUDA;  // a kernel met a work item it was not built for and skipped it
     if (h & 1) return QG_ERR_NONFINITE;
+    return QG_OK;
+}
+
+int qg_plan_set_parallel_sweep(qg_plan* p, int on) {
+    if (!p) return QG_ERR_NULL;
+    if (on != 0 && on != 1) return QG_ERR_ARG;
+    if (p->fork_on != (on == 1)) {
+        p->fork_on = on == 1;
+        // the captured graphs hold the old launch structure
+        cudaDeviceSynchronize();
+        for (cudaGraphExec_t* x : {&p->graph.exec, &p->graph.exec_k})
+            if (*x) {
+                cudaGraphExecDestroy(*x);
+                *x = nullptr;
+            }
+    }
+    return QG_OK;
+}
+
+int qg_plan_set_wait_limit(qg_plan* p, int64_t cycles) {
+    if (!p) return QG_ERR_NULL;
+    if (cycles < 0) return QG_ERR_ARG;
+    p->pa.bar_wait = cycles == 0 ? kTimeoutCycles : (long long)cycles;
     return QG_OK;
 }
 

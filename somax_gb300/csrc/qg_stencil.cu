@@ -326,6 +326,101 @@ __global__ void k_diag_finish(const double* __restrict__ acc, int64_t n, float* 
 }
 
 // ---------------------------------------------------------------------------------------
+// State statistics of the runner: min / mean / max over the finite entries of a packed
+// field and the count of non-finite ones, reduced on the device (one atomic per block).
+// acc: [0] min and [1] max as order-preserving ints, [2] the finite sum (double, in acc_d),
+// [3] finite and [4] non-finite counts.
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ int ordered_int(float f) {
+    const int i = __float_as_int(f);
+    return i >= 0 ? i : i ^ 0x7fffffff;
+}
+__device__ __forceinline__ float from_ordered(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
+
+struct StatsAcc {
+    int mn, mx;
+    double sum;
+    unsigned long long n_finite, n_bad;
+};
+
+__global__ void k_stats_init(StatsAcc* acc) {
+    acc->mn = ordered_int(INFINITY);
+    acc->mx = ordered_int(-INFINITY);
+    acc->sum = 0.0;
+    acc->n_finite = acc->n_bad = 0ull;
+}
+
+__global__ void __launch_bounds__(256) k_stats(const float* __restrict__ q, int64_t n, StatsAcc* acc) {
+    float mn = INFINITY, mx = -INFINITY;
+    double sum = 0.0;
+    unsigned long long nf = 0, nb = 0;
+    auto take = [&](float v) {
+        if (isfinite(v)) {
+            mn = fminf(mn, v);
+            mx = fmaxf(mx, v);
+            sum += (double)v;
+            ++nf;
+        } else {
+            ++nb;
+        }
+    };
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+    const bool vec = (reinterpret_cast<uintptr_t>(q) & 15) == 0;
+    const int64_t n4 = vec ? n / 4 : 0;
+    for (int64_t i = tid; i < n4; i += nth) {
+        const float4 v = __ldg(reinterpret_cast<const float4*>(q) + i);
+        take(v.x);
+        take(v.y);
+        take(v.z);
+        take(v.w);
+    }
+    for (int64_t i = 4 * n4 + tid; i < n; i += nth) take(q[i]);
+    for (int o = 16; o > 0; o >>= 1) {
+        mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        nf += __shfl_xor_sync(0xffffffffu, nf, o);
+        nb += __shfl_xor_sync(0xffffffffu, nb, o);
+    }
+    __shared__ StatsAcc part[8];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) part[w] = {ordered_int(mn), ordered_int(mx), sum, nf, nb};
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        StatsAcc b = part[0];
+        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
+            b.mn = min(b.mn, part[k].mn);
+            b.mx = max(b.mx, part[k].mx);
+            b.sum += part[k].sum;
+            b.n_finite += part[k].n_finite;
+            b.n_bad += part[k].n_bad;
+        }
+        atomicMin(&acc->mn, b.mn);
+        atomicMax(&acc->mx, b.mx);
+        atomicAdd(&acc->sum, b.sum);
+        atomicAdd(&acc->n_finite, b.n_finite);
+        atomicAdd(&acc->n_bad, b.n_bad);
+    }
+}
+
+__global__ void k_stats_finish(const StatsAcc* acc, double* out) {
+    const bool any = acc->n_finite > 0;
+    out[0] = any ? (double)from_ordered(acc->mn) : NAN;
+    out[1] = any ? acc->sum / (double)acc->n_finite : NAN;
+    out[2] = any ? (double)from_ordered(acc->mx) : NAN;
+    out[3] = (double)acc->n_bad;
+}
+
+cudaError_t launch_state_stats(const float* q, int64_t n, void* acc, double* out, int grid, cudaStream_t s) {
+    StatsAcc* a = static_cast<StatsAcc*>(acc);
+    cudaError_t e = launch_k(k_stats_init, 1, 1, 0, s, false, a);
+    if (!e) e = launch_k(k_stats, grid, 256, 0, s, false, q, n, a);
+    if (!e) e = launch_k(k_stats_finish, 1, 1, 0, s, false, (const StatsAcc*)a, out);
+    return e;
+}
+
+// ---------------------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------------------
 // 3-D boxes (BX, BY, nl) over a member's x-row planes: dims (Nx, Ny, nl), row pitch Px.

@@ -309,6 +309,15 @@ class Plan:
                                   C.c_void_p(en.data_ptr()), _stream_handle(q.device)), "qg_diagnose")
         return ke, en
 
+    def state_stats(self, q: torch.Tensor) -> torch.Tensor:
+        """(min, mean, max) over the finite entries of the packed field q and the count of its
+        non-finite entries, as a float64 device tensor of 4 values (``qg_state_stats``)."""
+        self._check_field(q, "q")
+        out = torch.empty(4, device=q.device, dtype=torch.float64)
+        check(self._L.qg_state_stats(self._h, C.c_void_p(q.data_ptr()), C.c_void_p(out.data_ptr()),
+                                     _stream_handle(q.device)), "qg_state_stats")
+        return out
+
     def status(self, device=None) -> int:
         flags = C.c_int(0)
         code = self._L.qg_status(self._h, C.byref(flags), _stream_handle(device or self.device))
@@ -368,6 +377,16 @@ class Plan:
         check(self._L.qg_plan_engine(self._h, C.byref(n), ms, 2), "qg_plan_engine")
         return {"cluster_ctas": n.value, "ms": {"multi_launch": round(float(ms[0]), 5),
                                                 "cluster": round(float(ms[1]), 5)}}
+
+    def set_wait_limit(self, cycles: int = 0):
+        """Clock64 cycles the persistent step kernel waits at a grid barrier before it gives
+        up and reports QG_ERR_TIMEOUT through ``status`` (0: the default, about 2 s)."""
+        check(self._L.qg_plan_set_wait_limit(self._h, int(cycles)), "qg_plan_set_wait_limit")
+
+    def set_parallel_sweep(self, on: bool = True):
+        """Launch the layer-per-warp sweep's (layer count, strip class) groups as parallel
+        graph branches (default) or one after another on the call's stream."""
+        check(self._L.qg_plan_set_parallel_sweep(self._h, int(bool(on))), "qg_plan_set_parallel_sweep")
 
     def set_profiling(self, on: bool):
         check(self._L.qg_set_profiling(self._h, int(on)), "qg_set_profiling")
