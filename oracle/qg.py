@@ -526,3 +526,16 @@ def diagnose(m: QGModel, q: np.ndarray) -> dict:
     return dict(psi=psi, u=u, v=v, kinetic_energy=ke, enstrophy=ens,
                 total_kinetic_energy=np.sum(ke), total_enstrophy=np.sum(ens),
                 relative_vorticity=laplacian(psi, g.dx, g.dy))
+
+
+def integrate_and_compare(case: dict) -> float:
+    """Process-pool worker of the ensemble parity tests: integrates one member in float64 and
+    returns the interior relative L2 distance of ``case["got"]`` from it.  ``case`` holds the
+    keyword arguments of ``baroclinic_model`` (``model``), the initial PV (``q0``), ``dt``,
+    ``n_steps``, ``scheme`` and the state to check (``got``)."""
+    set_workers(case.get("workers", 1))
+    m = baroclinic_model(**case["model"])
+    ref = integrate(m, np.asarray(case["q0"], np.float64), case["dt"], case["n_steps"], case["scheme"])
+    got = np.asarray(case["got"], np.float64)
+    s = (Ellipsis, slice(1, -1), slice(1, -1))
+    return float(np.linalg.norm(got[s] - ref[s]) / np.linalg.norm(ref[s]))

@@ -21,8 +21,11 @@
 // every plane element before reading it, so nothing left by an earlier call is read.
 //
 // First call on a device: the host looks up the array's device address with
-// cudaGetSymbolAddress (once per device, with that device current) and caches it.  Make
-// that first call outside any stream capture.
+// cudaGetSymbolAddress (once per device and context, with that device current) and caches
+// it together with the context's unique id.  Make that first call outside any stream
+// capture.  A later call in a new context of the device (after cudaDeviceReset, whose
+// module reload can move the array) sees a different id and looks the address up again.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -56,19 +59,52 @@ static __device__ __align__(256) float g_qg_static_scratch[kScratchFloats];
 
 std::mutex g_mu;
 float* g_base[64] = {nullptr};
+unsigned long long g_ctx_id[64] = {0};
 
-// Device address of the scratch on the current device (looked up once per device).
+using CtxGetCurrent = CUresult (*)(CUcontext*);
+using CtxGetId = CUresult (*)(CUcontext, unsigned long long*);
+CtxGetCurrent g_ctx_current = nullptr;
+CtxGetId g_ctx_get_id = nullptr;
+bool g_ctx_fn_tried = false;
+
+// Unique id of the current context (0 when the driver cannot say; the address is then
+// looked up on every call).  Called with g_mu held.
+unsigned long long current_context_id() {
+    if (!g_ctx_fn_tried) {
+        g_ctx_fn_tried = true;
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1, q2;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+            q1 == cudaDriverEntryPointSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+            q2 == cudaDriverEntryPointSuccess && f1 && f2) {
+            g_ctx_current = reinterpret_cast<CtxGetCurrent>(f1);
+            g_ctx_get_id = reinterpret_cast<CtxGetId>(f2);
+        }
+    }
+    if (!g_ctx_current || !g_ctx_get_id) return 0;
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (g_ctx_current(&ctx) != CUDA_SUCCESS || !ctx || g_ctx_get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// Device address of the scratch on the current device, looked up once per device and
+// context.
 cudaError_t scratch_base(float** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_base[dev]) {
+    const unsigned long long id = current_context_id();
+    if (!g_base[dev] || id == 0 || id != g_ctx_id[dev]) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_qg_static_scratch);
         if (e != cudaSuccess) return e;
         g_base[dev] = static_cast<float*>(p);
+        g_ctx_id[dev] = current_context_id();  // the lookup made the device's context current
     }
     *out = g_base[dev];
     return cudaSuccess;

@@ -78,6 +78,26 @@ C4_MIX = (
 CONFIGS = {c.name: c for c in (C1, C2, C3_512, C3_1024, C5)}
 
 
+def c4_members(seed: int = 0) -> list:
+    """The 256 members of the configuration-4 ensemble in order: (config, tau0 in N/m^2,
+    PV seed) per member, tau0 drawn uniformly from 0.05-0.12 N/m^2 with a seeded generator.
+    Member k's initial PV is ``initial_pv(config, pv_seed)``."""
+    rng = np.random.default_rng(1000 + seed)
+    out = []
+    for count, cfg in C4_MIX:
+        for _ in range(count):
+            out.append((cfg, float(rng.uniform(0.05, 0.12)), 10000 * seed + len(out)))
+    return out
+
+
+def member_kwargs(cfg: QGConfig, tau0: float | None = None) -> dict:
+    """``model_kwargs`` of a configuration with the wind amplitude of ``tau0`` (N/m^2)."""
+    kw = cfg.model_kwargs()
+    if tau0 is not None:
+        kw["wind_amplitude"] = wind_amplitude(tau0, cfg.L)
+    return kw
+
+
 def kminus3_field(n: int, seed: int, nl: int = 1) -> np.ndarray:
     """(nl, n+2, n+2) float64 fields, zero ring, unit RMS interior, with power spectrum
     proportional to k^-3 over the interior DST-I wavenumbers."""
