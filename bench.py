@@ -1,16 +1,24 @@
-"""Benchmark of the GB300 QG time step: model-days per second.
+"""Benchmark of the GB300 QG time step: member-days (model-days) per second.
 
-One bench step = one model day of integration (86400 / dt time steps) of the 3-layer
-128x128 double-gyre basin with SSP-RK3 at dt = 1200 s (72 steps), run through libqgcore.
+Default workload (``--config ensemble256``): the 256-member ragged ensemble (96 one-layer 64^2,
+96 three-layer 128^2, 48 three-layer 256^2 and 16 five-layer 256^2 double gyres) advanced
+together by one plan with split-BF16x3 tensor-core DST passes.  One bench step = one model day
+of every member (72 SSP-RK3 steps at dt = 1200 s).  ``--config baroclinic3_128`` runs the single
+3-layer 128^2 basin instead.
 
-  value      model-days/s with the state resident in HBM (CUDA events around each bench
+  value      member-days/s with the state resident in HBM (CUDA events around each bench
              step, L2 flushed between steps), whole job over all ranks
+  vs_baseline  value / the plain FP32 single-member path on the same members: every member
+             advanced alone by its own FP32 plan (CUDA-core DST passes, no batching), one
+             qg_step call per member and model day, timed in the same run
   e2e        the same metric through the public API with the state in pinned host memory:
              every bench step copies q host->device, integrates one day, copies q back
-  roofline   achieved bandwidth / throughput of the dominant kernel class from CUDA-event
-             timing of every launch in a profiled pass, against MEASURED_PEAKS.json
+  roofline   achieved bandwidth / throughput of the dominant kernel class: each class's share
+             of a profiled pass (CUDA events around every launch) applied to the timed step,
+             against MEASURED_PEAKS.json; ``stencil_hbm`` is the stencil class's line
   cpu_baseline  the float32 NumPy/SciPy restatement of the reference's CPU path on a
-             bounded sample of the same workload (rank 0, N = 1 only)
+             bounded sample of the same workload (rank 0, N = 1 only); the same leg checks
+             parity: one member of each class after 10 steps against the float64 restatement
 
 ``--impl reference`` times that CPU restatement alone (the reference's JAX path cannot be
 installed here) and prints the same line with ``"impl": "reference"``.
@@ -36,7 +44,8 @@ sys.path.insert(0, ROOT)
 
 import numpy as np  # noqa: E402
 
-METRIC = "QG model-days/sec per GB300 (3-layer 128^2 double gyre, SSP-RK3 dt=1200 s)"
+# the headline metric of the reference's benchmark configurations, for every workload here
+METRIC = "QG model-days/sec per GB300 vs plain FP32 path at \u22641e-5 rel err; stencil HBM GB/s"
 UNIT = "model-days/s"
 
 
@@ -172,7 +181,6 @@ def ensemble_cpu_rate(threads: int, min_seconds: float = 10.0):
     return 256 * tc.C4_MIX[0][1].dt / 86400.0 / t_step, ", ".join(desc)
 
 
-ENSEMBLE_METRIC = "QG member-days/sec per GB300 (256-member ragged ensemble, SSP-RK3 dt=1200 s)"
 ENSEMBLE_DESC = ("ensemble256: 96 x 1-layer 64^2 (Rd 50 km) + 96 x 3-layer 128^2 + 48 x 3-layer 256^2 + "
                  "16 x 5-layer 256^2 double gyres, tau0 ~ U(0.05, 0.12) N/m^2, ssprk3 dt=1200s")
 
@@ -182,16 +190,15 @@ def describe(name):
     from somax_gb300 import testcases as tc
 
     if name == "ensemble256":
-        return ENSEMBLE_METRIC, "member-days/s", ENSEMBLE_DESC + ", 72 steps = 1 model day per bench step"
+        return METRIC, "member-days/s", ENSEMBLE_DESC + ", 72 steps = 1 model day per bench step"
     if name == "masked3_512":
-        return ("QG model-days/sec per GB300 (3-layer 512^2 masked basin, SSP-RK3 dt=1200 s)", UNIT,
+        return (METRIC, UNIT,
                 "masked3_512: 3-layer 512x512 double gyre (Lx=Ly=5120 km) with a seeded coastline (15 % of the "
                 "T-cells land, ring land), one FP32 refinement sweep, FP64 capacitance correction, ssprk3 "
                 "dt=1200s, 72 steps = 1 model day per bench step")
     cfg = tc.CONFIGS[name]
-    metric = METRIC if name == "baroclinic3_128" else f"QG model-days/sec per GB300 ({name})"
     steps = int(round(86400.0 / cfg.dt))
-    return metric, UNIT, (f"{name}: {cfg.nl}-layer {cfg.n}x{cfg.n} double gyre (Lx=Ly=5120 km), "
+    return METRIC, UNIT, (f"{name}: {cfg.nl}-layer {cfg.n}x{cfg.n} double gyre (Lx=Ly=5120 km), "
                           f"{cfg.scheme} dt={cfg.dt:g}s, {steps} steps = 1 model day per bench step")
 
 
@@ -262,19 +269,15 @@ class Workload:
         from somax_gb300 import testcases as tc
 
         self.name = name
-        rng = np.random.default_rng(1000 + seed)
+        self.c4 = None
         if name == "ensemble256":
             cfgs, models, q0s = [], [], []
-            k = 0
-            for count, cfg in tc.C4_MIX:
-                for _ in range(count):
-                    kw = cfg.model_kwargs()
-                    kw["wind_amplitude"] = tc.wind_amplitude(float(rng.uniform(0.05, 0.12)), cfg.L)
-                    models.append(sg.BaroclinicQG.create(**kw, precision=precision, persistent=persistent,
-                                                         cluster=cluster))
-                    q0s.append(tc.initial_pv(cfg, seed=10000 * seed + k).astype(np.float32))
-                    cfgs.append(cfg)
-                    k += 1
+            self.c4 = tc.c4_members(seed)
+            for cfg, tau0, pv_seed in self.c4:
+                models.append(sg.BaroclinicQG.create(**tc.member_kwargs(cfg, tau0), precision=precision,
+                                                     persistent=persistent, cluster=cluster))
+                q0s.append(tc.initial_pv(cfg, seed=pv_seed).astype(np.float32))
+                cfgs.append(cfg)
             self.ens = sg.QGEnsemble(models, precision=precision, persistent=persistent, device=dev, stencil=stencil,
                                      gemm_tile=gemm_tile, cluster=cluster)
             self.plan = self.ens.plan
@@ -337,8 +340,14 @@ def traffic_table():
         return json.load(f).get("bytes_per_launch", {})
 
 
-def roofline(W, stats, precision, name, cluster=False):
+def roofline(W, stats, precision, name, cluster=False, step_ms=None):
     """Roofline of every kernel class from the profiled pass's per-launch event times.
+
+    The profiled pass runs one bench step with CUDA events around every launch (graphs and
+    the sweep's parallel branches still on, but every launch bracketed), so its classes add
+    up to more than the timed step.  With ``step_ms`` (the timed bench step) each class's
+    time is its share of the profiled pass times ``step_ms``, and achieved = algorithmic
+    bytes per launch / (that time / launches).
 
     Algorithmic HBM bytes per launch, per layer-cell of every member (lc = sum nl Ny Nx):
       dst_gemm     one DST-I pass: operand in (4 B: FP32, or BF16 hi + lo) + result out (4 B)
@@ -358,10 +367,13 @@ def roofline(W, stats, precision, name, cluster=False):
         bytes_per[4] = 8.0 * lc
     flops_per = {1: W.gemm_flops_per_pass() * (3.0 if precision == "bf16x3" else 1.0)}
     traffic = traffic_table().get(name, {})
+    prof_total = sum(ms for ms, n in stats.values() if n)
+    scale = step_ms / prof_total if step_ms and prof_total > 0 else 1.0
     kernels = {}
     for k, (ms, n) in stats.items():
         if not n or k not in bytes_per:
             continue
+        ms = ms * scale
         avg_s = ms / 1000.0 / n
         gbs = bytes_per[k] / avg_s / 1e9
         ent = {"launches": n, "total_ms": ms, "avg_us": avg_s * 1e6, "bytes_per_launch": bytes_per[k],
@@ -390,17 +402,112 @@ def roofline(W, stats, precision, name, cluster=False):
                 "frac": d["hbm_frac"]}
     roof.update({"kernel": dom_name, "traffic": d["traffic"], "peak_src": pk["src"],
                  "algorithmic_bytes_per_launch": d["bytes_per_launch"], "avg_launch_us": d["avg_us"],
+                 "durations": ("each class's share of a profiled pass (CUDA events around every launch) "
+                               f"applied to the timed bench step: profiled {prof_total:.3f} ms, timed "
+                               f"{step_ms:.3f} ms per step" if step_ms else "profiled pass, unscaled"),
                  "kernels": kernels})
     return roof
+
+
+def plain_fp32_rate(dev, mix, repeats: int = 3):
+    """Member-days/s of the plain FP32 single-member path on a mix of (count, config).
+
+    One member of each class gets its own FP32 plan (DST passes on the CUDA cores, no
+    batching, the library's default engine choice for that member alone) and is advanced one
+    model day per ``qg_step`` call, timed with CUDA events on the launch stream (median of
+    ``repeats`` days after a warm day).  Looping the members one after another takes the
+    count-weighted sum of those days.  Returns (member-days/s, per-class details)."""
+    import torch
+
+    import somax_gb300 as sg
+    from somax_gb300 import testcases as tc
+
+    per_class, t_day, total = {}, 0.0, 0
+    for count, cfg in mix:
+        m = sg.BaroclinicQG.create(**cfg.model_kwargs(), precision="fp32")
+        plan = m.plan(dev)
+        params = m._param_vector(dev)
+        q0 = torch.tensor(tc.initial_pv(cfg, seed=0).astype(np.float32), device=dev).reshape(-1)
+        steps = int(round(86400.0 / cfg.dt))
+        q = q0.clone()
+        plan.step(q, params, cfg.dt, steps, cfg.scheme)  # warm: graph capture
+        ts = []
+        for _ in range(repeats):
+            q.copy_(q0)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            plan.step(q, params, cfg.dt, steps, cfg.scheme)
+            b.record()
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        if plan.status(dev) != 0:
+            raise RuntimeError(f"plain FP32 path flagged a device error on {cfg.name}")
+        ms = statistics.median(ts)
+        per_class[cfg.name] = {"members": count, "ms_per_model_day": ms,
+                               "engine": "cluster" if plan.engine()["cluster_ctas"] else "multi-launch",
+                               "stencil": plan.tuning()["stencil"]}
+        t_day += count * ms
+        total += count
+    return total * 1000.0 / t_day, per_class
+
+
+def parity_10_steps(W, dev, threads):
+    """Interior relative L2 of q after 10 steps against the float64 restatement (part of the
+    CPU-baseline leg): one member of each class of the ensemble, or the single basin.  The
+    GPU run starts from the bench's initial state on a copy, outside the timed region."""
+    import torch
+
+    from oracle import masked as OM
+    from oracle import qg as O
+    from somax_gb300 import testcases as tc
+
+    n_steps = 10
+    O.set_workers(threads)
+    q = torch.tensor(W.q0, device=dev).reshape(-1)
+    W.plan.step(q, W.params, W.dt, n_steps, W.scheme)
+    if W.plan.status(dev) != 0:
+        raise RuntimeError("parity run flagged a device error")
+    if W.ens is not None:
+        got = W.ens.unpack(q)
+        picks, seen = [], set()
+        for i, (cfg, tau0, _) in enumerate(W.c4):
+            if cfg.name not in seen:
+                seen.add(cfg.name)
+                picks.append((i, cfg, tc.member_kwargs(cfg, tau0)))
+        cases = [(f"member {i} ({cfg.name})", cfg, kw, got[i], W.q0[W.ens.offsets[i]:W.ens.offsets[i] + W.ens.sizes[i]],
+                  None) for i, cfg, kw in picks]
+    else:
+        masked = W.name == "masked3_512"
+        cfg = tc.CONFIGS["baroclinic3_512" if masked else W.name]
+        mask = tc.land_mask(cfg.n, cfg.n, frac=0.15, seed=0) if masked else None
+        cases = [(W.name, cfg, cfg.model_kwargs(), q.view(W.model.shape), W.q0, mask)]
+    out = {}
+    for label, cfg, kw, g, q0, mask in cases:
+        om = O.baroclinic_model(nx=cfg.n, ny=cfg.n, Lx=cfg.L, Ly=cfg.L, f0=kw["f0"], beta=kw["beta"], H=cfg.H,
+                                g_prime=cfg.g_prime, lateral_viscosity=cfg.lateral_viscosity,
+                                bottom_drag=cfg.bottom_drag, wind_amplitude=kw["wind_amplitude"],
+                                biharmonic_viscosity=cfg.biharmonic_viscosity)
+        q0 = np.asarray(q0, np.float64).reshape(g.shape)
+        if mask is None:
+            ref = O.integrate(om, q0, cfg.dt, n_steps, cfg.scheme)
+        else:
+            ref = OM.integrate(om, q0, mask, cfg.dt, n_steps, cfg.scheme)
+        gg = g.cpu().double().numpy()
+        sl = (Ellipsis, slice(1, -1), slice(1, -1))
+        out[label] = float(np.linalg.norm(gg[sl] - ref[sl]) / np.linalg.norm(ref[sl]))
+    return {"rel_l2_10_steps": out, "max": max(out.values()), "bound": 1e-5,
+            "against": "float64 NumPy/SciPy restatement of the reference (interior cells)"}
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="baroclinic3_128")
+    ap.add_argument("--config", default="ensemble256",
+                    help="ensemble256 (default) | baroclinic3_128 | barotropic_64 | baroclinic3_256 | "
+                         "baroclinic3_512 | baroclinic3_1024 | masked3_512")
     ap.add_argument("--precision", default="bf16x3", help="DST-I GEMM arithmetic: fp32 | tf32 | bf16x3")
     ap.add_argument("--persistent", type=int, default=0,
                     help="1: all steps of a call in one persistent cooperative launch (tensor-core precisions)")
@@ -483,12 +590,23 @@ def main():
     torch.cuda.synchronize()
     stats = {k: plan.kernel_stats(k) for k in range(5)}
     plan.set_profiling(False)
-    roof = roofline(W, stats, args.precision, args.config, plan.engine()["cluster_ctas"] > 0)
+    roof = roofline(W, stats, args.precision, args.config, plan.engine()["cluster_ctas"] > 0, ms_per_step)
+
+    # ---- the plain FP32 single-member path on the same members (the metric's baseline) ----
+    vs_baseline, plain = None, None
+    if args.config != "masked3_512":
+        mix = tc.C4_MIX if W.ens is not None else ((1, tc.CONFIGS[args.config]),)
+        plain_rate, plain_classes = plain_fp32_rate(dev, mix)
+        plain_rate *= world  # every rank loops its own replica of the members
+        vs_baseline = value / plain_rate
+        plain = {"value": plain_rate, "unit": W.unit, "per_class": plain_classes,
+                 "how": "each member advanced alone by its own FP32 plan (CUDA-core DST passes, no batching), "
+                        f"one qg_step call per member and model day, looped over the {W.n_members} member(s)"}
 
     line = {
         "metric": W.metric, "value": value, "unit": W.unit, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "vs_baseline": vs_baseline, "dtype": "f32", "data": "synthetic",
         "config": {"workload": W.describe,
                    "precision": args.precision, "persistent": bool(args.persistent),
                    "l2": "flushed between timed steps (256 MB write)",
@@ -497,6 +615,9 @@ def main():
         "e2e": {"value": e2e_value, "unit": W.unit, "h2d_bytes_per_step": qbytes, "d2h_bytes_per_step": qbytes,
                 "api": "BaroclinicQG.step / QGEnsemble.step_host with pinned host q -> qg_step"},
         "roofline": roof,
+        "stencil_hbm": ({"achieved_gbs": roof["kernels"]["rhs_stencil"]["achieved_gbs"],
+                         "peak_gbs": peaks()["hbm_gbs"], "frac": roof["kernels"]["rhs_stencil"]["hbm_frac"]}
+                        if "rhs_stencil" in roof["kernels"] else None),
         "gpu_launches": launches_per_day * args.steps,
         "clocks": clk.summary(),
     }
@@ -513,6 +634,11 @@ def main():
             v, desc = ensemble_cpu_rate(threads, 10.0)
             sample = f"one member per class, count-weighted: {desc}; float32 NumPy/SciPy restatement"
         line["cpu_baseline"] = {"value": v, "unit": W.unit, "cores": threads, "kind": "port", "sample": sample}
+        line["parity"] = parity_10_steps(W, dev, threads)
+    if plain is not None:
+        line["plain_fp32"] = plain
+        line["config"]["vs_baseline"] = ("value / plain_fp32.value: the same members on the plain FP32 "
+                                         "single-member path, timed in this run")
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
