@@ -59,3 +59,53 @@ def test_non_finite_state_aborts():
     with pytest.raises(runner.IntegrationDivergedError):
         runner.chunked_integrate_with_diagnostics(m, sg.BaroclinicQGState(q=q), [0.0, 2400.0, 4800.0], 1200.0,
                                                   solver="ssprk3", log=lambda s: None)
+
+
+@pytest.mark.gpu
+def test_state_stats_kernel_matches_host_reduction():
+    """qg_state_stats (min / mean / max over the finite entries, non-finite count) against the
+    same reduction in float64 on the host, with NaN and inf entries planted in the field."""
+    m, _, q0 = _model()
+    plan = m.plan()
+    q = torch.tensor(q0, dtype=torch.float32, device="cuda").reshape(-1)
+    q[5] = float("nan")
+    q[77] = float("inf")
+    q[-1] = float("-inf")
+    got = plan.state_stats(q).cpu().numpy()
+    h = q.cpu().double().numpy()
+    f = h[np.isfinite(h)]
+    assert got[0] == f.min() and got[2] == f.max() and got[3] == 3
+    assert abs(got[1] - f.mean()) <= 1e-12 * np.abs(f).max()
+    allbad = torch.full_like(q, float("nan"))
+    got = plan.state_stats(allbad).cpu().numpy()
+    assert np.isnan(got[:3]).all() and got[3] == q.numel()
+
+
+@pytest.mark.gpu
+def test_runner_writes_snapshots_and_restart(tmp_path):
+    """With output_dir the runner writes snapshots.zarr (the saved states, appended while the
+    run goes on) and final_state.zarr; restarting from final_state.zarr and running the second
+    half gives the bits of one run over both halves (``_run.py:346-364,840-862``)."""
+    from somax_gb300 import io as qio
+
+    m, _, q0 = _model()
+    dt = 1200.0
+    ts = [0.0, 4 * dt, 8 * dt]
+    s0 = sg.BaroclinicQGState(q=torch.tensor(q0, dtype=torch.float32, device="cuda"))
+    res = runner.chunked_integrate_with_diagnostics(m, s0, ts, dt, solver="ssprk3", log=lambda s: None,
+                                                    output_dir=tmp_path / "run", attrs={"experiment": "t"})
+    snaps = qio.load_dataset(res.snapshots_path)
+    assert snaps["q"].dims == ("time", "layer", "y", "x")
+    np.testing.assert_array_equal(snaps["time"].values, ts)
+    np.testing.assert_array_equal(snaps["q"].values, res.ys.q.cpu().numpy())
+    assert snaps.attrs["experiment"] == "t" and snaps.attrs["state_class"] == "BaroclinicQGState"
+    final = runner.restart_state(res.final_state_path, m, device="cuda")
+    assert torch.equal(final.q, res.ys.q[-1])
+    # the first half, then a restart from its final_state.zarr
+    half = runner.chunked_integrate_with_diagnostics(m, s0, ts[:2], dt, solver="ssprk3", log=lambda s: None,
+                                                     output_dir=tmp_path / "half")
+    r0 = runner.restart_state(half.final_state_path, m, device="cuda")
+    rest = runner.chunked_integrate_with_diagnostics(m, r0, ts[1:], dt, solver="ssprk3", log=lambda s: None)
+    assert torch.equal(rest.ys.q[-1], res.ys.q[-1])
+    with pytest.raises(ValueError):
+        runner.restart_state(res.final_state_path, sg.BaroclinicQG.create(nx=20, ny=20))
