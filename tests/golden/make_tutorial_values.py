@@ -5,7 +5,7 @@ the text outputs its tutorial notebooks print.  This script reads those outputs 
 code cells' logic) from a somax checkout and writes them, with their cell citations, as a
 small JSON fixture that the tests compare the oracle against.
 
-Usage: python tests/golden/make_tutorial_values.py /root/reference
+Usage: python tests/golden/make_tutorial_values.py <path of a somax checkout>
 """
 
 from __future__ import annotations
@@ -76,4 +76,6 @@ def main(ref: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_tutorial_values.py <path of a somax checkout>")
+    main(sys.argv[1])
