@@ -167,6 +167,18 @@ int qg_rhs_vjp(qg_plan* plan, const float* q, const float* params, const float* 
                float* params_bar, int flags, void* stream);
 int qg_invert_vjp(qg_plan* plan, const float* psi_bar, float* q_bar, void* stream);
 
+/* Adjoint of one qg_step step (any scheme, in Butcher form) from the state y0 (packed, ring as
+   stepped): on entry y_bar is the cotangent of the step's result, on return the cotangent of
+   y0; params_bar (may be NULL) receives the parameter cotangents of the step (overwritten).
+   The step's stage inputs are recomputed with the fused right-hand side, then the stages are
+   reversed with qg_rhs_vjp's kernels and fused linear-combination kernels.  work: caller-owned
+   device scratch of qg_step_vjp_workspace(plan, scheme) floats.  The checkpointed adjoint of
+   integrate (diffrax's recursive checkpointing under eqx.filter_grad,
+   tests/models/test_qg_baroclinic.py:293-312) calls it once per step in reverse. */
+int64_t qg_step_vjp_workspace(const qg_plan* plan, int scheme);
+int qg_step_vjp(qg_plan* plan, const float* y0, const float* params, double dt, int scheme, float* y_bar,
+                float* params_bar, float* work, void* stream);
+
 /* Geostrophic projection P = G (Q G)^-1 Q of a multilayer shallow-water state (h, u, v), each a
    packed field like q (device pointers): ReparameterizedQG.project
    (somax/_src/models/qg/reparameterized.py:142-178).  Q: q = curl(u, v) - f0 (h - H) / H with
@@ -258,6 +270,51 @@ int qg_plan_gemm_tuning(const qg_plan* plan, int* tile_n, float* ms, int n);
    the autotuner's time of four SSP-RK3 steps with the multi-launch path and with the cluster
    engine (-1 when not measured). */
 int qg_plan_engine(const qg_plan* plan, int* cluster_ctas, float* ms, int n);
+
+/* ---------------------------------------------------------------------------------------
+   Multilayer shallow-water right-hand side: MultilayerShallowWater2D
+   (somax/_src/models/swm/multilayer.py:150-200 vector_field, :202-219 apply_boundary_conditions,
+   :259-363 create).  The state is one packed float32 array (3, n_layers, ny + 2, nx + 2): layer
+   thickness h (T points), then u (U points, east faces), then v (V points, north faces).
+   params: 3 floats in device memory, QG_SWM_P_* below.
+   --------------------------------------------------------------------------------------- */
+#define QG_SWM_PERIODIC 0 /* bc = "periodic": every field wraps */
+#define QG_SWM_WALL 1     /* bc = "wall": no normal flow, free slip, zero-gradient h */
+#define QG_SWM_NPARAMS 3
+#define QG_SWM_P_NU 0    /* lateral_viscosity (m^2/s) */
+#define QG_SWM_P_KAPPA 1 /* bottom_drag (1/s) */
+#define QG_SWM_P_TAU0 2  /* wind_amplitude (m/s^2); the top layer gets tau0 * tau_x(y) / H[0] */
+
+typedef struct qg_swm_desc {
+    int nx, ny;         /* interior cells */
+    int n_layers;       /* 1..QG_MAX_LAYERS */
+    double Lx, Ly;      /* domain size (m) */
+    double f0, beta;    /* f(y) = f0 + beta (y - Ly / 2), y_j = j * Ly / ny */
+    double H[QG_MAX_LAYERS];       /* layer thicknesses, top to bottom (m) */
+    double g_prime[QG_MAX_LAYERS]; /* g'_0 = g, then the reduced gravities (m/s^2) */
+    int wind_profile;   /* QG_WIND_DOUBLEGYRE: tau_x = -cos(2 pi y / Ly); QG_WIND_SINGLE: -cos(pi y / Ly) */
+    int bc;             /* QG_SWM_PERIODIC or QG_SWM_WALL */
+} qg_swm_desc;
+
+typedef struct qg_swm_plan qg_swm_plan;
+
+/* MultilayerShallowWater2D.create: device constants and the stepper's stage buffers. */
+int qg_swm_create(const qg_swm_desc* desc, qg_swm_plan** out);
+void qg_swm_destroy(qg_swm_plan* plan);
+/* Floats of one packed state (3 * n_layers * (ny + 2) * (nx + 2)). */
+int64_t qg_swm_state_size(const qg_swm_plan* plan);
+/* tend = vector_field(state) (dh, du, dv packed like the state); with QG_RHS_APPLY_BC the
+   boundary rules are applied to the state as it is read (the _rhs wrapper, core/model.py:47-49). */
+int qg_swm_rhs(qg_swm_plan* plan, const float* state, float* tend, const float* params, int flags, void* stream);
+/* apply_boundary_conditions in place. */
+int qg_swm_apply_bc(qg_swm_plan* plan, float* state, void* stream);
+/* Advance the state in place by n_steps constant steps (QG_SCHEME_*; Tsit5 is the reference's
+   default solver): BC on every stage input, QG_STEP_APPLY_BC applies it to the initial state
+   first (integrate() on a new state0), the returned state is as stepped. */
+int qg_swm_step(qg_swm_plan* plan, float* state, const float* params, double dt, int n_steps, int scheme,
+                int flags, void* stream);
+/* QG_OK or QG_ERR_NONFINITE (a tendency was not finite since the last call); clears the flag. */
+int qg_swm_status(qg_swm_plan* plan, int* flags, void* stream);
 
 #ifdef __cplusplus
 }

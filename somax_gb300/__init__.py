@@ -8,4 +8,7 @@ from .qg import (  # noqa: F401
     MemberSpec, Plan, QGDiagnostics, QGEnsemble, QGParams, SaveAt, Solution, SomaxModel, State, Tsit5,
 )
 from .reparameterized import MultilayerSW2DState, ReparameterizedQG, ReparamQGGeostrophy  # noqa: F401
+from .swm import (  # noqa: F401
+    MultilayerShallowWater2D, MultilayerSW2DDiagnostics, MultilayerSW2DParams, MultilayerSW2DPhysConsts,
+)
 from .transforms import ModalTransform, StratificationProfile  # noqa: F401

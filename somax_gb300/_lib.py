@@ -50,6 +50,15 @@ class MemberDesc(C.Structure):
     ]
 
 
+class SwmDesc(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int), ("ny", C.c_int), ("n_layers", C.c_int),
+        ("Lx", C.c_double), ("Ly", C.c_double), ("f0", C.c_double), ("beta", C.c_double),
+        ("H", C.c_double * MAX_LAYERS), ("g_prime", C.c_double * MAX_LAYERS),
+        ("wind_profile", C.c_int), ("bc", C.c_int),
+    ]
+
+
 class Options(C.Structure):
     _fields_ = [("dst_precision", C.c_int), ("refine_sweeps", C.c_int), ("use_graphs", C.c_int),
                 ("persistent", C.c_int), ("autotune", C.c_int), ("stencil", C.c_int),
@@ -93,6 +102,15 @@ def lib() -> C.CDLL:
         "qg_project": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, vp, vp]),
         "qg_plan_set_wait_limit": (C.c_int, [vp, i64]),
         "qg_state_stats": (C.c_int, [vp, vp, vp, vp]),
+        "qg_step_vjp_workspace": (i64, [vp, C.c_int]),
+        "qg_step_vjp": (C.c_int, [vp, vp, vp, C.c_double, C.c_int, vp, vp, vp, vp]),
+        "qg_swm_create": (C.c_int, [C.POINTER(SwmDesc), C.POINTER(vp)]),
+        "qg_swm_destroy": (None, [vp]),
+        "qg_swm_state_size": (i64, [vp]),
+        "qg_swm_rhs": (C.c_int, [vp, vp, vp, vp, C.c_int, vp]),
+        "qg_swm_apply_bc": (C.c_int, [vp, vp, vp]),
+        "qg_swm_step": (C.c_int, [vp, vp, vp, C.c_double, C.c_int, C.c_int, C.c_int, vp]),
+        "qg_swm_status": (C.c_int, [vp, C.POINTER(C.c_int), vp]),
         "qg_plan_set_parallel_sweep": (C.c_int, [vp, C.c_int]),
     }
     for name, (res, args) in sig.items():

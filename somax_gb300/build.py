@@ -19,7 +19,7 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIBDIR = PKG / "lib"
 LIB = LIBDIR / "libqgcore.so"
-SOURCES = ["qg_plan.cu", "qg_stencil.cu", "qg_gemm_simt.cu", "qg_gemm_tc.cu", "qg_static.cu", "qg_persistent.cu", "qg_adjoint.cu", "qg_sweep.cu", "qg_lsweep.cu", "qg_capacitance.cu", "qg_mask.cu", "qg_cluster.cu"]
+SOURCES = ["qg_plan.cu", "qg_stencil.cu", "qg_gemm_simt.cu", "qg_gemm_tc.cu", "qg_static.cu", "qg_persistent.cu", "qg_adjoint.cu", "qg_sweep.cu", "qg_lsweep.cu", "qg_capacitance.cu", "qg_mask.cu", "qg_cluster.cu", "qg_swm.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

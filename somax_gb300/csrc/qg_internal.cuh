@@ -105,6 +105,14 @@ cudaError_t launch_k(void (*kernel)(KArgs...), int grid, int block, size_t smem,
     return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
+// Butcher tableau of an explicit Runge-Kutta scheme: a[s][j] (j < s) and b[s], n stages.
+constexpr int kMaxButcher = 6;
+struct Tableau {
+    int n;
+    double a[kMaxButcher][kMaxButcher];
+    double b[kMaxButcher];
+};
+
 struct PrepArgs {
     const MemberDev* members;
     const StencilTile* tiles;
@@ -182,14 +190,31 @@ cudaError_t launch_sweep(const StencilArgs& a, const SweepItem* const* items, co
 // strips of kLSweepOut output columns, lsweep_strips_per_block(nl) strips per CTA.  Each strip
 // class has its own kernel: 0 = every column and row the strip reads is strictly inside the
 // member (no ring, member-edge or store predicates), 1 = the strip touches the ring or the
-// member's edge, 2 = masked member (land rules).
+// member's edge in x and in y, 2 = masked member (land rules), 3 = it touches them in x only
+// (its rows are strictly inside), 4 = in y only (its columns are strictly inside).
 constexpr int kLSweepOut = 60;
-constexpr int kLSweepClasses = 3;
+constexpr int kLSweepClasses = 5;
+// Row bands of a member's strips: band sy covers rows [sy R, lsweep_band_end).  A remainder of
+// fewer than kLSweepAbsorb rows below the last full band is absorbed into that band (while it
+// stays within the 64 rows whose wind a strip holds in registers), so that no strip pays a
+// whole strip's start-up for a few rows (every square member of N = n + 2 with n a multiple
+// of 32 would otherwise end in a 2-row band).
+constexpr int kLSweepAbsorb = 8;
+__host__ __device__ inline int lsweep_bands(int Ny, int R) {
+    int n = (Ny + R - 1) / R;
+    const int rem = Ny - (n - 1) * R;
+    if (n > 1 && rem < kLSweepAbsorb && R + rem <= 64) --n;
+    return n;
+}
+__host__ __device__ inline int lsweep_band_end(int Ny, int sy, int R) {
+    return sy + 1 >= lsweep_bands(Ny, R) ? Ny : (sy + 1) * R;
+}
 __host__ __device__ inline int lsweep_item_class(int Ny, int Nx, bool masked, int sx, int sy, int R) {
     if (masked) return 2;
-    const int x0 = sx * kLSweepOut, jb = sy * R, rhi = (jb + R < Ny ? jb + R : Ny) + 1;
+    const int x0 = sx * kLSweepOut, jb = sy * R, rhi = lsweep_band_end(Ny, sy, R) + 1;
     // columns x0 - 2 .. x0 + 61 and rows jb - 2 .. rhi are read
-    return (x0 - 2 >= 1 && x0 + 61 <= Nx - 2 && jb - 2 >= 1 && rhi <= Ny - 2) ? 0 : 1;
+    const bool xin = x0 - 2 >= 1 && x0 + 61 <= Nx - 2, yin = jb - 2 >= 1 && rhi <= Ny - 2;
+    return xin ? (yin ? 0 : 4) : (yin ? 3 : 1);
 }
 int lsweep_columns();
 int lsweep_strips_per_block(int nl);
@@ -245,6 +270,14 @@ struct VjpArgs {
 cudaError_t launch_vjp_stencil(const VjpArgs& v, cudaStream_t s);
 cudaError_t launch_vjp_operand(const VjpArgs& v, const float* psi_bar, cudaStream_t s);
 cudaError_t launch_vjp_finish(const VjpArgs& v, const float* xbar, float* qbar, float* pbar, cudaStream_t s);
+cudaError_t launch_vjp_params_only(const VjpArgs& v, float* pbar, cudaStream_t s);
+// out = base + sum_j c_j x_j; ybar += Yb, kbar_j += c_j Yb; out_j = c_j g (n floats each)
+cudaError_t launch_lincomb(float* out, const float* base, const float* const* x, const float* c, int n_terms,
+                           int64_t n, cudaStream_t s);
+cudaError_t launch_scatter_bar(float* ybar, const float* Yb, float* const* kbar, const float* c, int n_terms,
+                               int64_t n, cudaStream_t s);
+cudaError_t launch_fanout(const float* g, float* const* out, const float* c, int n_terms, int64_t n, cudaStream_t s);
+const Tableau* swm_tableau(int scheme);
 
 // host: cuTensorMapEncodeTiled through the driver entry point (no libcuda link needed)
 cudaError_t tmap_encode(void* map, int bf16, int rank, const void* base, const uint64_t* dims,

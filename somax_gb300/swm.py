@@ -1,0 +1,310 @@
+"""``MultilayerShallowWater2D`` (``somax/_src/models/swm/multilayer.py``) on the GPU.
+
+The right-hand side (``vector_field``, :150-200), the boundary rules
+(``apply_boundary_conditions``, :202-219 and the wall helpers :366-410) and the constant-step
+integration run in libqgcore.so (``qg_swm_*``, C ABI in include/qgcore.h): one fused kernel
+computes dh, du, dv of every layer with the boundary rules applied as the state is read, and
+a Butcher-form stepper combines the stages.  ``create`` keeps the reference's keyword
+arguments (:259-363); ``diagnose`` (:221-257) reduces the energy and potential enstrophy from
+the same C-grid operators on the device (torch, not a hot path).
+
+The state is a ``MultilayerSW2DState`` (h, u, v, each (nl, Ny, Nx) with the ghost ring);
+the library sees it packed as one (3, nl, Ny, Nx) float32 array.  Only the first-order upwind
+mass flux (``method="upwind1"``, the reference's default) is implemented.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+
+import numpy as np
+import torch
+
+from . import _lib
+from .qg import SaveAt, Solution, SomaxModel, _solver_name, _stream_handle, check
+from .reparameterized import MultilayerSW2DState
+from .transforms import ModalTransform, StratificationProfile
+
+K = _lib.K
+_SCHEMES = {"euler": K["QG_SCHEME_EULER"], "heun": K["QG_SCHEME_HEUN"], "ssprk3": K["QG_SCHEME_SSPRK3"],
+            "tsit5": K["QG_SCHEME_TSIT5"]}
+
+
+@dataclasses.dataclass
+class MultilayerSW2DParams:
+    """Differentiable parameters (multilayer.py:43-55)."""
+
+    lateral_viscosity: torch.Tensor
+    bottom_drag: torch.Tensor
+    wind_amplitude: torch.Tensor
+
+
+@dataclasses.dataclass(frozen=True)
+class MultilayerSW2DPhysConsts:
+    """Frozen constants (multilayer.py:58-72)."""
+
+    gravity: float = 9.81
+    f0: float = 1e-4
+    beta: float = 0.0
+    n_layers: int = 2
+
+
+@dataclasses.dataclass
+class MultilayerSW2DDiagnostics:
+    """Diagnostics (multilayer.py:75-95)."""
+
+    energy: torch.Tensor
+    total_energy: torch.Tensor
+    enstrophy: torch.Tensor
+    total_enstrophy: torch.Tensor
+    potential_vorticity: torch.Tensor
+    relative_vorticity: torch.Tensor
+    kinetic_energy_field: torch.Tensor
+
+
+@dataclasses.dataclass(frozen=True)
+class SWGrid:
+    nx: int
+    ny: int
+    Lx: float
+    Ly: float
+
+    @property
+    def Nx(self):
+        return self.nx + 2
+
+    @property
+    def Ny(self):
+        return self.ny + 2
+
+    @property
+    def dx(self):
+        return self.Lx / self.nx
+
+    @property
+    def dy(self):
+        return self.Ly / self.ny
+
+
+class SwmPlan:
+    """Owns a ``qg_swm_plan`` (device constants and stage buffers) on one device."""
+
+    def __init__(self, desc: "_lib.SwmDesc", device):
+        L = _lib.lib()
+        self.device = torch.device(device)
+        h = C.c_void_p()
+        with torch.cuda.device(self.device):
+            check(L.qg_swm_create(C.byref(desc), C.byref(h)), "qg_swm_create")
+        self._h, self._L = h, L
+        self.state_size = int(L.qg_swm_state_size(h))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                self._L.qg_swm_destroy(h)
+            except Exception:  # pragma: no cover
+                pass
+            self._h = None
+
+    def _check(self, t, name):
+        if not isinstance(t, torch.Tensor) or t.device.type != "cuda" or t.dtype != torch.float32:
+            raise TypeError(f"{name} must be a float32 CUDA tensor")
+        if not t.is_contiguous() or t.numel() != self.state_size:
+            raise ValueError(f"{name} must be contiguous with {self.state_size} elements")
+
+    def rhs(self, y: torch.Tensor, params: torch.Tensor, apply_bc: bool, out=None) -> torch.Tensor:
+        self._check(y, "state")
+        out = torch.empty_like(y) if out is None else out
+        check(self._L.qg_swm_rhs(self._h, C.c_void_p(y.data_ptr()), C.c_void_p(out.data_ptr()),
+                                 C.c_void_p(params.data_ptr()), K["QG_RHS_APPLY_BC"] if apply_bc else 0,
+                                 _stream_handle(y.device)), "qg_swm_rhs")
+        return out
+
+    def apply_bc(self, y: torch.Tensor) -> torch.Tensor:
+        self._check(y, "state")
+        check(self._L.qg_swm_apply_bc(self._h, C.c_void_p(y.data_ptr()), _stream_handle(y.device)), "qg_swm_apply_bc")
+        return y
+
+    def step(self, y: torch.Tensor, params: torch.Tensor, dt: float, n_steps: int, scheme: str, apply_bc: bool):
+        self._check(y, "state")
+        check(self._L.qg_swm_step(self._h, C.c_void_p(y.data_ptr()), C.c_void_p(params.data_ptr()), float(dt),
+                                  int(n_steps), _SCHEMES[scheme], K["QG_STEP_APPLY_BC"] if apply_bc else 0,
+                                  _stream_handle(y.device)), "qg_swm_step")
+        return y
+
+    def status(self) -> int:
+        flags = C.c_int(0)
+        return self._L.qg_swm_status(self._h, C.byref(flags), _stream_handle(self.device))
+
+
+class MultilayerShallowWater2D(SomaxModel):
+    """Multilayer 2D nonlinear shallow water model, vector-invariant form (multilayer.py:98-257)."""
+
+    state_cls = MultilayerSW2DState
+
+    def __init__(self, params, consts, grid, strat, modal, wind_profile, bc, method):
+        self.params = params
+        self.consts = consts
+        self.grid = grid
+        self.strat = strat
+        self.modal = modal
+        self.wind_profile = wind_profile
+        self.bc_type = bc
+        self.method = method
+        self._plans: dict = {}
+
+    @staticmethod
+    def create(nx: int = 64, ny: int = 64, Lx: float = 4e6, Ly: float = 4e6, g: float = 9.81,
+               f0: float = 9.375e-5, beta: float = 1.754e-11, n_layers: int = 3,
+               H=(400.0, 1100.0, 2600.0), g_prime=(9.81, 0.025, 0.0125), stratification=None,
+               lateral_viscosity: float = 0.0, bottom_drag: float = 0.0, wind_amplitude: float = 0.0,
+               wind_profile: str = "doublegyre", bc: str = "periodic", method: str = "upwind1"):
+        """``MultilayerShallowWater2D.create`` with the same keyword arguments."""
+        if stratification is not None:
+            strat = stratification
+        else:
+            if len(H) != n_layers or len(g_prime) != n_layers:
+                raise ValueError(f"n_layers ({n_layers}), len(H) ({len(H)}), and len(g_prime) "
+                                 f"({len(g_prime)}) must all be equal")
+            strat = StratificationProfile.from_layers(H=list(H), g_prime=list(g_prime))
+        if bc not in ("periodic", "wall"):
+            raise ValueError(f"bc must be 'periodic' or 'wall', got {bc!r}")
+        if method != "upwind1":
+            raise ValueError(f"only the upwind1 mass flux is implemented, got {method!r}")
+        modal = ModalTransform.from_stratification(strat, f0)
+        params = MultilayerSW2DParams(*(torch.tensor(float(x)) for x in (lateral_viscosity, bottom_drag,
+                                                                        wind_amplitude)))
+        consts = MultilayerSW2DPhysConsts(gravity=g, f0=f0, beta=beta, n_layers=strat.nl)
+        return MultilayerShallowWater2D(params, consts, SWGrid(nx, ny, Lx, Ly), strat, modal, wind_profile, bc,
+                                        method)
+
+    # ---- plumbing -------------------------------------------------------------------------
+    @property
+    def shape(self):
+        return (self.consts.n_layers, self.grid.Ny, self.grid.Nx)
+
+    def _desc(self):
+        d = _lib.SwmDesc()
+        g = self.grid
+        d.nx, d.ny, d.n_layers = g.nx, g.ny, self.consts.n_layers
+        d.Lx, d.Ly, d.f0, d.beta = g.Lx, g.Ly, self.consts.f0, self.consts.beta
+        for k in range(self.consts.n_layers):
+            d.H[k] = float(self.strat.H[k])
+            d.g_prime[k] = float(self.strat.g_prime[k])
+        d.wind_profile = K["QG_WIND_SINGLE"] if self.wind_profile == "single" else K["QG_WIND_DOUBLEGYRE"]
+        d.bc = K["QG_SWM_WALL"] if self.bc_type == "wall" else K["QG_SWM_PERIODIC"]
+        return d
+
+    def plan(self, device=None) -> SwmPlan:
+        if not torch.cuda.is_available():
+            raise RuntimeError("somax_gb300 needs a CUDA device (no CPU fallback)")
+        dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        if dev.type != "cuda":
+            dev = torch.device("cuda", torch.cuda.current_device())
+        key = dev.index
+        if key not in self._plans:
+            self._plans[key] = SwmPlan(self._desc(), dev)
+        return self._plans[key]
+
+    def _param_vector(self, device) -> torch.Tensor:
+        p = self.params
+        return torch.tensor([float(p.lateral_viscosity), float(p.bottom_drag), float(p.wind_amplitude)],
+                            dtype=torch.float32, device=device)
+
+    def pack(self, state) -> torch.Tensor:
+        for name in ("h", "u", "v"):
+            t = getattr(state, name)
+            if tuple(t.shape) != self.shape:
+                raise ValueError(f"{name} must have shape {self.shape}, got {tuple(t.shape)}")
+        dev = state.h.device if state.h.device.type == "cuda" else torch.device("cuda", torch.cuda.current_device())
+        return torch.stack([state.h, state.u, state.v]).to(device=dev, dtype=torch.float32).contiguous()
+
+    def unpack(self, y: torch.Tensor) -> MultilayerSW2DState:
+        y = y.view((3,) + self.shape)
+        return MultilayerSW2DState(h=y[0], u=y[1], v=y[2])
+
+    # ---- the model contract -------------------------------------------------------------
+    def vector_field(self, t, state, args=None) -> MultilayerSW2DState:
+        """Tendencies (dh, du, dv) of the state as given (multilayer.py:150-200)."""
+        y = self.pack(state)
+        plan = self.plan(y.device)
+        return self.unpack(plan.rhs(y.reshape(-1), self._param_vector(y.device), apply_bc=False))
+
+    def apply_boundary_conditions(self, state) -> MultilayerSW2DState:
+        """Periodic wrap or the wall rules (multilayer.py:202-219)."""
+        y = self.pack(state).clone()
+        self.plan(y.device).apply_bc(y.reshape(-1))
+        return self.unpack(y)
+
+    def step(self, state, dt: float, n_steps: int = 1, solver="tsit5", apply_bc: bool = True):
+        """``n_steps`` constant steps on the GPU; BC on every stage input (and on the initial
+        state with ``apply_bc``), the returned state as stepped."""
+        y = self.pack(state).clone().reshape(-1)
+        plan = self.plan(y.device)
+        plan.step(y, self._param_vector(y.device), dt, n_steps, _solver_name(solver), apply_bc)
+        return self.unpack(y)
+
+    def integrate(self, state0, t0: float, t1: float, dt: float, solver=None, saveat=None, **kw) -> Solution:
+        """``SomaxModel.integrate`` with constant steps (``core/model.py:53-88``; Tsit5 default)."""
+        if kw.get("stepsize_controller") not in (None, "constant"):
+            raise ValueError("only constant step sizes are supported")
+        scheme = _solver_name(solver) if solver is not None else "tsit5"
+        saveat = saveat or SaveAt(t1=True)
+        n_total = int(round((t1 - t0) / dt))
+        if abs(n_total * dt - (t1 - t0)) > 1e-9 * max(1.0, abs(t1 - t0)):
+            raise ValueError("(t1 - t0) must be a whole number of steps")
+        targets = [int(round((float(t) - t0) / dt)) for t in saveat.ts] if saveat.ts is not None else [n_total]
+        y = self.pack(state0).clone().reshape(-1)
+        plan = self.plan(y.device)
+        pv = self._param_vector(y.device)
+        plan.apply_bc(y)
+        ys, done = [], 0
+        for tgt in targets:
+            if tgt < done:
+                raise ValueError("saveat.ts must be increasing")
+            if tgt > done:
+                plan.step(y, pv, dt, tgt - done, scheme, False)
+                done = tgt
+            ys.append(y.clone().view((3,) + self.shape))
+        st = torch.stack(ys)
+        ts = torch.tensor([t0 + k * dt for k in targets], dtype=torch.float64)
+        return Solution(ts=ts, ys=MultilayerSW2DState(h=st[:, 0], u=st[:, 1], v=st[:, 2]))
+
+    def diagnose(self, state) -> MultilayerSW2DDiagnostics:
+        """Energy (KE + g' h^2 / 2) and potential enstrophy (q^2 h_X / 2) per layer, PV and
+        relative vorticity at X points, KE at T points (multilayer.py:221-257)."""
+        y = self.pack(state).double()
+        h, u, v = y[0], y[1], y[2]
+        g = self.grid
+        s = (slice(None), slice(1, -1), slice(1, -1))
+
+        def interior(inner):
+            out = torch.zeros_like(h)
+            out[s] = inner
+            return out
+
+        ke = 0.5 * (interior(0.5 * (u[s] ** 2 + (u ** 2)[:, 1:-1, :-2])) +
+                    interior(0.5 * (v[s] ** 2 + (v ** 2)[:, :-2, 1:-1])))
+        zeta = interior((v[:, 1:-1, 2:] - v[s]) / g.dx - (u[:, 2:, 1:-1] - u[s]) / g.dy)
+        yrow = torch.arange(g.Ny, dtype=torch.float64, device=h.device) * g.dy
+        f = (self.consts.f0 + self.consts.beta * (yrow - g.Ly / 2.0))[:, None].expand(g.Ny, g.Nx)
+        fX = 0.5 * (f[1:-1, 1:-1] + f[2:, 1:-1])
+        hX = interior(0.25 * (h[s] + h[:, 1:-1, 2:] + h[:, 2:, 1:-1] + h[:, 2:, 2:]))
+        q = torch.zeros_like(h)
+        q[s] = (zeta[s] + fX) / hX[s]
+        area = g.dx * g.dy
+        gp = torch.tensor(np.asarray(self.strat.g_prime, float), dtype=torch.float64, device=h.device)
+        energy = ke[s].sum(dim=(-2, -1)) * area + 0.5 * gp * (h[s] ** 2).sum(dim=(-2, -1)) * area
+        ens = 0.5 * (q[s] ** 2 * hX[s]).sum(dim=(-2, -1)) * area
+        return MultilayerSW2DDiagnostics(energy=energy, total_energy=energy.sum(), enstrophy=ens,
+                                         total_enstrophy=ens.sum(), potential_vorticity=q.float(),
+                                         relative_vorticity=zeta.float(), kinetic_energy_field=ke.float())
+
+    def status(self) -> int:
+        return self.plan().status()
+
+
+__all__ = ["MultilayerShallowWater2D", "MultilayerSW2DParams", "MultilayerSW2DPhysConsts", "MultilayerSW2DDiagnostics",
+           "MultilayerSW2DState"]

@@ -34,6 +34,22 @@ def test_struct_layout_matches_header(L):
     assert C.sizeof(_lib.MemberDesc) == 16 + 32 + 128 + 16 + 1024 + 64 + 8
     assert _lib.MemberDesc.mask.offset == 16 + 32 + 128 + 16 + 1024 + 64
     assert C.sizeof(_lib.Options) == 32
+    # qg_swm_desc: 3 ints (+4 pad), 4 doubles, 2 x 8 doubles, 2 ints
+    assert C.sizeof(_lib.SwmDesc) == 16 + 32 + 128 + 8
+    assert _lib.SwmDesc.wind_profile.offset == 176
+
+
+def test_swm_create_validates_before_cuda(L):
+    h = C.c_void_p()
+    d = _lib.SwmDesc()
+    d.nx, d.ny, d.n_layers = 0, 16, 2
+    assert L.qg_swm_create(C.byref(d), C.byref(h)) == _lib.K["QG_ERR_SHAPE"]
+    d.nx, d.Lx, d.Ly = 16, 1e6, 1e6
+    d.H[0] = d.H[1] = 500.0
+    d.bc = 7
+    assert L.qg_swm_create(C.byref(d), C.byref(h)) == _lib.K["QG_ERR_ARG"]
+    assert L.qg_swm_create(None, C.byref(h)) == _lib.K["QG_ERR_NULL"]
+    assert L.qg_swm_rhs(None, None, None, None, 0, None) == _lib.K["QG_ERR_NULL"]
 
 
 def test_plan_create_validates_before_cuda(L):
