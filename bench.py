@@ -191,6 +191,13 @@ def describe(name):
 
     if name == "ensemble256":
         return METRIC, "member-days/s", ENSEMBLE_DESC + ", 72 steps = 1 model day per bench step"
+    if name == "adjoint256":
+        return (METRIC, UNIT,
+                "adjoint256: one gradient per bench step of the quadratic misfit of the final layer-1 psi (seeded "
+                "target) with respect to q0 and tau0 after 100 ssprk3 steps (dt=1200s) of the 3-layer 256x256 double "
+                "gyre: forward with checkpoints every 10 steps, reverse sweep with segment recomputation and "
+                "qg_step_vjp per step; value = model-days of forward + reverse integration per second "
+                "(100 steps = 1.389 model days per gradient)")
     if name == "masked3_512":
         return (METRIC, UNIT,
                 "masked3_512: 3-layer 512x512 double gyre (Lx=Ly=5120 km) with a seeded coastline (15 % of the "
@@ -238,6 +245,9 @@ def run_reference(args):
         elif args.config == "masked3_512":
             v, n, el = masked_cpu_baseline(threads, per_step_s if k >= args.warmup else 1.0)
             desc = f"{n} ssprk3 steps of masked3_512 in float64 with cached sparse LU ({el:.1f} s)"
+        elif args.config == "adjoint256":
+            v, n, el = cpu_baseline(tc.C5, threads, per_step_s if k >= args.warmup else 1.0)
+            desc = f"{n} ssprk3 steps of baroclinic3_256 forward only (no CPU reverse mode; {el:.1f} s)"
         else:
             cfg = tc.CONFIGS[args.config]
             v, n, el = cpu_baseline(cfg, threads, per_step_s if k >= args.warmup else 1.0)
@@ -286,6 +296,20 @@ class Workload:
             self.members = [(c.n + 2, c.nl) for c in cfgs]
             self.dt, self.scheme = cfgs[0].dt, cfgs[0].scheme
             self.model = None
+        elif name == "adjoint256":
+            cfg = tc.C5
+            kw = cfg.model_kwargs()
+            self.cfg, self.kw = cfg, kw
+            self.model = sg.BaroclinicQG.create(**kw, precision=precision, stencil=stencil, gemm_tile=gemm_tile)
+            self.plan = self.model.plan(dev)
+            self.params = self.model._param_vector(dev)
+            self.q0 = tc.initial_pv(cfg, seed=seed).astype(np.float32)
+            tgt = torch.tensor(tc.initial_pv(cfg, seed=seed + 1), dtype=torch.float32, device=dev)
+            self.target = self.model._invert_pv(tgt)[0].detach().double()
+            self.members = [(cfg.n + 2, cfg.nl)]
+            self.dt, self.scheme = cfg.dt, cfg.scheme
+            self.adj_steps = 100
+            self.ens = None
         else:
             masked = name == "masked3_512"
             cfg = tc.CONFIGS["baroclinic3_512" if masked else name]
@@ -306,14 +330,44 @@ class Workload:
         self.n_members = len(self.members)
         self.steps_per_day = int(round(86400.0 / self.dt))
         self.q = torch.tensor(self.q0, device=dev).reshape(-1)
+        if name == "adjoint256":
+            # a bench step integrates 100 steps forward and back: its rate in model days
+            self.days_per_step = self.adj_steps * self.dt / 86400.0
+
+    def gradient(self, q0):
+        """(d loss / d q0, d loss / d tau0) through the public API: integrate with autograd."""
+        import torch
+
+        import somax_gb300 as sg
+
+        kw = self.kw
+        m = self.model
+        m.params = sg.QGParams(torch.tensor(kw["lateral_viscosity"]), torch.tensor(kw["bottom_drag"]),
+                               torch.tensor(float(kw["wind_amplitude"]), requires_grad=True),
+                               torch.tensor(kw["biharmonic_viscosity"]))
+        q = q0.detach().view(m.shape).requires_grad_(True)
+        sol = m.integrate(sg.BaroclinicQGState(q=q), 0.0, self.adj_steps * self.dt, self.dt, solver=self.scheme,
+                          checkpoint_every=10)
+        psi = m._invert_pv(sol.ys.q[-1])
+        loss = 0.5 * ((psi[0].double() - self.target) ** 2).sum()
+        loss.backward()
+        return q.grad, m.params.wind_amplitude.grad
 
     def device_step(self):
+        if self.name == "adjoint256":
+            self.gradient(self.q)
+            return
         self.plan.step(self.q, self.params, self.dt, self.steps_per_day, self.scheme)
 
     def host_step(self, qh, out):
-        """The public API with host buffers: H2D, one model day, D2H."""
+        """The public API with host buffers: H2D, one model day (or one gradient), D2H."""
         import somax_gb300 as sg
 
+        if self.name == "adjoint256":
+            q = qh.to(device=self.q.device, non_blocking=True)
+            gq, _ = self.gradient(q)
+            out.copy_(gq.reshape(-1), non_blocking=True)
+            return
         if self.ens is not None:
             self.ens.step_host(qh, out, self.dt, self.steps_per_day, self.scheme)
         else:
@@ -478,7 +532,7 @@ def parity_10_steps(W, dev, threads):
                   None) for i, cfg, kw in picks]
     else:
         masked = W.name == "masked3_512"
-        cfg = tc.CONFIGS["baroclinic3_512" if masked else W.name]
+        cfg = tc.C5 if W.name == "adjoint256" else tc.CONFIGS["baroclinic3_512" if masked else W.name]
         mask = tc.land_mask(cfg.n, cfg.n, frac=0.15, seed=0) if masked else None
         cases = [(W.name, cfg, cfg.model_kwargs(), q.view(W.model.shape), W.q0, mask)]
     out = {}
@@ -507,7 +561,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="ensemble256",
                     help="ensemble256 (default) | baroclinic3_128 | barotropic_64 | baroclinic3_256 | "
-                         "baroclinic3_512 | baroclinic3_1024 | masked3_512")
+                         "baroclinic3_512 | baroclinic3_1024 | masked3_512 | adjoint256")
     ap.add_argument("--precision", default="bf16x3", help="DST-I GEMM arithmetic: fp32 | tf32 | bf16x3")
     ap.add_argument("--persistent", type=int, default=0,
                     help="1: all steps of a call in one persistent cooperative launch (tensor-core precisions)")
@@ -563,7 +617,8 @@ def main():
         dist.barrier()
     dev_ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in ev), world, dev)
     ms_per_step = dev_ms / args.steps
-    value = whole_job_rate(world, W.n_members, args.steps, dev_ms / 1000.0)
+    days = getattr(W, "days_per_step", 1.0)  # model days per bench step and member
+    value = whole_job_rate(world, W.n_members, args.steps, dev_ms / 1000.0) * days
     status = plan.status(dev)
 
     # ---- e2e: public API with pinned host buffers --------------------------------------
@@ -578,11 +633,8 @@ def main():
         W.host_step(qh, out)
         torch.cuda.current_stream(dev).synchronize()
     e2e_s = max_over_ranks(time.perf_counter() - t0, world, dev)
-    e2e_value = whole_job_rate(world, W.n_members, args.steps, e2e_s)
+    e2e_value = whole_job_rate(world, W.n_members, args.steps, e2e_s) * days
     qbytes = qh.numel() * 4
-
-    # ---- launches per bench step (graph / persistent replay counts every kernel) ---------
-    launches_per_day = plan.launches_per_call(W.steps_per_day, W.scheme)
 
     # ---- profiled pass: per-kernel-class event timing (multi-launch path) ----------------
     plan.set_profiling(True)
@@ -590,11 +642,17 @@ def main():
     torch.cuda.synchronize()
     stats = {k: plan.kernel_stats(k) for k in range(5)}
     plan.set_profiling(False)
+
+    # ---- launches per bench step (graph / persistent replay counts every kernel) ---------
+    if args.config == "adjoint256":
+        launches_per_day = sum(n for _, n in stats.values())  # every launch of one gradient, counted
+    else:
+        launches_per_day = plan.launches_per_call(W.steps_per_day, W.scheme)
     roof = roofline(W, stats, args.precision, args.config, plan.engine()["cluster_ctas"] > 0, ms_per_step)
 
     # ---- the plain FP32 single-member path on the same members (the metric's baseline) ----
     vs_baseline, plain = None, None
-    if args.config != "masked3_512":
+    if args.config not in ("masked3_512", "adjoint256"):
         mix = tc.C4_MIX if W.ens is not None else ((1, tc.CONFIGS[args.config]),)
         plain_rate, plain_classes = plain_fp32_rate(dev, mix)
         plain_rate *= world  # every rank loops its own replica of the members
@@ -626,6 +684,11 @@ def main():
         if args.config == "masked3_512":
             v, n, el = masked_cpu_baseline(threads, 10.0)
             sample = f"{n} ssprk3 steps of masked3_512, float64 NumPy/SciPy restatement with cached sparse LU ({el:.1f} s)"
+        elif args.config == "adjoint256":
+            v, n, el = cpu_baseline(tc.C5, threads, 10.0)
+            sample = (f"{n} ssprk3 steps of baroclinic3_256, float32 NumPy/SciPy restatement, forward only "
+                      f"({el:.1f} s): the CPU restatement has no reverse mode, and a gradient costs at least one "
+                      "forward, so this overstates the CPU's gradient rate")
         elif W.model is not None:
             cfg = tc.CONFIGS[args.config]
             v, n, el = cpu_baseline(cfg, threads, 10.0)

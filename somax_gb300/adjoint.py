@@ -7,9 +7,11 @@ adjoint recomputes the forward from checkpoints).  Here the same derivatives com
 
 * :class:`RHS`       -> ``qg_rhs_vjp``    (q_bar and the parameter cotangents)
 * :class:`Invert`    -> ``qg_invert_vjp`` (one adjoint DST-I solve; the solve is self-adjoint)
-* :class:`Integrate` -> the adjoint of the explicit Runge-Kutta step built from ``qg_rhs_vjp``,
-  with the state kept every ``checkpoint_every`` steps and each segment recomputed on the
-  GPU during the backward sweep (memory: one state per checkpoint plus one segment).
+* :class:`Integrate` -> the adjoint of the explicit Runge-Kutta step (``qg_step_vjp``: the
+  step's stage inputs recomputed with the fused right-hand side and the stages reversed with
+  ``qg_rhs_vjp``'s kernels and fused linear-combination kernels, in one C-ABI call), with the
+  state kept every ``checkpoint_every`` steps and each segment recomputed on the GPU during
+  the backward sweep (memory: one state per checkpoint plus one segment).
 
 A step is ``y1 = y0 + dt * sum_i b_i k_i``, ``k_i = F(B(y0 + dt * sum_j a_ij k_j))`` with B
 the ring zeroing of the stage input (``core/model.py:47-49``); its adjoint for the cotangent
@@ -17,7 +19,8 @@ the ring zeroing of the stage input (``core/model.py:47-49``); its adjoint for t
 ``Y_bar_i = F_vjp(Y_i; k_bar_i)``, ``y0_bar += Y_bar_i``, ``k_bar_j += dt a_ij Y_bar_i``.
 The fused ``qg_step`` kernels produce the same ring (``y0 + dt * wind``) as this form, so the
 forward (every scheme) runs fused and only the recomputed stages of one step at a time run
-unfused.
+unfused.  ``step_vjp_torch`` is the same algebra written with torch operations around
+``qg_rhs`` / ``qg_rhs_vjp``; the tests compare the two.
 """
 
 from __future__ import annotations
@@ -82,6 +85,12 @@ def _advance(plan, q, p, dt, n, scheme):
 
 def step_vjp(plan, y0, p, dt, scheme, g):
     """(y0_bar, params_bar) of one step from ``y0`` for the cotangent ``g`` of its result."""
+    return plan.step_vjp(y0, p, dt, scheme, g)
+
+
+def step_vjp_torch(plan, y0, p, dt, scheme, g):
+    """``step_vjp`` with the stage algebra as torch operations around ``qg_rhs`` /
+    ``qg_rhs_vjp`` (the reference form of the fused call)."""
     a, b = rk_tableau(scheme)
     s_n = len(b)
     # stage inputs of the step (recomputed)

@@ -20,6 +20,8 @@
 // terms that are linear in nu, kappa, tau0 and nu4.
 #include <cuda_bf16.h>
 
+#include <algorithm>
+
 #include "qg_internal.cuh"
 
 namespace qg {
@@ -290,6 +292,89 @@ cudaError_t launch_vjp_finish(const VjpArgs& v, const float* xbar, float* qbar, 
         e = cudaGetLastError();
     }
     return e;
+}
+
+// Linear combinations over packed fields (caller packing, n floats each) for the Runge-Kutta
+// step's adjoint: out = base + sum_j c_j x_j (stage inputs), and the reverse sweep's
+// scatter of one stage cotangent Ybar: y_bar += Ybar, kbar_j += c_j Ybar.
+struct LinComb {
+    const float* x[kMaxButcher];
+    float* y[kMaxButcher];
+    float c[kMaxButcher];
+    int n_terms;
+};
+
+__global__ void k_lincomb(float* __restrict__ out, const float* __restrict__ base, LinComb lc, int64_t n) {
+    const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += nth) {
+        float v = base[t];
+        for (int j = 0; j < lc.n_terms; ++j) v = fmaf(lc.c[j], lc.x[j][t], v);
+        out[t] = v;
+    }
+}
+
+// y_bar += Ybar and kbar_j += c_j Ybar (j < n_terms), in one pass over Ybar.
+__global__ void k_scatter_bar(float* __restrict__ ybar, const float* __restrict__ Yb, LinComb lc, int64_t n) {
+    const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += nth) {
+        const float v = Yb[t];
+        ybar[t] += v;
+        for (int j = 0; j < lc.n_terms; ++j) lc.y[j][t] = fmaf(lc.c[j], v, lc.y[j][t]);
+    }
+}
+
+// kbar_s = c_s g for every stage s (the cotangents of the stage derivatives at the step's end).
+__global__ void k_fanout(const float* __restrict__ g, LinComb lc, int64_t n) {
+    const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += nth) {
+        const float v = g[t];
+        for (int j = 0; j < lc.n_terms; ++j) lc.y[j][t] = lc.c[j] * v;
+    }
+}
+
+namespace {
+int lincomb_grid(int64_t n) { return (int)std::min<int64_t>(8192, std::max<int64_t>(1, (n + 255) / 256)); }
+}  // namespace
+
+cudaError_t launch_lincomb(float* out, const float* base, const float* const* x, const float* c, int n_terms,
+                           int64_t n, cudaStream_t s) {
+    LinComb lc{};
+    lc.n_terms = n_terms;
+    for (int j = 0; j < n_terms; ++j) {
+        lc.x[j] = x[j];
+        lc.c[j] = c[j];
+    }
+    k_lincomb<<<lincomb_grid(n), 256, 0, s>>>(out, base, lc, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_bar(float* ybar, const float* Yb, float* const* kbar, const float* c, int n_terms,
+                               int64_t n, cudaStream_t s) {
+    LinComb lc{};
+    lc.n_terms = n_terms;
+    for (int j = 0; j < n_terms; ++j) {
+        lc.y[j] = kbar[j];
+        lc.c[j] = c[j];
+    }
+    k_scatter_bar<<<lincomb_grid(n), 256, 0, s>>>(ybar, Yb, lc, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fanout(const float* g, float* const* out, const float* c, int n_terms, int64_t n, cudaStream_t s) {
+    LinComb lc{};
+    lc.n_terms = n_terms;
+    for (int j = 0; j < n_terms; ++j) {
+        lc.y[j] = out[j];
+        lc.c[j] = c[j];
+    }
+    k_fanout<<<lincomb_grid(n), 256, 0, s>>>(g, lc, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_vjp_params_only(const VjpArgs& v, float* pbar, cudaStream_t s) {
+    const int n = v.n_members * QG_NPARAMS;
+    k_vjp_params<<<(n + 127) / 128, 128, 0, s>>>(v.pacc, n, pbar);
+    return cudaGetLastError();
 }
 
 }  // namespace qg

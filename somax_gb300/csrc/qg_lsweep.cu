@@ -20,8 +20,8 @@
 // Each strip class (lsweep_item_class) has its own kernel, so that each keeps the registers
 // of its own path: interior strips (every column and row read strictly inside the member)
 // carry no ring, member-edge or store predicates; edge strips apply the column rules as
-// per-lane 0/1 multipliers and selects and the row rules as warp-uniform tests; masked
-// members add the land rules.  The ring slot, window slot and exchange parity of every row
+// per-lane 0/1 multipliers and selects and the row rules as warp-uniform tests, each only
+// where the strip meets that kind of edge (x, y or both); masked members add the land rules.  The ring slot, window slot and exchange parity of every row
 // are compile-time constants of an eight-row unrolled walk (strip heights are multiples of
 // 16, so the first ingested row is 6 mod 8).
 //
@@ -461,7 +461,7 @@ __global__ void __launch_bounds__(lsweep_groups(NL) * NL * 32)
         k.Nx = M.Nx;
         k.Px = M.Px;
         k.jb = it.sy * R;
-        k.je = min(k.jb + R, k.Ny);
+        k.je = lsweep_band_end(k.Ny, it.sy, R);
         k.rhi = k.je + 1;  // outputs jb .. je - 1 read rows one beyond them, the biharmonic one more
         k.l = l;
         k.lane = lane;
@@ -526,8 +526,12 @@ __global__ void __launch_bounds__(lsweep_groups(NL) * NL * 32)
             chk = walk<NL, false, false, false>(k, cm, cl, c, chk);
         else if constexpr (CLS == 1)
             chk = walk<NL, false, true, true>(k, cm, cl, c, chk);
-        else
+        else if constexpr (CLS == 2)
             chk = walk<NL, true, true, true>(k, cm, cl, c, chk);
+        else if constexpr (CLS == 3)
+            chk = walk<NL, false, true, false>(k, cm, cl, c, chk);
+        else
+            chk = walk<NL, false, false, true>(k, cm, cl, c, chk);
     }
     const bool bad = __any_sync(kFull, !isfinite(chk.x) || !isfinite(chk.y));
     if (a.flags && lane == 0) {
@@ -537,7 +541,7 @@ __global__ void __launch_bounds__(lsweep_groups(NL) * NL * 32)
 }
 
 using LSweepKernel = void (*)(StencilArgs, const SweepItem*, int, int);
-#define QG_LSWEEP_ROW(n) k_lsweep<n, 0>, k_lsweep<n, 1>, k_lsweep<n, 2>
+#define QG_LSWEEP_ROW(n) k_lsweep<n, 0>, k_lsweep<n, 1>, k_lsweep<n, 2>, k_lsweep<n, 3>, k_lsweep<n, 4>
 constexpr LSweepKernel kLSweep[kMaxLayers * kLSweepClasses] = {QG_LSWEEP_ROW(1), QG_LSWEEP_ROW(2), QG_LSWEEP_ROW(3),
                                                                QG_LSWEEP_ROW(4), QG_LSWEEP_ROW(5), QG_LSWEEP_ROW(6),
                                                                QG_LSWEEP_ROW(7), QG_LSWEEP_ROW(8)};

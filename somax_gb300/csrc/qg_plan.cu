@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <new>
 #include <vector>
 
@@ -385,6 +386,47 @@ GemmArgs gemm_args(qg_plan* p, int pass, const void* A, void* C, int a_fmt, int 
     return g;
 }
 
+// The output tiles of one M-tile (a member's N-tiles: 258-wide members need two 144-wide
+// tiles) read the same A rows.  A GEMM launch hands tile t, t + G, t + 2G, ... to CTA t of its
+// G = SM-count CTAs, so the list is reordered to space the N-tiles of each M-tile exactly G
+// apart: the CTA that takes the first takes the next right after it, while the A rows it
+// just streamed are still in L2, instead of two CTAs missing on the same rows at once.
+// Batches of up to G M-tiles with k N-tiles each become k chunks of G slots (chunk j holding
+// N-tile j of every M-tile of the batch), the free slots filled with single-tile M-tiles;
+// single tiles left over go last.  Only the order changes: every tile is computed once.
+std::vector<GemmTile> space_n_tiles(const std::vector<GemmTile>& in, int G) {
+    if (G < 1) return in;
+    std::vector<std::vector<GemmTile>> rows;  // tiles of one (member, mt), nt ascending
+    for (const GemmTile& t : in) {
+        if (!rows.empty() && rows.back()[0].member == t.member && rows.back()[0].mt == t.mt)
+            rows.back().push_back(t);
+        else
+            rows.push_back({t});
+    }
+    std::vector<GemmTile> singles, out;
+    std::vector<std::vector<GemmTile>*> multi;
+    for (auto& r : rows) {
+        if (r.size() == 1)
+            singles.push_back(r[0]);
+        else
+            multi.push_back(&r);
+    }
+    size_t next_single = 0;
+    for (size_t i = 0; i < multi.size();) {
+        // a batch: up to G consecutive M-tiles with the same N-tile count
+        const size_t k = multi[i]->size();
+        size_t j = i;
+        while (j < multi.size() && j - i < (size_t)G && multi[j]->size() == k) ++j;
+        for (size_t nt = 0; nt < k; ++nt) {
+            for (size_t r = i; r < j; ++r) out.push_back((*multi[r])[nt]);
+            for (size_t f = j - i; f < (size_t)G && next_single < singles.size(); ++f) out.push_back(singles[next_single++]);
+        }
+        i = j;
+    }
+    while (next_single < singles.size()) out.push_back(singles[next_single++]);
+    return out;
+}
+
 cudaError_t run_gemm(qg_plan* p, const GemmArgs& g, cudaStream_t s) {
     const int nt = pass_xin(g.pass) ? p->n_gx : p->n_gy;
     return timed(p, QG_K_GEMM, s, [&] {
@@ -563,11 +605,6 @@ int scheme_stages(int scheme, Stage* st) {
 
 // Butcher tableaus of the schemes stepped in Butcher form: Euler and Tsit5 (Tsitouras 2011,
 // the coefficients diffrax.Tsit5 uses).  a[s][j] (j < s) and b[s].
-struct Tableau {
-    int n;
-    double a[6][6];
-    double b[6];
-};
 const Tableau* butcher(int scheme) {
     static const Tableau euler = {1, {{0}}, {1.0}};
     static const Tableau tsit5 = {
@@ -892,6 +929,7 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
     const int BMg = tc ? 128 : kSimtBM;
     const int n_bn = tc ? kNumBN : 1;
     std::vector<GemmTile> gxv[kNumBN], gyv[kNumBN];
+    std::map<long long, std::pair<float*, uint16_t*>> dst_cache;  // (size, pitch) -> device DST-I matrix
     for (int i = 0; i < n_members; ++i) {
         const qg_member_desc& d = members[i];
         MemberDev& M = p->mh[i];
@@ -916,7 +954,7 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
         off_layer += n;
         p->max_nl = std::max(p->max_nl, n);
         // constant fields
-        std::vector<float> by(M.Ny), F(M.Ny), ex, ey, Sx, Sy;
+        std::vector<float> by(M.Ny), F(M.Ny), ex, ey;
         for (int j = 0; j < M.Ny; ++j) {
             const double y = j * dy;
             by[j] = (float)(d.beta * (y - d.Ly / 2.0));
@@ -925,20 +963,16 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
         }
         dst_eigs(M.Nx, dx, ex);
         dst_eigs(M.Ny, dy, ey);
-        dst_matrix(M.Nx, M.Px, Sx);
-        dst_matrix(M.Ny, M.Py, Sy);
-        float *dby, *dF, *dex, *dey, *dSx, *dSy;
+        float *dby, *dF, *dex, *dey;
         if ((e = upload(p, &dby, by)) || (e = upload(p, &dF, F)) || (e = upload(p, &dex, ex)) ||
-            (e = upload(p, &dey, ey)) || (e = upload(p, &dSx, Sx)) || (e = upload(p, &dSy, Sy)))
+            (e = upload(p, &dey, ey)))
             break;
         M.by = dby;
         M.F = dF;
         M.ex = dex;
         M.ey = dey;
-        M.Sx = dSx;
-        M.Sy = dSy;
-        if (o.dst_precision == QG_DST_BF16X3) {
-            // bf16 hi/lo split of the DST matrices (hi plane then lo plane)
+        {
+            // bf16 hi/lo split of a DST matrix (hi plane then lo plane)
             auto split = [&](const std::vector<float>& S, uint16_t** dst) {
                 std::vector<uint16_t> h(2 * S.size());
                 for (size_t k = 0; k < S.size(); ++k) {
@@ -957,8 +991,31 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
                 }
                 return upload(p, dst, h);
             };
+            // The DST-I matrix of a size and pitch is the same for every member: one device copy
+            // per (size, pitch), shared, so that every GEMM pass reads it from L2 instead of one
+            // DRAM copy per member (28 MB per pass on the 256-member ensemble).
+            auto shared_dst = [&](int nn, int ld, float** f32, uint16_t** bf) -> cudaError_t {
+                const long long key = (long long)nn << 32 | (unsigned)ld;
+                auto it = dst_cache.find(key);
+                if (it == dst_cache.end()) {
+                    std::vector<float> S;
+                    dst_matrix(nn, ld, S);
+                    float* d32 = nullptr;
+                    uint16_t* dbf = nullptr;
+                    cudaError_t ee = upload(p, &d32, S);
+                    if (!ee && o.dst_precision == QG_DST_BF16X3) ee = split(S, &dbf);
+                    if (ee) return ee;
+                    it = dst_cache.emplace(key, std::make_pair(d32, dbf)).first;
+                }
+                *f32 = it->second.first;
+                *bf = it->second.second;
+                return cudaSuccess;
+            };
+            float *dSx, *dSy;
             uint16_t *bx, *byy;
-            if ((e = split(Sx, &bx)) || (e = split(Sy, &byy))) break;
+            if ((e = shared_dst(M.Nx, M.Px, &dSx, &bx)) || (e = shared_dst(M.Ny, M.Py, &dSy, &byy))) break;
+            M.Sx = dSx;
+            M.Sy = dSy;
             M.Sx_bf = bx;
             M.Sy_bf = byy;
         }
@@ -994,7 +1051,8 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
         // column-sweep strips
         for (int v = 0; v < kSweepLists; ++v) {
             const int R = kSweepRows[v % 3], W = v >= 3 ? lsweep_columns() : sweep_columns();
-            for (int sy = 0; sy < (M.Ny + R - 1) / R; ++sy)
+            const int bands = v >= 3 ? lsweep_bands(M.Ny, R) : (M.Ny + R - 1) / R;
+            for (int sy = 0; sy < bands; ++sy)
                 for (int sx = 0; sx < (M.Nx + W - 1) / W; ++sx) sw_v[v].push_back({i, sx, sy});
         }
         // tiles
@@ -1048,6 +1106,8 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
             e = upload(p, &p->sw_items_v[v], g);
         }
         for (int v = 0; v < n_bn && !e; ++v) {
+            gxv[v] = space_n_tiles(gxv[v], p->n_sm);
+            gyv[v] = space_n_tiles(gyv[v], p->n_sm);
             p->n_gx_v[v] = (int)gxv[v].size();
             p->n_gy_v[v] = (int)gyv[v].size();
             if (!(e = upload(p, &p->gx_v[v], gxv[v]))) e = upload(p, &p->gy_v[v], gyv[v]);
@@ -1347,13 +1407,11 @@ int qg_step(qg_plan* p, float* q, const float* params, double dt, int n_steps, i
     return cuda_err(e);
 }
 
-int qg_rhs_vjp(qg_plan* p, const float* q, const float* params, const float* dq_bar, float* q_bar,
-               float* params_bar, int flags, void* stream) {
-    if (!p || !q || !params || !dq_bar || !q_bar) return QG_ERR_NULL;
-    if (flags & ~QG_RHS_APPLY_BC) return QG_ERR_ARG;
-    if (p->n_cap > 0) return QG_ERR_UNSUPPORTED;  // no adjoint of the masked inversion yet
-    cudaStream_t s = (cudaStream_t)stream;
-    const int bc = (flags & QG_RHS_APPLY_BC) ? 1 : 0;
+namespace {
+// q_bar = (d dq / d q)^T dq_bar of the rhs at q; the parameter cotangents are added to the
+// plan's FP64 accumulators (zeroed by the caller).
+cudaError_t rhs_vjp_core(qg_plan* p, const float* q, const float* params, const float* dq_bar, float* q_bar,
+                         int bc, cudaStream_t s) {
     // forward psi (layer, caller packing) into the YA plane, which holds at least one field
     cudaError_t e = run_prep(p, q, nullptr, 0, bc, s);
     if (!e) e = run_dst_solve(p, s);
@@ -1371,11 +1429,76 @@ int qg_rhs_vjp(qg_plan* p, const float* q, const float* params, const float* dq_
     v.direct = p->S2;
     v.rhs = p->XB;
     if (!e) e = cudaMemsetAsync(p->XB, 0, (size_t)p->xplane * sizeof(float), s);
-    if (!e) e = cudaMemsetAsync(p->vjp_acc, 0, (size_t)p->n_members * QG_NPARAMS * sizeof(double), s);
     if (!e) e = timed(p, QG_K_STENCIL, s, [&] { return launch_vjp_stencil(v, s); });
     if (!e) e = timed(p, QG_K_PREP, s, [&] { return launch_vjp_operand(v, nullptr, s); });
     if (!e) e = run_dst_solve(p, s);
-    if (!e) e = timed(p, QG_K_OTHER, s, [&] { return launch_vjp_finish(v, p->XC, q_bar, params_bar, s); });
+    if (!e) e = timed(p, QG_K_OTHER, s, [&] { return launch_vjp_finish(v, p->XC, q_bar, nullptr, s); });
+    return e;
+}
+}  // namespace
+
+int qg_rhs_vjp(qg_plan* p, const float* q, const float* params, const float* dq_bar, float* q_bar,
+               float* params_bar, int flags, void* stream) {
+    if (!p || !q || !params || !dq_bar || !q_bar) return QG_ERR_NULL;
+    if (flags & ~QG_RHS_APPLY_BC) return QG_ERR_ARG;
+    if (p->n_cap > 0) return QG_ERR_UNSUPPORTED;  // no adjoint of the masked inversion yet
+    cudaStream_t s = (cudaStream_t)stream;
+    const int bc = (flags & QG_RHS_APPLY_BC) ? 1 : 0;
+    cudaError_t e = cudaMemsetAsync(p->vjp_acc, 0, (size_t)p->n_members * QG_NPARAMS * sizeof(double), s);
+    if (!e) e = rhs_vjp_core(p, q, params, dq_bar, q_bar, bc, s);
+    if (!e && params_bar) e = launch_vjp_params_only(vjp_args(p), params_bar, s);
+    return cuda_err(e);
+}
+
+int64_t qg_step_vjp_workspace(const qg_plan* p, int scheme) {
+    const Tableau* tb = swm_tableau(scheme);
+    if (!p || !tb) return -1;
+    return (int64_t)(3 * tb->n - 1) * p->state_size;
+}
+
+int qg_step_vjp(qg_plan* p, const float* y0, const float* params, double dt, int scheme, float* y_bar,
+                float* params_bar, float* work, void* stream) {
+    if (!p || !y0 || !params || !y_bar || !work) return QG_ERR_NULL;
+    if (p->n_cap > 0) return QG_ERR_UNSUPPORTED;
+    const Tableau* tb = swm_tableau(scheme);
+    if (!tb || !(dt == dt)) return QG_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int ns = tb->n;
+    const int64_t n = p->state_size;
+    // work: stage inputs Y_1 .. Y_{ns-1}, stage derivatives k_0 .. k_{ns-2}, their cotangents
+    // kbar_0 .. kbar_{ns-1}, and one stage-input cotangent Ybar
+    const float* Y[kMaxButcher];
+    float* K[kMaxButcher];
+    float* kbar[kMaxButcher];
+    Y[0] = y0;
+    for (int i = 1; i < ns; ++i) Y[i] = work + (int64_t)(i - 1) * n;
+    for (int i = 0; i < ns - 1; ++i) K[i] = work + (int64_t)(ns - 1 + i) * n;
+    for (int i = 0; i < ns; ++i) kbar[i] = work + (int64_t)(2 * ns - 2 + i) * n;
+    float* Yb = work + (int64_t)(3 * ns - 2) * n;
+    // the step's stage inputs again: Y_s = y0 + dt sum_j a_sj k_j, k_j = F(B(Y_j))
+    cudaError_t e = cudaSuccess;
+    for (int st = 1; st < ns && !e; ++st) {
+        const int r = qg_rhs(p, Y[st - 1], K[st - 1], params, QG_RHS_APPLY_BC, stream);
+        if (r != QG_OK) return r;
+        float c[kMaxButcher];
+        for (int j = 0; j < st; ++j) c[j] = (float)(dt * tb->a[st][j]);
+        e = launch_lincomb(const_cast<float*>(Y[st]), y0, K, c, st, n, s);
+    }
+    // reverse sweep: kbar_s = dt b_s g; per stage from the last, Ybar = F_vjp(Y_s; kbar_s),
+    // then y_bar += Ybar and kbar_j += dt a_sj Ybar (j < s)
+    if (!e) {
+        float c[kMaxButcher];
+        for (int j = 0; j < ns; ++j) c[j] = (float)(dt * tb->b[j]);
+        e = launch_fanout(y_bar, kbar, c, ns, n, s);
+    }
+    if (!e) e = cudaMemsetAsync(p->vjp_acc, 0, (size_t)p->n_members * QG_NPARAMS * sizeof(double), s);
+    for (int st = ns - 1; st >= 0 && !e; --st) {
+        e = rhs_vjp_core(p, Y[st], params, kbar[st], Yb, 1, s);
+        float c[kMaxButcher];
+        for (int j = 0; j < st; ++j) c[j] = (float)(dt * tb->a[st][j]);
+        if (!e) e = launch_scatter_bar(y_bar, Yb, kbar, c, st, n, s);
+    }
+    if (!e && params_bar) e = launch_vjp_params_only(vjp_args(p), params_bar, s);
     return cuda_err(e);
 }
 
@@ -1537,3 +1660,16 @@ int autotune_engine(qg_plan* p) {
 }
 
 }  // namespace
+
+namespace qg {
+// Every scheme in Butcher form (the shallow-water stepper): Euler and Tsit5 as above, Heun
+// (diffrax.Heun: c = [0, 1], b = [1/2, 1/2]) and the Shu-Osher SSP-RK3 (a21 = 1,
+// a31 = a32 = 1/4, b = [1/6, 1/6, 2/3]).
+const Tableau* swm_tableau(int scheme) {
+    static const Tableau heun = {2, {{0, 0}, {1.0, 0}}, {0.5, 0.5}};
+    static const Tableau ssprk3 = {3, {{0, 0, 0}, {1.0, 0, 0}, {0.25, 0.25, 0}}, {1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0}};
+    if (scheme == QG_SCHEME_HEUN) return &heun;
+    if (scheme == QG_SCHEME_SSPRK3) return &ssprk3;
+    return butcher(scheme);
+}
+}  // namespace qg

@@ -166,17 +166,25 @@ def _stream_handle(device) -> C.c_void_p:
 
 def lsweep_classes(spec, rows: int) -> set:
     """Strip classes of a member's layer-per-warp sweep items with ``rows``-row strips: 0 =
-    every column and row the strip reads strictly inside the member, 1 = edge strip, 2 =
-    masked member (one kernel launch per class and layer count present)."""
+    every column and row the strip reads strictly inside the member, 1 = edge strip in x and
+    y, 2 = masked member, 3 = edge in x only, 4 = edge in y only (one kernel launch per class
+    and layer count present)."""
     if spec.mask is not None:
         return {2}
     Ny, Nx = spec.ny + 2, spec.nx + 2
+    # row bands: a remainder of fewer than 8 rows joins the last full band (lsweep_bands)
+    bands = (Ny + rows - 1) // rows
+    rem = Ny - (bands - 1) * rows
+    if bands > 1 and rem < 8 and rows + rem <= 64:
+        bands -= 1
     out = set()
-    for sy in range((Ny + rows - 1) // rows):
+    for sy in range(bands):
         for sx in range((Nx + 59) // 60):
             x0, jb = 60 * sx, rows * sy
-            rhi = min(jb + rows, Ny) + 1
-            out.add(0 if (x0 - 2 >= 1 and x0 + 61 <= Nx - 2 and jb - 2 >= 1 and rhi <= Ny - 2) else 1)
+            rhi = (Ny if sy == bands - 1 else jb + rows) + 1
+            xin = x0 - 2 >= 1 and x0 + 61 <= Nx - 2
+            yin = jb - 2 >= 1 and rhi <= Ny - 2
+            out.add((0 if yin else 4) if xin else (3 if yin else 1))
     return out
 
 
@@ -278,6 +286,26 @@ class Plan:
                                  C.c_void_p(p_bar.data_ptr() if p_bar is not None else None), flags,
                                  _stream_handle(q.device)), "qg_rhs_vjp")
         return q_bar, p_bar
+
+    def step_vjp(self, y0: torch.Tensor, params: torch.Tensor, dt: float, scheme: str, g: torch.Tensor,
+                 want_params: bool = True):
+        """(y0_bar, params_bar) of one ``step`` of ``scheme`` from ``y0`` for the cotangent ``g`` of
+        its result (``qg_step_vjp``: stage recomputation and reverse sweep in one call)."""
+        self._check_field(y0, "y0")
+        self._check_field(g, "g")
+        params = self._params(params, y0.device)
+        work = getattr(self, "_vjp_work", {}).get((scheme, y0.device))
+        if work is None:
+            n = int(self._L.qg_step_vjp_workspace(self._h, SCHEMES[scheme]))
+            work = torch.empty(n, dtype=torch.float32, device=y0.device)
+            self._vjp_work = {**getattr(self, "_vjp_work", {}), (scheme, y0.device): work}
+        y_bar = g.detach().clone()
+        p_bar = torch.empty_like(params) if want_params else None
+        check(self._L.qg_step_vjp(self._h, C.c_void_p(y0.data_ptr()), C.c_void_p(params.data_ptr()), float(dt),
+                                  SCHEMES[scheme], C.c_void_p(y_bar.data_ptr()),
+                                  C.c_void_p(p_bar.data_ptr() if p_bar is not None else None),
+                                  C.c_void_p(work.data_ptr()), _stream_handle(y0.device)), "qg_step_vjp")
+        return y_bar, p_bar
 
     def invert_vjp(self, psi_bar: torch.Tensor) -> torch.Tensor:
         """q_bar of ``invert(q)`` for the cotangent ``psi_bar`` (the map is linear in q)."""

@@ -54,10 +54,11 @@ class Spec(types.SimpleNamespace):
 
 
 @pytest.mark.parametrize("nx,ny,rows,expected", [
-    (128, 128, 16, {0, 1}),   # 130 wide: strips 0, 1 (interior rows), 2 (10 columns)
-    (64, 64, 16, {1}),        # 66 wide: both strips touch the edge
-    (256, 256, 64, {0, 1}),
+    (128, 128, 16, {0, 1, 3, 4}),  # 130 wide: strips 0, 2 touch x edges, strip 1 only the top / bottom bands
+    (64, 64, 16, {1, 3}),          # 66 wide: both strips touch the x edges
+    (256, 256, 64, {0, 1, 3, 4}),
     (3, 5, 16, {1}),
+    (128, 40, 32, {1, 4}),         # 42 rows: no band strictly inside (the 10-row remainder has its own band)
 ])
 def test_lsweep_strip_classes(nx, ny, rows, expected):
     assert lsweep_classes(Spec(nx=nx, ny=ny, mask=None), rows) == expected

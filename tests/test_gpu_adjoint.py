@@ -237,3 +237,31 @@ def test_c5_adjoint_vs_fp32_differences_20_directions():
 
     fd_tau = OA.fd_directional(L_tau, np.array([tau]), np.array([1.0]), rel=1e-3)
     assert gtau == pytest.approx(fd_tau, rel=RTOL_GRAD)
+
+
+@pytest.mark.parametrize("scheme", ["euler", "heun", "ssprk3", "tsit5"])
+@pytest.mark.parametrize("precision", ["fp32", "bf16x3"])
+def test_step_vjp_fused_equals_torch_form(scheme, precision):
+    """``qg_step_vjp`` (stage recomputation and reverse sweep in one C-ABI call with fused
+    linear-combination kernels) against the same algebra written with torch operations around
+    ``qg_rhs`` / ``qg_rhs_vjp``: the same kernels in the same order, so within FP32 rounding of
+    the combination order (1e-6), for the state and the parameter cotangents.  Two calls in a
+    row on the same workspace agree to the same bound (not bit for bit: the VJP stencil sums
+    the layers' contributions to the modal right-hand side with atomic adds, whose order
+    varies)."""
+    from somax_gb300 import adjoint as A
+
+    m, _ = pair(40, 33, 3, precision=precision, **PHYS)
+    plan = m.plan()
+    y0 = cuda(field(m.shape, 41)).reshape(-1)
+    g = cuda(field(m.shape, 42, scale=1.0)).reshape(-1)
+    pv = m._param_vector(y0.device)
+    yb, pb = A.step_vjp(plan, y0, pv, 1200.0, scheme, g)
+    yb2, pb2 = A.step_vjp(plan, y0, pv, 1200.0, scheme, g)
+    yt, pt = A.step_vjp_torch(plan, y0, pv, 1200.0, scheme, g)
+    assert plan.status() == 0
+    assert rel(yb2, yb.cpu().double().numpy()) < 1e-6 and rel(pb2, pb.cpu().double().numpy()) < 1e-6
+    assert rel(yb, yt.cpu().double().numpy()) < 1e-6
+    for k in range(4):
+        if float(pt[k]) != 0.0:
+            assert abs(float(pb[k]) - float(pt[k])) <= 1e-5 * abs(float(pt[k])), (k, float(pb[k]), float(pt[k]))

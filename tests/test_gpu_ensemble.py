@@ -115,8 +115,9 @@ def test_ensemble_parameters_per_member():
 
 def test_parallel_sweep_branches_bitwise_equal_serial():
     """The layer-per-warp sweep's (layer count, strip class) launches forked as parallel graph
-    branches give the same bits as the same launches one after another: ten groups (1-5 layers,
-    interior and edge strips), so that nine side branches share the plan's four side streams,
+    branches give the same bits as the same launches one after another: twenty groups (1-5
+    layers, interior strips and the three kinds of edge strip), so that nineteen side branches
+    share the plan's four side streams,
     stepped 19 steps (two replays of the eight-step graph with programmatic dependent launch
     across the join, then three of the one-step graph)."""
     specs = [((130, 98), 1, 21), ((130, 98), 2, 22), ((190, 150), 3, 23), ((130, 130), 4, 24), ((200, 140), 5, 25)]
@@ -127,7 +128,7 @@ def test_parallel_sweep_branches_bitwise_equal_serial():
         qs.append(torch.tensor(q, dtype=torch.float32, device="cuda"))
     ens = sg.QGEnsemble(ms, precision="bf16x3", persistent=False, stencil="lsweep32", cluster=False)
     groups = {(m.spec.n_layers, c) for m in ms for c in sg.qg.lsweep_classes(m.spec, 32)}
-    assert len(groups) == 10
+    assert len(groups) == 20
     q0 = ens.pack(qs)
     a = q0.clone()
     ens.step(a, 1200.0, 19, "ssprk3")

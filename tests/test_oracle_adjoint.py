@@ -93,6 +93,10 @@ class FakePlan:
             gq, gp = torch.autograd.grad(out, (qq, pp), g)
         return gq, (gp if want_params else None)
 
+    def step_vjp(self, y0, p, dt, scheme, g):
+        # the library's qg_step_vjp runs this algebra in one call; here its torch form
+        return A.step_vjp_torch(self, y0, p, dt, scheme, g)
+
     def step(self, q, p, dt, n, scheme, apply_bc=True):
         a, b = rk_tableau(scheme)
         y = _ring_zero(q) if apply_bc else q.clone()
