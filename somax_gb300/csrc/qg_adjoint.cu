@@ -1,5 +1,12 @@
 // Hand-written adjoint (vector-Jacobian product) of the fused RHS and of the PV inversion.
 //
+// Masked members (land mask): q is read as 0 on land, psi is 0 there and dq = 0 there (wind
+// included), lap(q) is zero on land as on the ring; so the cotangent a, qb, psi and M Lf(a)
+// are zeroed on land, and so are the cotangents of q and psi at land cells.  The masked
+// inversion (two DST solves around the capacitance correction, psi = G x - G E C^-1 R G x with
+// G the symmetric solve, C = R G E and R / E the restriction to / extension from the land
+// boundary points) is a symmetric map, so the adjoint solve is the same masked inversion.
+//
 // Forward, per member (baroclinic.py:135-190; B is the optional ring zeroing of q, Z the
 // zeroing of the psi ring of the baroclinic model, nu4 the biharmonic extension):
 //   qb  = B q,   psi = Z Cm2l L^-1 Cl2m qb
@@ -85,15 +92,18 @@ __global__ void __launch_bounds__(NT) k_vjp_stencil(const MemberDev* __restrict_
             for (int c = threadIdx.x; c < SY * SX; c += NT) {
                 const int y = c / SX, x = c % SX, j = j0 + y, i = i0 + x;
                 const bool in = j >= 0 && j < Ny && i >= 0 && i < Nx;
-                sa[y][x] = (in && interior(j, i, Ny, Nx)) ? gbar[cidx(M, l, j, i)] : 0.f;
-                sq[y][x] = (in && !(apply_bc && on_ring(j, i, Ny, Nx))) ? q[cidx(M, l, j, i)] : 0.f;
-                sp[y][x] = in ? psi[cidx(M, l, j, i)] : 0.f;
+                // land of a masked member: dq = 0 there, q is read as 0 and psi is 0
+                const bool land = in && is_land(M.mask, Ny, Nx, j, i);
+                sa[y][x] = (in && interior(j, i, Ny, Nx) && !land) ? gbar[cidx(M, l, j, i)] : 0.f;
+                sq[y][x] = (in && !(apply_bc && on_ring(j, i, Ny, Nx)) && !land) ? q[cidx(M, l, j, i)] : 0.f;
+                sp[y][x] = (in && !land) ? psi[cidx(M, l, j, i)] : 0.f;
             }
             __syncthreads();
             for (int c = threadIdx.x; c < SY * SX; c += NT) {
                 const int y = c / SX, x = c % SX, j = j0 + y, i = i0 + x;
-                float v = 0.f;
-                if (y > 0 && x > 0 && y < SY - 1 && x < SX - 1 && interior(j, i, Ny, Nx))
+                float v = 0.f;  // lap(qb) is zero on the ring and on land
+                if (y > 0 && x > 0 && y < SY - 1 && x < SX - 1 && interior(j, i, Ny, Nx) &&
+                    !is_land(M.mask, Ny, Nx, j, i))
                     v = (sa[y][x + 1] - 2.f * sa[y][x] + sa[y][x - 1]) * idx2 +
                         (sa[y + 1][x] - 2.f * sa[y][x] + sa[y - 1][x]) * idy2;
                 sm[y][x] = v;
@@ -134,10 +144,11 @@ __global__ void __launch_bounds__(NT) k_vjp_stencil(const MemberDev* __restrict_
                     (A(0, 1) - 2.f * A(0, 0) + A(0, -1)) * idx2 + (A(1, 0) - 2.f * A(0, 0) + A(-1, 0)) * idy2;
                 const float lfm = (sm[y][x + 1] - 2.f * sm[y][x] + sm[y][x - 1]) * idx2 +
                                   (sm[y + 1][x] - 2.f * sm[y][x] + sm[y - 1][x]) * idy2;
-                direct[xidx(M, l, j, i)] = -jg * M.inv_12dxdy + nu * lfa - nu4 * lfm;
+                const bool land_b = is_land(M.mask, Ny, Nx, j, i);  // q and psi of land cells are fixed at 0
+                direct[xidx(M, l, j, i)] = land_b ? 0.f : -jg * M.inv_12dxdy + nu * lfa - nu4 * lfm;
                 float pb = -jf * M.inv_12dxdy - jb * M.beta_12dx;
                 if (l == nl - 1) pb -= kappa * lfa;
-                if (!(zero_psi_ring && on_ring(j, i, Ny, Nx)))
+                if (!(zero_psi_ring && on_ring(j, i, Ny, Nx)) && !land_b)
                     for (int m = 0; m < nl; ++m) atomicAdd(&rhs[xidx(M, m, j, i)], M.Cm2l[l * kMaxLayers + m] * pb);
                 if (interior(j, i, Ny, Nx)) {
                     const float lq = (G(0, 0, 0, 1) - 2.f * G(0, 0, 0, 0) + G(0, 0, 0, -1)) * idx2 +
@@ -186,6 +197,7 @@ __global__ void __launch_bounds__(NT) k_vjp_tau(const MemberDev* __restrict__ me
     const int64_t n = (int64_t)M.Ny * M.Nx;
     for (int64_t c = blockIdx.x * (int64_t)NT + threadIdx.x; c < n; c += (int64_t)gridDim.x * NT) {
         const int j = (int)(c / M.Nx), i = (int)(c % M.Nx);
+        if (is_land(M.mask, M.Ny, M.Nx, j, i)) continue;  // dq = 0 on land, wind included
         acc += (double)gbar[cidx(M, 0, j, i)] * M.F[j] * M.invH0;
     }
     acc = warp_sum(acc);
@@ -214,7 +226,7 @@ __global__ void __launch_bounds__(NT) k_vjp_operand(const MemberDev* __restrict_
         if (j >= M.Ny || i >= M.Nx) continue;
         float pb[kMaxLayers];
         if (psi_bar) {
-            const bool zero = !M.barotropic && on_ring(j, i, M.Ny, M.Nx);
+            const bool zero = (!M.barotropic && on_ring(j, i, M.Ny, M.Nx)) || is_land(M.mask, M.Ny, M.Nx, j, i);
             for (int l = 0; l < nl; ++l) pb[l] = zero ? 0.f : psi_bar[cidx(M, l, j, i)];
         }
         for (int m = 0; m < nl; ++m) {
@@ -250,7 +262,8 @@ __global__ void __launch_bounds__(NT) k_vjp_finish(const MemberDev* __restrict__
     for (int c = threadIdx.x; c < TXr * TYr; c += NT) {
         const int j = t.ty * TYr + c / TXr, i = t.tx * TXr + c % TXr;
         if (j >= M.Ny || i >= M.Nx) continue;
-        const bool zero = apply_bc && on_ring(j, i, M.Ny, M.Nx);
+        // q of the ring (under the BC) and of land cells is not read by the forward
+        const bool zero = (apply_bc && on_ring(j, i, M.Ny, M.Nx)) || is_land(M.mask, M.Ny, M.Nx, j, i);
         float xb[kMaxLayers];
         for (int m = 0; m < nl; ++m) xb[m] = xbar[xidx(M, m, j, i)];
         for (int l = 0; l < nl; ++l) {

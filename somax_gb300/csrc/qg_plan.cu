@@ -1413,8 +1413,9 @@ namespace {
 cudaError_t rhs_vjp_core(qg_plan* p, const float* q, const float* params, const float* dq_bar, float* q_bar,
                          int bc, cudaStream_t s) {
     // forward psi (layer, caller packing) into the YA plane, which holds at least one field
+    // (the masked inversion for members with land)
     cudaError_t e = run_prep(p, q, nullptr, 0, bc, s);
-    if (!e) e = run_dst_solve(p, s);
+    if (!e) e = run_inversion(p, s);
     if (!e)
         e = timed(p, QG_K_OTHER, s, [&] {
             return launch_mode_to_layer(p->md, p->st_tiles, p->n_st, p->st_large, p->XC, p->YA, s, use_pdl(p));
@@ -1431,7 +1432,7 @@ cudaError_t rhs_vjp_core(qg_plan* p, const float* q, const float* params, const 
     if (!e) e = cudaMemsetAsync(p->XB, 0, (size_t)p->xplane * sizeof(float), s);
     if (!e) e = timed(p, QG_K_STENCIL, s, [&] { return launch_vjp_stencil(v, s); });
     if (!e) e = timed(p, QG_K_PREP, s, [&] { return launch_vjp_operand(v, nullptr, s); });
-    if (!e) e = run_dst_solve(p, s);
+    if (!e) e = run_inversion(p, s);  // the adjoint solve: the inversion is self-adjoint
     if (!e) e = timed(p, QG_K_OTHER, s, [&] { return launch_vjp_finish(v, p->XC, q_bar, nullptr, s); });
     return e;
 }
@@ -1441,7 +1442,6 @@ int qg_rhs_vjp(qg_plan* p, const float* q, const float* params, const float* dq_
                float* params_bar, int flags, void* stream) {
     if (!p || !q || !params || !dq_bar || !q_bar) return QG_ERR_NULL;
     if (flags & ~QG_RHS_APPLY_BC) return QG_ERR_ARG;
-    if (p->n_cap > 0) return QG_ERR_UNSUPPORTED;  // no adjoint of the masked inversion yet
     cudaStream_t s = (cudaStream_t)stream;
     const int bc = (flags & QG_RHS_APPLY_BC) ? 1 : 0;
     cudaError_t e = cudaMemsetAsync(p->vjp_acc, 0, (size_t)p->n_members * QG_NPARAMS * sizeof(double), s);
@@ -1459,7 +1459,6 @@ int64_t qg_step_vjp_workspace(const qg_plan* p, int scheme) {
 int qg_step_vjp(qg_plan* p, const float* y0, const float* params, double dt, int scheme, float* y_bar,
                 float* params_bar, float* work, void* stream) {
     if (!p || !y0 || !params || !y_bar || !work) return QG_ERR_NULL;
-    if (p->n_cap > 0) return QG_ERR_UNSUPPORTED;
     const Tableau* tb = swm_tableau(scheme);
     if (!tb || !(dt == dt)) return QG_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
@@ -1504,11 +1503,10 @@ int qg_step_vjp(qg_plan* p, const float* y0, const float* params, double dt, int
 
 int qg_invert_vjp(qg_plan* p, const float* psi_bar, float* q_bar, void* stream) {
     if (!p || !psi_bar || !q_bar) return QG_ERR_NULL;
-    if (p->n_cap > 0) return QG_ERR_UNSUPPORTED;
     cudaStream_t s = (cudaStream_t)stream;
     VjpArgs v = vjp_args(p);
     cudaError_t e = timed(p, QG_K_PREP, s, [&] { return launch_vjp_operand(v, psi_bar, s); });
-    if (!e) e = run_dst_solve(p, s);
+    if (!e) e = run_inversion(p, s);  // self-adjoint, masked members included
     if (!e) e = timed(p, QG_K_OTHER, s, [&] { return launch_vjp_finish(v, p->XC, q_bar, nullptr, s); });
     return cuda_err(e);
 }

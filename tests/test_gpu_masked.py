@@ -119,9 +119,101 @@ def test_ensemble_mixes_masked_and_open_members():
         assert rel(got, ref) < RTOL_STEP
 
 
-def test_masked_adjoint_is_refused():
-    mask = tc.land_mask(20, 20, frac=0.15, seed=1)
-    m, _ = pair(20, 20, 2, mask)
-    q = cuda(field((2, 22, 22), 6))
-    with pytest.raises(RuntimeError):
-        m.plan().rhs_vjp(q, m._param_vector(torch.device("cuda")), q, apply_bc=True)
+def _dense_jacobian(f, x, h=1e-7):
+    """Columns (f(x + h e_j) - f(x - h e_j)) / 2h: exact up to rounding for the masked RHS
+    (quadratic in q) and the masked inversion (linear)."""
+    x = np.asarray(x, np.float64)
+    cols = []
+    for j in range(x.size):
+        e = np.zeros(x.size)
+        e[j] = h
+        cols.append(((f((x.ravel() + e).reshape(x.shape)) - f((x.ravel() - e).reshape(x.shape))) / (2 * h)).ravel())
+    return np.stack(cols, axis=1)
+
+
+@pytest.mark.parametrize("barotropic,apply_bc", [(False, True), (False, False), (True, True)])
+@pytest.mark.parametrize("precision", ["fp32", "bf16x3"])
+def test_masked_rhs_vjp_dense(barotropic, apply_bc, precision):
+    """qg_rhs_vjp of a masked member against the transposed dense Jacobian of the float64 masked
+    RHS (land rules: q read as 0, psi = 0, dq = 0 and lap q = 0 on land; the capacitance
+    correction around the DST solve), and the parameter cotangents against the float64
+    parameter derivatives.  RTOL_MASK (the masked inversion's FP32 floor)."""
+    nx, ny, nl = 20, 16, 1 if barotropic else 2
+    mask = tc.land_mask(ny, nx, frac=0.15, seed=4)
+    m, o = pair(nx, ny, nl, mask, precision, barotropic=barotropic)
+    shape = m.shape
+    q = field((nl, ny + 2, nx + 2), 8).reshape(shape)
+    g = np.random.default_rng(9).standard_normal(shape)
+    q32 = q.astype(np.float32).astype(np.float64)
+
+    def F(x):
+        xx = O.apply_boundary_conditions(o, x) if apply_bc else x
+        return OM.vector_field(o, xx, mask)
+
+    Jt_g = _dense_jacobian(F, q32, h=float(np.abs(q32).max())).T @ g.ravel()
+    pv = m._param_vector(torch.device("cuda"))
+    qb, pb = m.plan().rhs_vjp(cuda(q32).reshape(-1), pv, cuda(g).reshape(-1), apply_bc=apply_bc)
+    assert m.plan().status() == 0
+    assert rel(qb, Jt_g) < RTOL_MASK
+    # parameters: the RHS is affine in each of them
+    names = ("lateral_viscosity", "bottom_drag", "wind_amplitude", "biharmonic_viscosity")
+    base = F(q32)
+    xx = O.apply_boundary_conditions(o, q32) if apply_bc else q32
+    for k, name in enumerate(names):
+        val = float(getattr(o, name))
+        # affine in each parameter: any step is exact; size it so the change is 1e3 |rhs|
+        g1 = OM.vector_field(o, xx, mask, params={name: val + 1.0}) - base
+        h = 1e3 * float(np.linalg.norm(base)) / max(float(np.linalg.norm(g1)), 1e-300)
+        d = (OM.vector_field(o, xx, mask, params={name: val + h}) - base) / h
+        ref = float(np.sum(d * g))
+        if abs(ref) > 0:
+            assert abs(float(pb[k]) - ref) <= 1e-3 * abs(ref), (name, float(pb[k]), ref)
+
+
+@pytest.mark.parametrize("precision,refine", [("fp32", 0), ("bf16x3", 1)])
+def test_masked_invert_vjp_dense(precision, refine):
+    """qg_invert_vjp of a masked member is the transposed dense matrix of the masked inversion
+    (the map is symmetric: the adjoint runs the same capacitance-corrected solve)."""
+    nx, ny, nl = 18, 15, 2
+    mask = tc.land_mask(ny, nx, frac=0.15, seed=11)
+    m, o = pair(nx, ny, nl, mask, precision, refine=refine)
+    shape = m.shape
+    g = np.random.default_rng(12).standard_normal(shape)
+    At_g = _dense_jacobian(lambda x: OM.invert_pv(o, x, mask), np.zeros(shape), h=1.0).T @ g.ravel()
+    qb = m.plan().invert_vjp(cuda(g).reshape(-1))
+    assert m.plan().status() == 0
+    assert rel(qb, At_g) < RTOL_MASK
+
+
+def test_masked_integrate_gradient_vs_float64_differences():
+    """Gradient through 5 SSP-RK3 steps of a masked 3-layer basin (checkpoints every 2) along a
+    random direction of q0 and in tau0, against float64 central differences of the masked
+    oracle (1e-3)."""
+    nx, ny, nl = 24, 20, 3
+    mask = tc.land_mask(ny, nx, frac=0.15, seed=13)
+    m, o = pair(nx, ny, nl, mask, "bf16x3")
+    q0 = np.where(OM.land(mask), 0.0, field((nl, ny + 2, nx + 2), 14)).astype(np.float32).astype(np.float64)
+    w = np.random.default_rng(15).standard_normal(q0.shape)
+    d = np.where(OM.land(mask), 0.0, np.random.default_rng(16).standard_normal(q0.shape)) * 1e-6
+    dt, n = 1200.0, 5
+    tau = float(o.wind_amplitude)
+
+    qt = cuda(q0).requires_grad_(True)
+    m.params = sg.QGParams(torch.tensor(60.0), torch.tensor(1e-7), torch.tensor(tau, requires_grad=True),
+                           torch.tensor(1e9))
+    sol = m.integrate(sg.BaroclinicQGState(q=qt), 0.0, n * dt, dt, solver="ssprk3", checkpoint_every=2)
+    loss = (sol.ys.q[-1].double() * torch.tensor(w, device="cuda")).sum()
+    loss.backward()
+    gd = float((qt.grad.double().cpu().numpy() * d).sum())
+    gtau = float(m.params.wind_amplitude.grad)
+
+    def L(q, t):
+        import dataclasses
+        oo = dataclasses.replace(o, wind_amplitude=t)
+        return float(np.sum(OM.integrate(oo, q, mask, dt, n, "ssprk3") * w))
+
+    eps = 1e-3
+    fd = (L(q0 + eps * d, tau) - L(q0 - eps * d, tau)) / (2 * eps)
+    fdt = (L(q0, tau * (1 + eps)) - L(q0, tau * (1 - eps))) / (2 * eps * tau)
+    assert abs(gd - fd) <= 1e-3 * abs(fd), (gd, fd)
+    assert abs(gtau - fdt) <= 1e-3 * abs(fdt), (gtau, fdt)
