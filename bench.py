@@ -272,7 +272,7 @@ def run_reference(args):
 class Workload:
     """One bench step = one model day of every member, on one device."""
 
-    def __init__(self, name, precision, persistent, dev, seed, stencil=None, gemm_tile=None, cluster=None):
+    def __init__(self, name, precision, persistent, dev, seed, stencil=None, gemm_tile=None, cluster=None, groups=1):
         import torch
 
         import somax_gb300 as sg
@@ -289,7 +289,7 @@ class Workload:
                 q0s.append(tc.initial_pv(cfg, seed=pv_seed).astype(np.float32))
                 cfgs.append(cfg)
             self.ens = sg.QGEnsemble(models, precision=precision, persistent=persistent, device=dev, stencil=stencil,
-                                     gemm_tile=gemm_tile, cluster=cluster)
+                                     gemm_tile=gemm_tile, cluster=cluster, groups=groups)
             self.plan = self.ens.plan
             self.params = self.ens.params(dev)
             self.q0 = np.concatenate([q.reshape(-1) for q in q0s])
@@ -571,6 +571,8 @@ def main():
                     help="force a stencil variant (tile32x8 | tile64x16 | sweep16 | sweep32 | sweep64 | lsweep16 | lsweep32 | lsweep64); "
                          "default: the autotuner's pick")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--groups", type=int, default=1,
+                    help="ensemble only: split the members into this many plans stepped concurrently on their own streams")
     ap.add_argument("--cluster", default="auto", choices=["auto", "on", "off"],
                     help="cluster-resident stepping of small members: autotuned, forced on, or off")
     args = ap.parse_args()
@@ -593,7 +595,7 @@ def main():
         dist.init_process_group("nccl", device_id=dev)
 
     W = Workload(args.config, args.precision, bool(args.persistent), dev, rank, args.stencil, args.gemm_tile,
-                 {"auto": None, "on": True, "off": False}[args.cluster])
+                 {"auto": None, "on": True, "off": False}[args.cluster], args.groups)
     plan = W.plan
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
 
@@ -666,7 +668,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": vs_baseline, "dtype": "f32", "data": "synthetic",
         "config": {"workload": W.describe,
-                   "precision": args.precision, "persistent": bool(args.persistent),
+                   "precision": args.precision, "persistent": bool(args.persistent), "groups": args.groups,
                    "l2": "flushed between timed steps (256 MB write)",
                    "replicas": "independent basins per rank" if world > 1 else "one device",
                    "tuning": dict(plan.tuning(), engine=plan.engine()), "status": status},

@@ -192,6 +192,11 @@ int qg_project(qg_plan* plan, const float* h, const float* u, const float* v, fl
 
 /* Kinetic energy and enstrophy per layer: ke, ens each sum(n_layers) floats (device). */
 int qg_diagnose(qg_plan* plan, const float* q, float* ke, float* ens, void* stream);
+/* The whole diagnose record (baroclinic.py:197-228) with one inversion: psi, u = -d_y psi (V
+   points), v = d_x psi (U points), zeta = lap psi (packed fields like q, ring 0 for u, v, zeta),
+   and ke, ens as qg_diagnose. */
+int qg_diagnose_fields(qg_plan* plan, const float* q, float* psi, float* u, float* v, float* zeta, float* ke,
+                       float* ens, void* stream);
 
 /* qg_invert for one member without a plan and without allocating device memory.
    No counterpart in the reference: this is for callers that may not allocate at the time

@@ -102,6 +102,7 @@ def lib() -> C.CDLL:
         "qg_project": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, vp, vp]),
         "qg_plan_set_wait_limit": (C.c_int, [vp, i64]),
         "qg_state_stats": (C.c_int, [vp, vp, vp, vp]),
+        "qg_diagnose_fields": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, vp, vp]),
         "qg_step_vjp_workspace": (i64, [vp, C.c_int]),
         "qg_step_vjp": (C.c_int, [vp, vp, vp, C.c_double, C.c_int, vp, vp, vp, vp]),
         "qg_swm_create": (C.c_int, [C.POINTER(SwmDesc), C.POINTER(vp)]),

@@ -237,6 +237,8 @@ cudaError_t launch_diag_acc(const MemberDev* members, const StencilTile* tiles, 
 // min / mean / max of the finite entries and the non-finite count of n floats into out[0..3]
 // (device doubles); acc: 32 bytes of device scratch
 cudaError_t launch_state_stats(const float* q, int64_t n, void* acc, double* out, int grid, cudaStream_t s);
+cudaError_t launch_diag_fields(const MemberDev* members, const StencilTile* tiles, int ntiles, int large,
+                               const float* psi, float* u, float* v, float* zeta, cudaStream_t s);
 cudaError_t launch_diag_finish(const double* acc, int64_t n_layers, float* ke, float* ens,
                                cudaStream_t s);
 // geostrophic projection of a shallow-water state (h, u, v): the PV q in front of the

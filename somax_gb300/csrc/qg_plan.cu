@@ -1525,6 +1525,30 @@ int qg_diagnose(qg_plan* p, const float* q, float* ke, float* ens, void* stream)
     return cuda_err(e);
 }
 
+int qg_diagnose_fields(qg_plan* p, const float* q, float* psi, float* u, float* v, float* zeta, float* ke,
+                       float* ens, void* stream) {
+    if (!p || !q || !psi || !u || !v || !zeta || !ke || !ens) return QG_ERR_NULL;
+    cudaStream_t s = (cudaStream_t)stream;
+    // one inversion: psi_hat stays in XC for the KE reduction
+    cudaError_t e = run_prep(p, q, nullptr, 0, 0, s);
+    if (!e) e = run_inversion(p, s);
+    if (!e)
+        e = timed(p, QG_K_OTHER, s, [&] {
+            return launch_mode_to_layer(p->md, p->st_tiles, p->n_st, p->st_large, p->XC, psi, s, false);
+        });
+    if (!e)
+        e = timed(p, QG_K_OTHER, s, [&] {
+            return launch_diag_fields(p->md, p->st_tiles, p->n_st, p->st_large, psi, u, v, zeta, s);
+        });
+    if (!e) e = cudaMemsetAsync(p->diag_acc, 0, sizeof(double) * 2 * p->total_layers, s);
+    if (!e)
+        e = timed(p, QG_K_OTHER, s, [&] {
+            return launch_diag_acc(p->md, p->st_tiles, p->n_st, p->st_large, q, p->XC, p->diag_acc, s);
+        });
+    if (!e) e = launch_diag_finish(p->diag_acc, p->total_layers, ke, ens, s);
+    return cuda_err(e);
+}
+
 int qg_state_stats(qg_plan* p, const float* q, double* stats, void* stream) {
     if (!p || !q || !stats) return QG_ERR_NULL;
     const int grid = std::max(1, std::min(p->n_sm * 4, (int)((p->state_size / 4 + 255) / 256)));

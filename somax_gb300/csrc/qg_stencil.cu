@@ -315,6 +315,43 @@ __global__ void __launch_bounds__(NTHREADS) k_diag(const MemberDev* __restrict__
     }
 }
 
+// The velocity and vorticity fields of diagnose (baroclinic.py:197-228) from the layer psi
+// (caller packing): u = -d_y psi on the V points, v = d_x psi on the U points (forward
+// differences written to the interior), zeta = lap(psi) (5-point, interior); the ring is 0.
+__global__ void __launch_bounds__(NTHREADS) k_diag_fields(const MemberDev* __restrict__ members,
+                                                          const StencilTile* __restrict__ tiles, int TX, int TY,
+                                                          const float* __restrict__ psi, float* __restrict__ u,
+                                                          float* __restrict__ v, float* __restrict__ zeta) {
+    const StencilTile t = tiles[blockIdx.x];
+    const MemberDev& M = members[t.member];
+    const int nl = M.nl, Ny = M.Ny, Nx = M.Nx;
+    const float idx = 1.f / M.dx, idy = 1.f / M.dy, idx2 = M.inv_dx2, idy2 = M.inv_dy2;
+    for (int c = threadIdx.x; c < TX * TY; c += blockDim.x) {
+        const int j = t.ty * TY + c / TX, i = t.tx * TX + c % TX;
+        if (j >= Ny || i >= Nx) continue;
+        const bool in = j > 0 && i > 0 && j < Ny - 1 && i < Nx - 1;
+        for (int l = 0; l < nl; ++l) {
+            const int64_t o = caller_idx(M, l, j, i);
+            float uu = 0.f, vv = 0.f, zz = 0.f;
+            if (in) {
+                const float pc = psi[o], pn = psi[o + Nx], ps = psi[o - Nx], pe = psi[o + 1], pw = psi[o - 1];
+                uu = -(pn - pc) * idy;
+                vv = (pe - pc) * idx;
+                zz = (pe - 2.f * pc + pw) * idx2 + (pn - 2.f * pc + ps) * idy2;
+            }
+            u[o] = uu;
+            v[o] = vv;
+            zeta[o] = zz;
+        }
+    }
+}
+
+cudaError_t launch_diag_fields(const MemberDev* members, const StencilTile* tiles, int ntiles, int large,
+                               const float* psi, float* u, float* v, float* zeta, cudaStream_t s) {
+    return launch_k(k_diag_fields, ntiles, NTHREADS, 0, s, false, members, tiles, large ? TileL::TX : TileS::TX,
+                    large ? TileL::TY : TileS::TY, psi, u, v, zeta);
+}
+
 __global__ void k_diag_finish(const double* __restrict__ acc, int64_t n, float* ke, float* ens) {
     pdl_wait();
     pdl_launch_dependents();

@@ -346,6 +346,17 @@ class Plan:
                                      _stream_handle(q.device)), "qg_state_stats")
         return out
 
+    def diagnose_fields(self, q: torch.Tensor):
+        """(psi, u, v, zeta, ke, ens) of the packed field q from one inversion (``qg_diagnose_fields``)."""
+        self._check_field(q, "q")
+        psi, u, v, zeta = (torch.empty_like(q) for _ in range(4))
+        nlt = sum(m.n_layers for m in self.members)
+        ke = torch.empty(nlt, device=q.device, dtype=torch.float32)
+        en = torch.empty(nlt, device=q.device, dtype=torch.float32)
+        ptr = [C.c_void_p(t.data_ptr()) for t in (q, psi, u, v, zeta, ke, en)]
+        check(self._L.qg_diagnose_fields(self._h, *ptr, _stream_handle(q.device)), "qg_diagnose_fields")
+        return psi, u, v, zeta, ke, en
+
     def status(self, device=None) -> int:
         flags = C.c_int(0)
         code = self._L.qg_status(self._h, C.byref(flags), _stream_handle(device or self.device))
@@ -653,27 +664,18 @@ class _QGBase(SomaxModel):
         return Solution(ts=ts, ys=self.state_cls(q=torch.stack(ys)))
 
     def diagnose(self, state) -> QGDiagnostics:
+        """``diagnose`` (``baroclinic.py:197-228``): psi, u, v, relative vorticity, KE and
+        enstrophy per layer, all from one inversion on the GPU (``qg_diagnose_fields``)."""
         q = self._field(state.q)
         plan = self.plan(q.device)
-        psi = plan.invert(q)
-        ke, en = plan.diagnose(q)
-        g = self.grid
-        p3 = psi.reshape((-1, g.Ny, g.Nx))
-        u = torch.zeros_like(p3)
-        v = torch.zeros_like(p3)
-        u[:, 1:-1, 1:-1] = -(p3[:, 2:, 1:-1] - p3[:, 1:-1, 1:-1]) / g.dy
-        v[:, 1:-1, 1:-1] = (p3[:, 1:-1, 2:] - p3[:, 1:-1, 1:-1]) / g.dx
-        zeta = torch.zeros_like(p3)
-        c = p3[:, 1:-1, 1:-1]
-        zeta[:, 1:-1, 1:-1] = (p3[:, 1:-1, 2:] - 2 * c + p3[:, 1:-1, :-2]) / g.dx**2 + (
-            p3[:, 2:, 1:-1] - 2 * c + p3[:, :-2, 1:-1]) / g.dy**2
-        shp = psi.shape
+        shp = q.shape
+        psi, u, v, zeta, ke, en = plan.diagnose_fields(q.reshape(-1).contiguous())
         radii = None if self.modal is None else self.modal.rossby_radii
         if self.barotropic:
             ke, en = ke[0], en[0]
-        return QGDiagnostics(psi=psi, u=u.reshape(shp), v=v.reshape(shp), kinetic_energy=ke,
+        return QGDiagnostics(psi=psi.view(shp), u=u.view(shp), v=v.view(shp), kinetic_energy=ke,
                              total_kinetic_energy=ke.sum(), enstrophy=en, total_enstrophy=en.sum(),
-                             relative_vorticity=zeta.reshape(shp), rossby_radii=radii)
+                             relative_vorticity=zeta.view(shp), rossby_radii=radii)
 
 
 class BaroclinicQG(_QGBase):
@@ -743,18 +745,121 @@ class BarotropicQG(_QGBase):
                             gemm_tile=gemm_tile, cluster=cluster)
 
 
+class PlanGroup:
+    """Members split into ``groups`` contiguous ranges of about equal cell count, one ``Plan``
+    each.  The ranges' packed states are contiguous slices of the whole packed state, so a call
+    hands each plan its slice with no copy; ``step`` forks the plans onto their own streams and
+    joins them, so that independent members' launches overlap on the GPU (one group's DST passes
+    beside another's stencil).  Offers the ``Plan`` methods the ensemble uses."""
+
+    def __init__(self, members: Sequence["MemberSpec"], groups: int, device=None, **plan_kw):
+        n = len(members)
+        groups = max(1, min(int(groups), n))
+        cells = [m.cells for m in members]
+        total, bounds, acc = float(sum(cells)), [0], 0.0
+        for i, c in enumerate(cells):
+            acc += c
+            if len(bounds) < groups and i + 1 < n and acc >= total * len(bounds) / groups:
+                bounds.append(i + 1)
+        bounds.append(n)
+        self.ranges = list(zip(bounds[:-1], bounds[1:]))
+        self.plans = [Plan(list(members[a:b]), device=device, **plan_kw) for a, b in self.ranges]
+        self.device = self.plans[0].device
+        self.members = list(members)
+        self.state_size = sum(p.state_size for p in self.plans)
+        self.bases, base = [], 0
+        for p in self.plans:
+            self.bases.append(base)
+            base += p.state_size
+        self.offsets = [b + o for b, p in zip(self.bases, self.plans) for o in p.offsets]
+        self.streams = [torch.cuda.Stream(device=self.device) for _ in self.plans]
+        self.precision = self.plans[0].precision
+        self.refine = self.plans[0].refine
+        self.persistent = self.plans[0].persistent
+
+    def _slices(self, q: torch.Tensor, params: torch.Tensor):
+        params = params.detach().to(device=q.device, dtype=torch.float32).contiguous()
+        for p, b, (lo, hi) in zip(self.plans, self.bases, self.ranges):
+            yield p, q[b:b + p.state_size], params[4 * lo:4 * hi]
+
+    def step(self, q, params, dt, n_steps, scheme, apply_bc=True):
+        if q.numel() != self.state_size or not q.is_contiguous():
+            raise ValueError(f"q must be contiguous with {self.state_size} elements")
+        cur = torch.cuda.current_stream(q.device)
+        start = torch.cuda.Event()
+        start.record(cur)
+        for (p, qs, ps), st in zip(list(self._slices(q, params)), self.streams):
+            st.wait_event(start)
+            with torch.cuda.stream(st):
+                p.step(qs, ps, dt, n_steps, scheme, apply_bc)
+            done = torch.cuda.Event()
+            done.record(st)
+            cur.wait_event(done)
+        return q
+
+    def rhs(self, q, params, apply_bc=False, out=None):
+        out = torch.empty_like(q) if out is None else out
+        for (p, qs, ps), b in zip(self._slices(q, params), self.bases):
+            p.rhs(qs, ps, apply_bc=apply_bc, out=out[b:b + p.state_size])
+        return out
+
+    def invert(self, q, out=None):
+        out = torch.empty_like(q) if out is None else out
+        for p, b in zip(self.plans, self.bases):
+            p.invert(q[b:b + p.state_size], out=out[b:b + p.state_size])
+        return out
+
+    def status(self, device=None) -> int:
+        codes = [p.status(device) for p in self.plans]
+        return next((c for c in codes if c), 0)
+
+    def launches_per_call(self, n_steps: int, scheme: str) -> int:
+        return sum(p.launches_per_call(n_steps, scheme) for p in self.plans)
+
+    def tuning(self) -> dict:
+        t = dict(self.plans[0].tuning())
+        t["groups"] = [{"members": hi - lo, **{k: v for k, v in p.tuning().items() if k in ("stencil", "gemm_tile_n")}}
+                       for p, (lo, hi) in zip(self.plans, self.ranges)]
+        return t
+
+    def engine(self) -> dict:
+        return self.plans[0].engine()
+
+    def set_profiling(self, on: bool):
+        for p in self.plans:
+            p.set_profiling(on)
+
+    def kernel_stats(self, kclass: int):
+        ms = n = 0
+        for p in self.plans:
+            a, b = p.kernel_stats(kclass)
+            ms += a
+            n += b
+        return ms, n
+
+    def set_parallel_sweep(self, on: bool = True):
+        for p in self.plans:
+            p.set_parallel_sweep(on)
+
+
 class QGEnsemble:
     """Many independent members (any mix of grid sizes, layer counts and parameters) advanced
     together: one plan, every launch covers all members (the persistent step kernel for the
-    tensor-core precisions).  States are packed member after member in the reference layout."""
+    tensor-core precisions); with ``groups`` > 1 the members are split into that many plans
+    stepped concurrently on their own streams (``PlanGroup``).  States are packed member after
+    member in the reference layout."""
 
     def __init__(self, models: Sequence[_QGBase], precision="bf16x3", refine=0, use_graphs=True, persistent=True,
-                 device=None, stencil=None, gemm_tile=None, cluster=None):
+                 device=None, stencil=None, gemm_tile=None, cluster=None, groups: int = 1):
         if not models:
             raise ValueError("an ensemble needs at least one member")
         self.models = list(models)
-        self.plan = Plan([m.spec for m in self.models], precision, refine, use_graphs, device, persistent,
-                         stencil=stencil, gemm_tile=gemm_tile, cluster=cluster)
+        kw = dict(precision=precision, refine=refine, use_graphs=use_graphs, persistent=persistent, stencil=stencil,
+                  gemm_tile=gemm_tile, cluster=cluster)
+        if groups > 1:
+            self.plan = PlanGroup([m.spec for m in self.models], groups, device=device, **kw)
+        else:
+            self.plan = Plan([m.spec for m in self.models], device=device, **kw)
         self.offsets = self.plan.offsets
         self.sizes = [int(np.prod(m.shape)) for m in self.models]
 

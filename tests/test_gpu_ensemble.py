@@ -142,3 +142,27 @@ def test_parallel_sweep_branches_bitwise_equal_serial():
     assert torch.isfinite(a).all()
     assert torch.equal(a, b)
     assert torch.equal(a, c)
+
+
+def test_member_groups_bitwise_equal_one_plan():
+    """An ensemble split into three plans stepped concurrently on their own streams (groups=3)
+    gives the bits of the one-plan ensemble when the stencil variant and tile width are forced:
+    every member's arithmetic is its own, whatever plan it sits in."""
+    specs = [((64, 64), 1, 31), ((64, 64), 1, 32), ((128, 96), 3, 33), ((96, 80), 3, 34), ((60, 50), 5, 35),
+             ((40, 33), 2, 36)]
+    ms, qs = [], []
+    for n, nl, seed in specs:
+        m, _, q = member(n, nl, seed, "bf16x3", persistent=False)
+        ms.append(m)
+        qs.append(torch.tensor(q, dtype=torch.float32, device="cuda"))
+    kw = dict(precision="bf16x3", persistent=False, stencil="lsweep32", gemm_tile=144, cluster=False)
+    one = sg.QGEnsemble(ms, **kw)
+    three = sg.QGEnsemble(ms, groups=3, **kw)
+    assert len(three.plan.plans) == 3 and three.offsets == one.offsets
+    a = one.pack(qs)
+    b = a.clone()
+    one.step(a, 1200.0, 11, "ssprk3")
+    three.step(b, 1200.0, 11, "ssprk3")
+    assert one.plan.status() == 0 and three.plan.status() == 0
+    assert torch.equal(a, b)
+    assert torch.equal(one.rhs(one.pack(qs)), three.rhs(three.pack(qs)))

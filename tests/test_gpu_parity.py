@@ -204,6 +204,20 @@ def test_diagnose():
     np.testing.assert_allclose(d.kinetic_energy.cpu().numpy(), r["kinetic_energy"], rtol=1e-5)
     np.testing.assert_allclose(d.enstrophy.cpu().numpy(), r["enstrophy"], rtol=1e-5)
     assert rel(d.u, r["u"]) < 1e-5 and rel(d.v, r["v"]) < 1e-5
+    assert rel(d.psi, r["psi"]) < 2e-6 and rel(d.relative_vorticity, r["relative_vorticity"]) < 1e-5
+
+
+def test_diagnose_barotropic_fields():
+    """The full diagnose record from one inversion (qg_diagnose_fields) for a barotropic member
+    (psi ring kept)."""
+    mb = sg.BarotropicQG.create(nx=30, ny=22, Lx=1e6, Ly=8e5)
+    ob = O.barotropic_model(nx=30, ny=22, Lx=1e6, Ly=8e5)
+    qb = field((24, 32), 11)
+    d = mb.diagnose(sg.BarotropicQGState(q=cuda(qb)))
+    r = O.diagnose(ob, qb)
+    assert rel(d.psi, r["psi"]) < 2e-6 and rel(d.u, r["u"]) < 1e-5 and rel(d.relative_vorticity,
+                                                                          r["relative_vorticity"]) < 1e-5
+    assert float(d.kinetic_energy) == pytest.approx(float(r["total_kinetic_energy"]), rel=1e-5)
 
 
 def test_nonfinite_flag():
