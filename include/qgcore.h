@@ -170,9 +170,12 @@ int qg_invert_vjp(qg_plan* plan, const float* psi_bar, float* q_bar, void* strea
 /* Adjoint of one qg_step step (any scheme, in Butcher form) from the state y0 (packed, ring as
    stepped): on entry y_bar is the cotangent of the step's result, on return the cotangent of
    y0; params_bar (may be NULL) receives the parameter cotangents of the step (overwritten).
-   The step's stage inputs are recomputed with the fused right-hand side, then the stages are
-   reversed with qg_rhs_vjp's kernels and fused linear-combination kernels.  work: caller-owned
-   device scratch of qg_step_vjp_workspace(plan, scheme) floats.  The checkpointed adjoint of
+   The step's stage inputs are recomputed with the fused right-hand side (keeping each stage's
+   streamfunction), then the stages are reversed with qg_rhs_vjp's kernels and fused
+   linear-combination kernels.  work: caller-owned
+   device scratch of qg_step_vjp_workspace(plan, scheme) floats.  With graphs on (qg_options)
+   the call's launches are captured once and replayed while y0, params, y_bar, params_bar,
+   work, dt and scheme repeat; a change of any of them captures again.  The checkpointed adjoint of
    integrate (diffrax's recursive checkpointing under eqx.filter_grad,
    tests/models/test_qg_baroclinic.py:293-312) calls it once per step in reverse. */
 int64_t qg_step_vjp_workspace(const qg_plan* plan, int scheme);

@@ -228,6 +228,15 @@ struct StepGraph {
     int scheme = -1;
 };
 
+// The captured launch sequence of one qg_step_vjp call and the arguments it was captured with
+// (replayed while they repeat).
+struct VjpGraph {
+    cudaGraphExec_t exec = nullptr;
+    const void* ptr[5] = {};  // y0, params, y_bar, params_bar, work
+    double dt = 0.0;
+    int scheme = -1;
+};
+
 struct qg_plan {
     int n_members = 0;
     qg_options opts{};
@@ -308,6 +317,7 @@ struct qg_plan {
     cudaEvent_t join_ev[kSweepGroups] = {};
     bool fork_on = true;  // qg_plan_set_parallel_sweep: 0 launches the groups one after another
     StepGraph graph;
+    VjpGraph vjp_graph;
     // profiling
     bool profiling = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev[QG_K_COUNT];
@@ -1233,6 +1243,7 @@ void qg_plan_destroy(qg_plan* p) {
     cudaDeviceSynchronize();
     if (p->graph.exec) cudaGraphExecDestroy(p->graph.exec);
     if (p->graph.exec_k) cudaGraphExecDestroy(p->graph.exec_k);
+    if (p->vjp_graph.exec) cudaGraphExecDestroy(p->vjp_graph.exec);
     for (auto& v : p->ev)
         for (auto& pr : v) {
             cudaEventDestroy(pr.first);
@@ -1300,11 +1311,9 @@ int qg_project(qg_plan* p, const float* h, const float* u, const float* v, float
     return cuda_err(e);
 }
 
-int qg_rhs(qg_plan* p, const float* q, float* dq, const float* params, int flags, void* stream) {
-    if (!p || !q || !dq || !params) return QG_ERR_NULL;
-    if (flags & ~QG_RHS_APPLY_BC) return QG_ERR_ARG;
-    cudaStream_t s = (cudaStream_t)stream;
-    const int bc = (flags & QG_RHS_APPLY_BC) ? 1 : 0;
+namespace {
+// dq = vector_field(q) (with the BC on read when bc), every member, on stream s.
+cudaError_t rhs_core(qg_plan* p, const float* q, float* dq, const float* params, int bc, cudaStream_t s) {
     // q is staged into the S1 plane (TMA-able pitch); the stencil applies the BC on read
     cudaError_t e = run_prep(p, q, p->S1, 0, bc, s);
     if (!e) e = run_inversion(p, s);
@@ -1315,7 +1324,14 @@ int qg_rhs(qg_plan* p, const float* q, float* dq, const float* params, int flags
         a.dq = dq;
         e = timed(p, QG_K_STENCIL, s, [&] { return launch_stencil(p, a, s, use_pdl(p)); });
     }
-    return cuda_err(e);
+    return e;
+}
+}  // namespace
+
+int qg_rhs(qg_plan* p, const float* q, float* dq, const float* params, int flags, void* stream) {
+    if (!p || !q || !dq || !params) return QG_ERR_NULL;
+    if (flags & ~QG_RHS_APPLY_BC) return QG_ERR_ARG;
+    return cuda_err(rhs_core(p, q, dq, params, (flags & QG_RHS_APPLY_BC) ? 1 : 0, (cudaStream_t)stream));
 }
 
 int qg_step(qg_plan* p, float* q, const float* params, double dt, int n_steps, int scheme,
@@ -1409,22 +1425,27 @@ int qg_step(qg_plan* p, float* q, const float* params, double dt, int n_steps, i
 
 namespace {
 // q_bar = (d dq / d q)^T dq_bar of the rhs at q; the parameter cotangents are added to the
-// plan's FP64 accumulators (zeroed by the caller).
+// plan's FP64 accumulators (zeroed by the caller).  psi: the layer psi of q (caller packing)
+// when the caller has it, else null (computed here).
 cudaError_t rhs_vjp_core(qg_plan* p, const float* q, const float* params, const float* dq_bar, float* q_bar,
-                         int bc, cudaStream_t s) {
-    // forward psi (layer, caller packing) into the YA plane, which holds at least one field
-    // (the masked inversion for members with land)
-    cudaError_t e = run_prep(p, q, nullptr, 0, bc, s);
-    if (!e) e = run_inversion(p, s);
-    if (!e)
-        e = timed(p, QG_K_OTHER, s, [&] {
-            return launch_mode_to_layer(p->md, p->st_tiles, p->n_st, p->st_large, p->XC, p->YA, s, use_pdl(p));
-        });
+                         int bc, cudaStream_t s, const float* psi = nullptr) {
+    cudaError_t e = cudaSuccess;
+    if (!psi) {
+        // forward psi (layer, caller packing) into the YA plane, which holds at least one field
+        // (the masked inversion for members with land)
+        e = run_prep(p, q, nullptr, 0, bc, s);
+        if (!e) e = run_inversion(p, s);
+        if (!e)
+            e = timed(p, QG_K_OTHER, s, [&] {
+                return launch_mode_to_layer(p->md, p->st_tiles, p->n_st, p->st_large, p->XC, p->YA, s, use_pdl(p));
+            });
+        psi = p->YA;
+    }
     // stencil transposes: direct cotangent into S2, the adjoint solve's modal rhs into XB
     VjpArgs v = vjp_args(p);
     v.q = q;
     v.apply_bc = bc;
-    v.psi = p->YA;
+    v.psi = psi;
     v.gbar = dq_bar;
     v.params = params;
     v.direct = p->S2;
@@ -1453,35 +1474,42 @@ int qg_rhs_vjp(qg_plan* p, const float* q, const float* params, const float* dq_
 int64_t qg_step_vjp_workspace(const qg_plan* p, int scheme) {
     const Tableau* tb = swm_tableau(scheme);
     if (!p || !tb) return -1;
-    return (int64_t)(3 * tb->n - 1) * p->state_size;
+    return (int64_t)(4 * tb->n - 2) * p->state_size;
 }
 
-int qg_step_vjp(qg_plan* p, const float* y0, const float* params, double dt, int scheme, float* y_bar,
-                float* params_bar, float* work, void* stream) {
-    if (!p || !y0 || !params || !y_bar || !work) return QG_ERR_NULL;
-    const Tableau* tb = swm_tableau(scheme);
-    if (!tb || !(dt == dt)) return QG_ERR_ARG;
-    cudaStream_t s = (cudaStream_t)stream;
+namespace {
+// The launches of one step's adjoint (qg_step_vjp) on stream s.
+cudaError_t step_vjp_body(qg_plan* p, const float* y0, const float* params, double dt, const Tableau* tb,
+                          float* y_bar, float* params_bar, float* work, cudaStream_t s) {
     const int ns = tb->n;
     const int64_t n = p->state_size;
     // work: stage inputs Y_1 .. Y_{ns-1}, stage derivatives k_0 .. k_{ns-2}, their cotangents
-    // kbar_0 .. kbar_{ns-1}, and one stage-input cotangent Ybar
+    // kbar_0 .. kbar_{ns-1}, one stage-input cotangent Ybar, and the layer psi of the stage
+    // inputs Y_0 .. Y_{ns-2} (from the recomputation, so that the reverse sweep inverts only
+    // the last stage's input again)
     const float* Y[kMaxButcher];
     float* K[kMaxButcher];
     float* kbar[kMaxButcher];
+    float* Psi[kMaxButcher];
     Y[0] = y0;
     for (int i = 1; i < ns; ++i) Y[i] = work + (int64_t)(i - 1) * n;
     for (int i = 0; i < ns - 1; ++i) K[i] = work + (int64_t)(ns - 1 + i) * n;
     for (int i = 0; i < ns; ++i) kbar[i] = work + (int64_t)(2 * ns - 2 + i) * n;
     float* Yb = work + (int64_t)(3 * ns - 2) * n;
+    for (int i = 0; i < ns - 1; ++i) Psi[i] = work + (int64_t)(3 * ns - 1 + i) * n;
     // the step's stage inputs again: Y_s = y0 + dt sum_j a_sj k_j, k_j = F(B(Y_j))
     cudaError_t e = cudaSuccess;
     for (int st = 1; st < ns && !e; ++st) {
-        const int r = qg_rhs(p, Y[st - 1], K[st - 1], params, QG_RHS_APPLY_BC, stream);
-        if (r != QG_OK) return r;
+        e = rhs_core(p, Y[st - 1], K[st - 1], params, 1, s);
+        // psi_hat of B(Y_{st-1}) is still in XC: keep its layer psi for the reverse sweep
+        if (!e)
+            e = timed(p, QG_K_OTHER, s, [&] {
+                return launch_mode_to_layer(p->md, p->st_tiles, p->n_st, p->st_large, p->XC, Psi[st - 1], s,
+                                            use_pdl(p));
+            });
         float c[kMaxButcher];
         for (int j = 0; j < st; ++j) c[j] = (float)(dt * tb->a[st][j]);
-        e = launch_lincomb(const_cast<float*>(Y[st]), y0, K, c, st, n, s);
+        if (!e) e = launch_lincomb(const_cast<float*>(Y[st]), y0, K, c, st, n, s);
     }
     // reverse sweep: kbar_s = dt b_s g; per stage from the last, Ybar = F_vjp(Y_s; kbar_s),
     // then y_bar += Ybar and kbar_j += dt a_sj Ybar (j < s)
@@ -1492,13 +1520,55 @@ int qg_step_vjp(qg_plan* p, const float* y0, const float* params, double dt, int
     }
     if (!e) e = cudaMemsetAsync(p->vjp_acc, 0, (size_t)p->n_members * QG_NPARAMS * sizeof(double), s);
     for (int st = ns - 1; st >= 0 && !e; --st) {
-        e = rhs_vjp_core(p, Y[st], params, kbar[st], Yb, 1, s);
+        e = rhs_vjp_core(p, Y[st], params, kbar[st], Yb, 1, s, st < ns - 1 ? Psi[st] : nullptr);
         float c[kMaxButcher];
         for (int j = 0; j < st; ++j) c[j] = (float)(dt * tb->a[st][j]);
         if (!e) e = launch_scatter_bar(y_bar, Yb, kbar, c, st, n, s);
     }
     if (!e && params_bar) e = launch_vjp_params_only(vjp_args(p), params_bar, s);
-    return cuda_err(e);
+    return e;
+}
+}  // namespace
+
+int qg_step_vjp(qg_plan* p, const float* y0, const float* params, double dt, int scheme, float* y_bar,
+                float* params_bar, float* work, void* stream) {
+    if (!p || !y0 || !params || !y_bar || !work) return QG_ERR_NULL;
+    const Tableau* tb = swm_tableau(scheme);
+    if (!tb || !(dt == dt)) return QG_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!p->opts.use_graphs || p->profiling)
+        return cuda_err(step_vjp_body(p, y0, params, dt, tb, y_bar, params_bar, work, s));
+    // a step's adjoint is ~10 launches per stage: captured once per set of arguments and
+    // replayed as one graph while they repeat (callers that stage every step's state and
+    // cotangent in the same buffers replay it every step)
+    VjpGraph& g = p->vjp_graph;
+    const void* ptr[5] = {y0, params, y_bar, params_bar, work};
+    bool same = g.exec && g.dt == dt && g.scheme == scheme;
+    for (int k = 0; k < 5 && same; ++k) same = g.ptr[k] == ptr[k];
+    cudaError_t e = cudaSuccess;
+    if (!same) {
+        if (g.exec) {
+            cudaGraphExecDestroy(g.exec);
+            g.exec = nullptr;
+        }
+        cudaGraph_t graph = nullptr;
+        e = cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal);
+        if (!e) {
+            const cudaError_t e1 = step_vjp_body(p, y0, params, dt, tb, y_bar, params_bar, work, p->cap);
+            e = cudaStreamEndCapture(p->cap, &graph);
+            if (!e) e = e1;
+        }
+        if (!e) e = cudaGraphInstantiate(&g.exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (e) {
+            g.exec = nullptr;
+            return cuda_err(e);
+        }
+        for (int k = 0; k < 5; ++k) g.ptr[k] = ptr[k];
+        g.dt = dt;
+        g.scheme = scheme;
+    }
+    return cuda_err(cudaGraphLaunch(g.exec, s));
 }
 
 int qg_invert_vjp(qg_plan* p, const float* psi_bar, float* q_bar, void* stream) {
@@ -1580,7 +1650,7 @@ int qg_plan_set_parallel_sweep(qg_plan* p, int on) {
         p->fork_on = on == 1;
         // the captured graphs hold the old launch structure
         cudaDeviceSynchronize();
-        for (cudaGraphExec_t* x : {&p->graph.exec, &p->graph.exec_k})
+        for (cudaGraphExec_t* x : {&p->graph.exec, &p->graph.exec_k, &p->vjp_graph.exec})
             if (*x) {
                 cudaGraphExecDestroy(*x);
                 *x = nullptr;

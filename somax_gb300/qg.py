@@ -294,18 +294,25 @@ class Plan:
         self._check_field(y0, "y0")
         self._check_field(g, "g")
         params = self._params(params, y0.device)
-        work = getattr(self, "_vjp_work", {}).get((scheme, y0.device))
-        if work is None:
+        # the call's state, cotangent and parameters go through buffers that stay put from call
+        # to call, so that the library replays its captured graph of the step's adjoint
+        key = (scheme, y0.device)
+        bufs = getattr(self, "_vjp_bufs", {})
+        if key not in bufs:
             n = int(self._L.qg_step_vjp_workspace(self._h, SCHEMES[scheme]))
-            work = torch.empty(n, dtype=torch.float32, device=y0.device)
-            self._vjp_work = {**getattr(self, "_vjp_work", {}), (scheme, y0.device): work}
-        y_bar = g.detach().clone()
-        p_bar = torch.empty_like(params) if want_params else None
-        check(self._L.qg_step_vjp(self._h, C.c_void_p(y0.data_ptr()), C.c_void_p(params.data_ptr()), float(dt),
-                                  SCHEMES[scheme], C.c_void_p(y_bar.data_ptr()),
-                                  C.c_void_p(p_bar.data_ptr() if p_bar is not None else None),
-                                  C.c_void_p(work.data_ptr()), _stream_handle(y0.device)), "qg_step_vjp")
-        return y_bar, p_bar
+            bufs[key] = dict(work=torch.empty(n, dtype=torch.float32, device=y0.device),
+                             y0=torch.empty_like(y0), y_bar=torch.empty_like(y0), params=torch.empty_like(params),
+                             p_bar=torch.empty_like(params))
+            self._vjp_bufs = bufs
+        b = bufs[key]
+        b["y0"].copy_(y0)
+        b["y_bar"].copy_(g)
+        b["params"].copy_(params)
+        check(self._L.qg_step_vjp(self._h, C.c_void_p(b["y0"].data_ptr()), C.c_void_p(b["params"].data_ptr()),
+                                  float(dt), SCHEMES[scheme], C.c_void_p(b["y_bar"].data_ptr()),
+                                  C.c_void_p(b["p_bar"].data_ptr()), C.c_void_p(b["work"].data_ptr()),
+                                  _stream_handle(y0.device)), "qg_step_vjp")
+        return b["y_bar"].clone(), (b["p_bar"].clone() if want_params else None)
 
     def invert_vjp(self, psi_bar: torch.Tensor) -> torch.Tensor:
         """q_bar of ``invert(q)`` for the cotangent ``psi_bar`` (the map is linear in q)."""
