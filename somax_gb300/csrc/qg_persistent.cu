@@ -109,6 +109,7 @@ __device__ void gemm_phase(const PersistArgs& a, uint8_t* smem, Shared& sh, uint
         proxy_fence_shared();  // the stencil phase wrote this shared memory with generic stores
         for (int t = blockIdx.x; t < n && !*abort; t += gridDim.x) {
             const GemmTile tl = tiles[t];
+            if (tl.member < 0) continue;  // a padding entry of the balanced schedule
             const TcMaps* tm = maps + (tl.member * 4 + PASS);
             const TcGeom g = tc_geom<PASS>(a.members[tl.member], a.xplane, a.yplane);
             const int nkb = (g.K + C::BK - 1) / C::BK;
@@ -128,6 +129,7 @@ __device__ void gemm_phase(const PersistArgs& a, uint8_t* smem, Shared& sh, uint
     } else if (warp == 1 && lane == 0) {
         for (int t = blockIdx.x; t < n && !*abort; t += gridDim.x) {
             const GemmTile tl = tiles[t];
+            if (tl.member < 0) continue;  // a padding entry of the balanced schedule
             const TcGeom g = tc_geom<PASS>(a.members[tl.member], a.xplane, a.yplane);
             const int nkb = (g.K + C::BK - 1) / C::BK;
             const uint32_t buf = c.mma_tiles & 1, use = c.mma_tiles >> 1;
@@ -152,6 +154,7 @@ __device__ void gemm_phase(const PersistArgs& a, uint8_t* smem, Shared& sh, uint
         const int part = (warp - 4) >> 2;  // column chunks part, part + EPI / 4, ...
         for (int t = blockIdx.x; t < n; t += gridDim.x) {
             const GemmTile tl = tiles[t];
+            if (tl.member < 0) continue;  // a padding entry of the balanced schedule
             const MemberDev& M = a.members[tl.member];
             const TcGeom g = tc_geom<PASS>(M, a.xplane, a.yplane);
             const uint32_t buf = c.epi_tiles & 1, use = c.epi_tiles >> 1;

@@ -396,16 +396,17 @@ GemmArgs gemm_args(qg_plan* p, int pass, const void* A, void* C, int a_fmt, int 
     return g;
 }
 
-// The output tiles of one M-tile (a member's N-tiles: 258-wide members need two 144-wide
-// tiles) read the same A rows.  A GEMM launch hands tile t, t + G, t + 2G, ... to CTA t of its
-// G = SM-count CTAs, so the list is reordered to space the N-tiles of each M-tile exactly G
-// apart: the CTA that takes the first takes the next right after it, while the A rows it
-// just streamed are still in L2, instead of two CTAs missing on the same rows at once.
-// Batches of up to G M-tiles with k N-tiles each become k chunks of G slots (chunk j holding
-// N-tile j of every M-tile of the batch), the free slots filled with single-tile M-tiles;
-// single tiles left over go last.  Only the order changes: every tile is computed once.
-std::vector<GemmTile> space_n_tiles(const std::vector<GemmTile>& in, int G) {
-    if (G < 1) return in;
+// Schedule of a tensor-core GEMM pass's tiles over its G = SM-count CTAs (CTA b takes tiles
+// b, b + G, b + 2G, ... of the list, one after another).  The output tiles of one M-tile (a
+// member's N-tiles: 258-wide members need two 144-wide ones) read the same A rows, so they stay
+// together on one CTA, in sequence, while the A rows it just streamed are still in L2.  The
+// M-tiles go to CTAs longest first, each to the CTA with the least work so far (cost of a
+// tile: its k-blocks plus a fixed epilogue share), which evens out the CTAs' totals (the
+// pass lasts as long as its busiest CTA); CTAs with fewer tiles get padding entries
+// (member -1) that every role of the kernel skips.  Lists shorter than two tiles per CTA keep
+// their order.  Only the order changes: every tile is computed once.
+std::vector<GemmTile> schedule_tiles(const std::vector<GemmTile>& in, int G, const std::vector<int>& kdim) {
+    if (G < 1 || (int64_t)in.size() < 2 * (int64_t)G) return in;
     std::vector<std::vector<GemmTile>> rows;  // tiles of one (member, mt), nt ascending
     for (const GemmTile& t : in) {
         if (!rows.empty() && rows.back()[0].member == t.member && rows.back()[0].mt == t.mt)
@@ -413,27 +414,24 @@ std::vector<GemmTile> space_n_tiles(const std::vector<GemmTile>& in, int G) {
         else
             rows.push_back({t});
     }
-    std::vector<GemmTile> singles, out;
-    std::vector<std::vector<GemmTile>*> multi;
-    for (auto& r : rows) {
-        if (r.size() == 1)
-            singles.push_back(r[0]);
-        else
-            multi.push_back(&r);
+    std::vector<double> cost(rows.size());
+    for (size_t r = 0; r < rows.size(); ++r)
+        cost[r] = rows[r].size() * ((kdim[rows[r][0].member] + 63) / 64 + 1.5);
+    std::vector<size_t> order(rows.size());
+    for (size_t r = 0; r < order.size(); ++r) order[r] = r;
+    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return cost[a] > cost[b]; });
+    std::vector<double> load(G, 0.0);
+    std::vector<std::vector<GemmTile>> seq(G);
+    for (size_t r : order) {
+        const int b = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        load[b] += cost[r];
+        for (const GemmTile& t : rows[r]) seq[b].push_back(t);
     }
-    size_t next_single = 0;
-    for (size_t i = 0; i < multi.size();) {
-        // a batch: up to G consecutive M-tiles with the same N-tile count
-        const size_t k = multi[i]->size();
-        size_t j = i;
-        while (j < multi.size() && j - i < (size_t)G && multi[j]->size() == k) ++j;
-        for (size_t nt = 0; nt < k; ++nt) {
-            for (size_t r = i; r < j; ++r) out.push_back((*multi[r])[nt]);
-            for (size_t f = j - i; f < (size_t)G && next_single < singles.size(); ++f) out.push_back(singles[next_single++]);
-        }
-        i = j;
-    }
-    while (next_single < singles.size()) out.push_back(singles[next_single++]);
+    size_t L = 0;
+    for (const auto& q : seq) L = std::max(L, q.size());
+    std::vector<GemmTile> out(L * G, GemmTile{-1, 0, 0});
+    for (int b = 0; b < G; ++b)
+        for (size_t k = 0; k < seq[b].size(); ++k) out[k * G + b] = seq[b][k];
     return out;
 }
 
@@ -1115,9 +1113,18 @@ int qg_plan_create(const qg_member_desc* members, int n_members, const qg_option
             p->n_sw_v[v] = (int)g.size();
             e = upload(p, &p->sw_items_v[v], g);
         }
+        if (tc) {
+            std::vector<int> kx(n_members), ky(n_members);  // contraction lengths of the x / y passes
+            for (int i = 0; i < n_members; ++i) {
+                kx[i] = members[i].nx + 2;
+                ky[i] = members[i].ny + 2;
+            }
+            for (int v = 0; v < n_bn; ++v) {
+                gxv[v] = schedule_tiles(gxv[v], p->n_sm, kx);
+                gyv[v] = schedule_tiles(gyv[v], p->n_sm, ky);
+            }
+        }
         for (int v = 0; v < n_bn && !e; ++v) {
-            gxv[v] = space_n_tiles(gxv[v], p->n_sm);
-            gyv[v] = space_n_tiles(gyv[v], p->n_sm);
             p->n_gx_v[v] = (int)gxv[v].size();
             p->n_gy_v[v] = (int)gyv[v].size();
             if (!(e = upload(p, &p->gx_v[v], gxv[v]))) e = upload(p, &p->gy_v[v], gyv[v]);
