@@ -20,6 +20,11 @@ of every member (72 SSP-RK3 steps at dt = 1200 s).  ``--config baroclinic3_128``
              bounded sample of the same workload (rank 0, N = 1 only); the same leg checks
              parity: one member of each class after 10 steps against the float64 restatement
 
+``--config swm_jet64`` (the reference's 2-layer 64^2 shallow-water jet run) and ``swm3_1024``
+(a 3-layer 1024^2 shallow-water double gyre) time the multilayer shallow-water stepper
+(``qg_swm_step``) instead, with their own roofline (k_swm_stage), CPU baseline
+(the float32 restatement) and parity fields.
+
 ``--impl reference`` times that CPU restatement alone (the reference's JAX path cannot be
 installed here) and prints the same line with ``"impl": "reference"``.
 
@@ -209,6 +214,208 @@ def describe(name):
                           f"{cfg.scheme} dt={cfg.dt:g}s, {steps} steps = 1 model day per bench step")
 
 
+# ---- the multilayer shallow-water workloads ---------------------------------------------------
+SWM_METRIC = "SWM model-days/sec per GB300; k_swm_stage HBM GB/s"
+SWM_DESC = {
+    "swm_jet64": ("swm_jet64: the swm_jet run of the reference (baroclinic_instability_swm): 2-layer 64x64 periodic "
+                  "multilayer shallow water, Lx=Ly=1000 km, H=(500,4500) m, g'=(9.81,0.025), nu=1000 m^2/s, "
+                  "drag 1e-7/s, opposite 0.5 m/s jets; tsit5 dt=20s, 4320 steps = 1 model day per bench step"),
+    "swm3_1024": ("swm3_1024: 3-layer 1024x1024 wall-bounded multilayer shallow-water double gyre, Lx=Ly=4000 km, "
+                  "H=(400,1100,2600) m, nu=100 m^2/s, wind 8e-5 m^2/s^2, from rest + a seeded 2 m height anomaly; "
+                  "tsit5 dt=10s, 360 steps = 1 model hour per bench step"),
+}
+SWM_STAGES = {"euler": 1, "heun": 2, "ssprk3": 3, "tsit5": 6}
+
+
+def swm_cpu_rate(cfg, min_seconds: float = 10.0):
+    """Model-days/s of the float32 restatement of the shallow-water step (oracle.swm: NumPy
+    elementwise, one thread) on the host: whole steps until at least ``min_seconds``.
+    Returns (model-days/s, steps, seconds)."""
+    from oracle import qg as O
+    from oracle import swm as W
+    from somax_gb300 import testcases as tc
+
+    o = W.create(**cfg.oracle_kwargs())
+    y = np.stack(W.apply_boundary_conditions(o, *tc.swm_initial_state(cfg))).astype(np.float32)
+    y = O.rk_step(lambda z: W.rhs(o, z), y, cfg.dt, cfg.scheme).astype(np.float32)  # warm
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        y = O.rk_step(lambda z: W.rhs(o, z), y, cfg.dt, cfg.scheme).astype(np.float32)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= min_seconds:
+            break
+    return steps * cfg.dt / 86400.0 / el, steps, el
+
+
+def swm_parity(cfg, plan, pv, dev):
+    """Relative L2 of h, u, v after a few steps (10 up to 256^2, else 2) from the bench's initial
+    state against the float64 restatement, each bounded by max(1e-5, 4 x the error of the
+    same restatement run in float32) as in the shallow-water tests."""
+    import torch
+
+    from oracle import swm as W
+    from somax_gb300 import testcases as tc
+
+    n_steps = 10 if cfg.n <= 256 else 2
+    o = W.create(**cfg.oracle_kwargs())
+    y0 = tc.swm_initial_state(cfg)
+    y = torch.tensor(y0, device=dev).reshape(-1)
+    plan.step(y, pv, cfg.dt, n_steps, cfg.scheme, True)
+    if plan.status() != 0:
+        raise RuntimeError("shallow-water parity run flagged a non-finite tendency")
+    got = y.view(y0.shape).cpu().double().numpy()
+    ref = W.integrate(o, y0.astype(np.float64), cfg.dt, n_steps, cfg.scheme)
+    f32 = W.integrate(o, y0, cfg.dt, n_steps, cfg.scheme)
+
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+    out, ok = {}, True
+    for k, name in enumerate("huv"):
+        e, floor = rel(got[k], ref[k]), rel(f32[k].astype(np.float64), ref[k])
+        bound = max(1e-5, 4.0 * floor)
+        out[name] = {"rel_l2": e, "float32_restatement": floor, "bound": bound}
+        ok &= e < bound
+    return {"steps": n_steps, "fields": out, "pass": bool(ok),
+            "against": "float64 NumPy restatement of multilayer.py:150-219 (interior-write C-grid operators)"}
+
+
+def swm_roofline(cfg, plan, pv, dev, step_ms):
+    """Achieved bandwidth of the fused stage kernel from a profiled pass (CUDA events around
+    every launch, graphs off) of min(bench steps, 64) steps, its time scaled to the timed
+    bench step (the profiled pass's total against the timed time of as many steps).
+
+    Algorithmic HBM bytes of k_swm_stage, per layer-cell (lc = nl Ny Nx): stage s reads the
+    step's state and s earlier stage derivatives (h, u, v each: 12 B per state) and writes one
+    state (its derivative, or the next state on the last stage): (s + 2) x 12 B; a Tsit5 step
+    runs s = 0..5, 324 B."""
+    import torch
+
+    from somax_gb300 import _lib
+    from somax_gb300 import testcases as tc
+
+    pk = peaks()
+    ns = SWM_STAGES[cfg.scheme]
+    lc = cfg.nl * (cfg.n + 2) ** 2
+    P = min(cfg.bench_steps, 64)
+    y = torch.tensor(tc.swm_initial_state(cfg), device=dev).reshape(-1)
+    plan.set_profiling(True)
+    plan.step(y, pv, cfg.dt, P, cfg.scheme, True)
+    torch.cuda.synchronize()
+    stats = {"swm_stage": plan.kernel_stats(_lib.K["QG_SWM_K_STAGE"])}
+    plan.set_profiling(False)
+    bytes_step = {"swm_stage": 12.0 * lc * sum(s + 2 for s in range(ns))}
+    prof_total = sum(ms for ms, _ in stats.values())
+    timed_ms = step_ms * P / cfg.bench_steps  # the timed bench step's share for P steps
+    scale = timed_ms / prof_total if prof_total > 0 else 1.0
+    traffic = traffic_table().get(cfg.name, {})
+    kernels = {}
+    for name, (ms, n) in stats.items():
+        if not n:
+            continue
+        ms_t = ms * scale
+        per_launch = bytes_step[name] * P / n
+        gbs = bytes_step[name] * P / (ms_t / 1000.0) / 1e9
+        kernels[name] = {"launches": n, "total_ms": ms_t, "avg_us": ms_t * 1000.0 / n,
+                         "bytes_per_launch": per_launch, "achieved_gbs": gbs, "hbm_frac": gbs / pk["hbm_gbs"],
+                         "bound": "hbm", "traffic": traffic.get(name)}
+    dom = max(kernels, key=lambda k: kernels[k]["total_ms"])
+    d = kernels[dom]
+    step_bytes = sum(bytes_step.values())
+    return {"bound": "hbm", "achieved": d["achieved_gbs"], "peak": pk["hbm_gbs"], "unit": "GB/s",
+            "frac": d["hbm_frac"], "kernel": dom, "traffic": d["traffic"], "peak_src": pk["src"],
+            "algorithmic_bytes_per_launch": d["bytes_per_launch"], "avg_launch_us": d["avg_us"],
+            "step_bytes": step_bytes, "step_gbs": step_bytes / (step_ms / cfg.bench_steps / 1000.0) / 1e9,
+            "durations": (f"each class's share of a profiled pass of {P} steps (CUDA events around every launch) "
+                          f"applied to the timed bench step: profiled {prof_total:.3f} ms, timed {timed_ms:.3f} ms "
+                          f"for {P} steps"),
+            "kernels": kernels}
+
+
+def run_swm(args, dev, world, rank, local):
+    """The shallow-water bench line: ``--config swm_jet64`` or ``swm3_1024``."""
+    import torch
+
+    import somax_gb300 as sg
+    from somax_gb300 import testcases as tc
+
+    cfg = tc.SWM_CONFIGS[args.config]
+    m = sg.MultilayerShallowWater2D.create(**cfg.model_kwargs())
+    plan = m.plan(dev)
+    pv = m._param_vector(dev)
+    y0 = tc.swm_initial_state(cfg, seed=rank)
+    y = torch.tensor(y0, device=dev).reshape(-1)
+    plan.apply_bc(y)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
+    for _ in range(args.warmup):
+        plan.step(y, pv, cfg.dt, cfg.bench_steps, cfg.scheme, False)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            ev[k][0].record()
+            plan.step(y, pv, cfg.dt, cfg.bench_steps, cfg.scheme, False)
+            ev[k][1].record()
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    dev_ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in ev), world, dev)
+    ms_per_step = dev_ms / args.steps
+    days = cfg.bench_steps * cfg.dt / 86400.0
+    value = world * args.steps * days / (dev_ms / 1000.0)
+    status = plan.status()
+
+    # e2e: the C-ABI step with the state in pinned host memory (H2D, the steps, D2H)
+    yh = torch.tensor(y0).reshape(-1).pin_memory()
+    out = torch.empty_like(yh).pin_memory()
+    yd = torch.empty_like(y)
+
+    def host_step():
+        yd.copy_(yh, non_blocking=True)
+        plan.step(yd, pv, cfg.dt, cfg.bench_steps, cfg.scheme, True)
+        out.copy_(yd, non_blocking=True)
+        torch.cuda.current_stream(dev).synchronize()
+
+    host_step()
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        host_step()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world, dev)
+    e2e_value = world * args.steps * days / e2e_s
+
+    roof = swm_roofline(cfg, plan, pv, dev, ms_per_step)
+    ns = SWM_STAGES[cfg.scheme]
+    line = {
+        "metric": SWM_METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": SWM_DESC[cfg.name], "l2": "flushed between timed steps (256 MB write)",
+                   "graphs": "8-step CUDA graphs replayed", "status": status,
+                   "replicas": "independent basins per rank" if world > 1 else "one device"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": yh.numel() * 4,
+                "d2h_bytes_per_step": out.numel() * 4,
+                "api": "qg_swm_step (MultilayerShallowWater2D's plan) on a pinned host state copied in and out"},
+        "roofline": roof,
+        "gpu_launches": ns * cfg.bench_steps * args.steps,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, n, el = swm_cpu_rate(cfg, 10.0)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+                                "sample": f"{n} {cfg.scheme} steps of {cfg.name}, float32 NumPy restatement "
+                                          f"(elementwise, one thread; {el:.1f} s)"}
+        line["parity"] = swm_parity(cfg, plan, pv, dev)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def max_over_ranks(x: float, world: int, device) -> float:
     """The largest of every rank's x: a multi-rank job takes as long as its slowest rank."""
     if world <= 1:
@@ -236,6 +443,25 @@ def run_reference(args):
     if rank != 0:
         return
     threads = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    if args.config in tc.SWM_CONFIGS:
+        cfg = tc.SWM_CONFIGS[args.config]
+        vals, samples = [], []
+        for k in range(args.warmup + args.steps):
+            v, n, el = swm_cpu_rate(cfg, 5.0 if k >= args.warmup else 1.0)
+            if k >= args.warmup:
+                vals.append(v)
+                samples.append(f"{n} {cfg.scheme} steps of {cfg.name} ({el:.1f} s)")
+        value = statistics.median(vals)
+        sample = (f"per bench step >= 5 s of the float32 NumPy restatement (elementwise, one thread), e.g. "
+                  f"{samples[0]}; the reference's JAX path is not installable")
+        print(json.dumps({
+            "impl": "reference", "metric": SWM_METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": SWM_DESC[cfg.name], "sample": sample},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}), flush=True)
+        return
     metric, unit, workload = describe(args.config)
     per_step_s = 5.0
     vals, samples = [], []
@@ -561,7 +787,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="ensemble256",
                     help="ensemble256 (default) | baroclinic3_128 | barotropic_64 | baroclinic3_256 | "
-                         "baroclinic3_512 | baroclinic3_1024 | masked3_512 | adjoint256")
+                         "baroclinic3_512 | baroclinic3_1024 | masked3_512 | adjoint256 | swm_jet64 | swm3_1024")
     ap.add_argument("--precision", default="bf16x3", help="DST-I GEMM arithmetic: fp32 | tf32 | bf16x3")
     ap.add_argument("--persistent", type=int, default=0,
                     help="1: all steps of a call in one persistent cooperative launch (tensor-core precisions)")
@@ -593,6 +819,12 @@ def main():
     dev = torch.device("cuda", local)
     if world > 1:
         dist.init_process_group("nccl", device_id=dev)
+
+    if args.config in tc.SWM_CONFIGS:
+        run_swm(args, dev, world, rank, local)
+        if world > 1:
+            dist.destroy_process_group()
+        return
 
     W = Workload(args.config, args.precision, bool(args.persistent), dev, rank, args.stencil, args.gemm_tile,
                  {"auto": None, "on": True, "off": False}[args.cluster], args.groups)

@@ -318,9 +318,29 @@ int qg_swm_rhs(qg_swm_plan* plan, const float* state, float* tend, const float* 
 int qg_swm_apply_bc(qg_swm_plan* plan, float* state, void* stream);
 /* Advance the state in place by n_steps constant steps (QG_SCHEME_*; Tsit5 is the reference's
    default solver): BC on every stage input, QG_STEP_APPLY_BC applies it to the initial state
-   first (integrate() on a new state0), the returned state is as stepped. */
+   first (integrate() on a new state0), the returned state is as stepped.  The params are
+   copied into the plan on the stream first; each stage is one fused launch (stage input,
+   right-hand side, and on the last stage the next state, written alternately into the state
+   and a plan buffer); the steps run as captured CUDA graphs of 8 and of 1 steps, replayed
+   while the state pointer, dt and the scheme repeat (recaptured otherwise). */
 int qg_swm_step(qg_swm_plan* plan, float* state, const float* params, double dt, int n_steps, int scheme,
                 int flags, void* stream);
+/* Per-kernel-class timing of qg_swm_step: CUDA events on the launch stream around every
+   launch while profiling is on (graphs are bypassed then); set_profiling resets the counters.
+   No reference counterpart: the benchmark's per-kernel durations. */
+#define QG_SWM_K_STAGE 0   /* k_swm_stage: stage input, right-hand side, (last stage) next state */
+#define QG_SWM_K_COMBINE 1 /* k_swm_combine: a stage input of qg_reparam_step or its final combination */
+#define QG_SWM_K_COUNT 2
+int qg_swm_set_profiling(qg_swm_plan* plan, int enable);
+int qg_swm_kernel_stats(qg_swm_plan* plan, int kclass, double* total_ms, int64_t* launches);
+/* ReparameterizedQG (somax/_src/models/qg/reparameterized.py:65-228) stepped like qg_swm_step:
+   every stage input gets the model's apply_boundary_conditions (the SWM wall rules, then the
+   geostrophic projection of qg_project on qgplan, reparameterized.py:186-189) before the
+   shallow-water vector_field (:180-184); QG_STEP_APPLY_BC does the same to the initial state.
+   plan must have wall boundaries (QG_ERR_ARG) and qgplan one baroclinic member of the same
+   grid and layers (QG_ERR_SHAPE).  Launched directly (no graph). */
+int qg_reparam_step(qg_swm_plan* plan, qg_plan* qgplan, float* state, const float* params, double dt,
+                    int n_steps, int scheme, int flags, void* stream);
 /* QG_OK or QG_ERR_NONFINITE (a tendency was not finite since the last call); clears the flag. */
 int qg_swm_status(qg_swm_plan* plan, int* flags, void* stream);
 

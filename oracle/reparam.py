@@ -66,3 +66,21 @@ def project(m: O.QGModel, h: np.ndarray, u: np.ndarray, v: np.ndarray):
     a_psi = m.modes.to_layer(ev * m.modes.to_modal(psi))
     hg = H * (1.0 + m.f0 * a_psi)
     return hg, ug, vg, psi
+
+
+def integrate(m: O.QGModel, ms, y0: np.ndarray, dt: float, n_steps: int, scheme: str = "tsit5") -> np.ndarray:
+    """``ReparameterizedQG`` through ``SomaxModel.integrate`` with constant steps on the stacked
+    state y = (3, nl, Ny, Nx) = (h, u, v): ``apply_boundary_conditions`` (the SWM wall rules,
+    then the projection; ``reparameterized.py:186-189``) on the initial state and on every stage
+    input before the shallow-water ``vector_field`` (``reparameterized.py:180-184``); ``m`` is
+    the QG model of the projection's inversion, ``ms`` the ``oracle.swm`` model (wall BC)."""
+    from oracle import swm as W
+
+    def bc(y):
+        h, u, v = W.apply_boundary_conditions(ms, y[0], y[1], y[2])
+        return np.stack(project(m, h, u, v)[:3])
+
+    y = bc(np.asarray(y0, dtype=np.float64))
+    for _ in range(n_steps):
+        y = O.rk_step(lambda z: np.stack(W.vector_field(ms, *bc(z))), y, dt, scheme)
+    return y

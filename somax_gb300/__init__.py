@@ -3,12 +3,15 @@ QG model API.  The compute path is libqgcore.so (hand-written CUDA, C ABI in
 include/qgcore.h); this package is the Python host side that mirrors somax's classes."""
 
 from .qg import (  # noqa: F401
-    SSPRK3, BaroclinicQG, BaroclinicQGDiagnostics, BaroclinicQGParams, BaroclinicQGState,
-    BarotropicQG, BarotropicQGDiagnostics, BarotropicQGParams, BarotropicQGState, Euler, Heun,
+    SSPRK3, BaroclinicQG, BaroclinicQGDiagnostics, BaroclinicQGParams, BaroclinicQGPhysConsts, BaroclinicQGState,
+    BarotropicQG, BarotropicQGDiagnostics, BarotropicQGParams, BarotropicQGPhysConsts, BarotropicQGState, Euler, Heun,
     MemberSpec, Plan, QGDiagnostics, QGEnsemble, QGParams, SaveAt, Solution, SomaxModel, State, Tsit5,
 )
-from .reparameterized import MultilayerSW2DState, ReparameterizedQG, ReparamQGGeostrophy  # noqa: F401
+from .reparameterized import MultilayerSW2DState, ReparameterizedQG, ReparamQGDiagnostics  # noqa: F401
 from .swm import (  # noqa: F401
     MultilayerShallowWater2D, MultilayerSW2DDiagnostics, MultilayerSW2DParams, MultilayerSW2DPhysConsts,
 )
 from .transforms import ModalTransform, StratificationProfile  # noqa: F401
+from .gfd_testcases import (  # noqa: F401
+    baroclinic_instability_swm, doublegyre_baroclinic_qg, doublegyre_qg, doublegyre_reparameterized_qg,
+)

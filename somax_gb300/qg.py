@@ -132,6 +132,23 @@ BarotropicQGDiagnostics = QGDiagnostics
 
 
 @dataclasses.dataclass(frozen=True)
+class BaroclinicQGPhysConsts:
+    """Frozen constants of the multilayer model (``baroclinic.py:51-62``)."""
+
+    f0: float = 1e-4
+    beta: float = 1.6e-11
+    n_layers: int = 2
+
+
+@dataclasses.dataclass(frozen=True)
+class BarotropicQGPhysConsts:
+    """Frozen constants of the barotropic model (``barotropic.py:47-58``)."""
+
+    f0: float = 1e-4
+    beta: float = 1.6e-11
+
+
+@dataclasses.dataclass(frozen=True)
 class Grid:
     """Arakawa C-grid with one ghost ring (finitevolx ``ArakawaCGrid2D.from_interior``)."""
 
@@ -691,6 +708,10 @@ class BaroclinicQG(_QGBase):
     state_cls = BaroclinicQGState
 
     @property
+    def consts(self) -> BaroclinicQGPhysConsts:
+        return BaroclinicQGPhysConsts(f0=self.spec.f0, beta=self.spec.beta, n_layers=self.spec.n_layers)
+
+    @property
     def helmholtz_lambdas(self) -> np.ndarray:
         return self.spec.f0**2 * np.asarray(self.modal.eigenvalues)
 
@@ -738,6 +759,10 @@ class BarotropicQG(_QGBase):
 
     state_cls = BarotropicQGState
     barotropic = True
+
+    @property
+    def consts(self) -> BarotropicQGPhysConsts:
+        return BarotropicQGPhysConsts(f0=self.spec.f0, beta=self.spec.beta)
 
     @staticmethod
     def create(nx=64, ny=64, Lx=1e6, Ly=1e6, f0=1e-4, beta=1.6e-11, lateral_viscosity=0.0,

@@ -1,12 +1,13 @@
-"""The geostrophic projection of ``ReparameterizedQG`` (``somax/_src/models/qg/reparameterized.py``).
+"""``ReparameterizedQG`` (``somax/_src/models/qg/reparameterized.py``) on the GPU.
 
 The reparameterized QG model is the multilayer shallow-water model plus the projection
-P = G (Q G)^-1 Q onto the geostrophic manifold after every step (Thiry, Li, Memin & Roullet
-2024).  This module mirrors the model's projection API (``create``, ``project``,
-``_solve_helmholtz``, the geostrophic parts of ``diagnose``) on the same CUDA inversion as the
-QG classes, through ``qg_project`` (C ABI): a PV kernel, the modal DST-I Helmholtz solve and a
-reconstruction kernel.  The shallow-water right-hand side itself (``vector_field``) belongs to
-the multilayer SWM, which this library does not carry.
+P = G (Q G)^-1 Q onto the geostrophic manifold, applied to every stage input by
+``apply_boundary_conditions`` (Thiry, Li, Memin & Roullet 2024).  As in the reference the model
+wraps a ``MultilayerShallowWater2D`` (wall boundaries) and delegates ``vector_field``, the
+parameters, constants and grid to it.  The projection runs on the same CUDA inversion as the
+QG classes through ``qg_project`` (C ABI): a PV kernel, the modal DST-I Helmholtz solve and a
+reconstruction kernel; ``step`` / ``integrate`` run the whole stage loop in the library
+(``qg_reparam_step``: combine, wall rules, projection, shallow-water right-hand side).
 """
 
 from __future__ import annotations
@@ -17,7 +18,7 @@ import dataclasses
 import torch
 
 from . import _lib
-from .qg import MemberSpec, Plan, _stream_handle, check
+from .qg import MemberSpec, Plan, SaveAt, Solution, _solver_name, _stream_handle, check
 from .transforms import ModalTransform, StratificationProfile
 
 
@@ -32,25 +33,56 @@ class MultilayerSW2DState:
 
 
 @dataclasses.dataclass
-class ReparamQGGeostrophy:
-    """The QG-specific fields of ``ReparamQGDiagnostics`` (``reparameterized.py:37-62``)."""
+class ReparamQGDiagnostics:
+    """``ReparamQGDiagnostics`` (``reparameterized.py:37-62``): the shallow-water diagnostics
+    plus psi and the ageostrophic velocity u - u_g, v - v_g."""
 
+    energy: torch.Tensor
+    total_energy: torch.Tensor
+    enstrophy: torch.Tensor
+    total_enstrophy: torch.Tensor
+    potential_vorticity: torch.Tensor
+    relative_vorticity: torch.Tensor
+    kinetic_energy_field: torch.Tensor
     psi: torch.Tensor
     u_ageostrophic: torch.Tensor
     v_ageostrophic: torch.Tensor
 
 
 class ReparameterizedQG:
-    """``ReparameterizedQG`` (``reparameterized.py:65-315``): the geostrophic projection."""
+    """``ReparameterizedQG`` (``reparameterized.py:65-315``): multilayer SWM + the geostrophic
+    projection."""
 
-    def __init__(self, spec: MemberSpec, strat: StratificationProfile, modal: ModalTransform, precision="fp32",
-                 refine=0):
+    def __init__(self, swm, spec: MemberSpec, strat: StratificationProfile, modal: ModalTransform,
+                 precision="fp32", refine=0):
+        self.swm = swm
         self.spec = spec
         self.strat = strat
         self.modal = modal
         self.precision = precision
         self.refine = refine
         self._plans: dict = {}
+
+    # delegate properties (reparameterized.py:95-123)
+    @property
+    def params(self):
+        return self.swm.params
+
+    @params.setter
+    def params(self, value):
+        self.swm.params = value
+
+    @property
+    def consts(self):
+        return self.swm.consts
+
+    @property
+    def grid(self):
+        return self.swm.grid
+
+    @property
+    def helmholtz_lambdas(self):
+        return self.modal.eigenvalues * self.spec.f0 ** 2
 
     @staticmethod
     def create(nx=64, ny=64, Lx=4e6, Ly=4e6, g=9.81, f0=9.375e-5, beta=1.754e-11, n_layers=3,
@@ -59,8 +91,10 @@ class ReparameterizedQG:
                bc="wall", method="upwind1", poisson_bc="dst", precision="fp32", refine=0,
                eigs="consistent") -> "ReparameterizedQG":
         """``ReparameterizedQG.create`` (``reparameterized.py:230-315``) with the same keyword
-        arguments; the shallow-water ones (``g``, viscosity, drag, wind, ``method``) are
-        accepted for the drop-in signature and do not enter the projection."""
+        arguments: the shallow-water model with wall boundaries, and the projection's modal
+        Helmholtz inversion (DST-I GEMMs in ``precision``, ``refine`` FP32 refinement sweeps)."""
+        from .swm import MultilayerShallowWater2D
+
         if bc != "wall":
             raise ValueError(f"ReparameterizedQG requires wall BCs (got bc={bc!r}). The geostrophic projection "
                              "uses Dirichlet Helmholtz inversion which is incompatible with periodic BCs.")
@@ -73,16 +107,22 @@ class ReparameterizedQG:
                 raise ValueError(f"n_layers ({n_layers}), len(H) ({len(H)}), and len(g_prime) "
                                  f"({len(g_prime)}) must all be equal")
             strat = StratificationProfile.from_layers(H=list(H), g_prime=list(g_prime))
+        swm = MultilayerShallowWater2D.create(nx=nx, ny=ny, Lx=Lx, Ly=Ly, g=g, f0=f0, beta=beta,
+                                              n_layers=strat.nl, stratification=strat,
+                                              lateral_viscosity=lateral_viscosity, bottom_drag=bottom_drag,
+                                              wind_amplitude=wind_amplitude, wind_profile=wind_profile, bc="wall",
+                                              method=method)
         modal = ModalTransform.from_stratification(strat, f0, eigs)
         spec = MemberSpec(nx, ny, Lx, Ly, f0, beta, list(strat.H), list(strat.g_prime), False, wind_profile,
                           eigs, modal, None)
-        return ReparameterizedQG(spec, strat, modal, precision, refine)
+        return ReparameterizedQG(swm, spec, strat, modal, precision, refine)
 
     @property
     def shape(self):
         return (self.spec.n_layers, self.spec.ny + 2, self.spec.nx + 2)
 
     def plan(self, device=None) -> Plan:
+        """The inversion's plan on ``device`` (the projection's modal Helmholtz solve)."""
         device = torch.device(device if device is not None else "cuda")
         if device.index is None:
             device = torch.device("cuda", torch.cuda.current_device())
@@ -112,22 +152,73 @@ class ReparameterizedQG:
         hg, ug, vg, _ = self._project(state)
         return MultilayerSW2DState(h=hg, u=ug, v=vg)
 
-    def apply_boundary_conditions(self, state: MultilayerSW2DState) -> MultilayerSW2DState:
-        """The projection step of ``apply_boundary_conditions`` (``reparameterized.py:186-189``);
-        the wall BCs of the shallow-water state that precede it belong to the SWM."""
-        return self.project(state)
-
     def _solve_helmholtz(self, q: torch.Tensor) -> torch.Tensor:
         """(Q G)^-1 (``reparameterized.py:125-140``): modal Helmholtz solve, zero ring."""
         q = self._field(q, "q")
         return self.plan(q.device).invert(q)
 
-    def diagnose(self, state: MultilayerSW2DState) -> ReparamQGGeostrophy:
-        """The QG fields of ``diagnose`` (``reparameterized.py:191-228``): psi and the
-        ageostrophic velocity u - u_g, v - v_g (the SWM energies are the SWM's)."""
-        _, ug, vg, psi = self._project(state)
-        return ReparamQGGeostrophy(psi=psi, u_ageostrophic=state.u - ug, v_ageostrophic=state.v - vg)
+    # ---- the model contract -------------------------------------------------------------
+    def vector_field(self, t, state, args=None) -> MultilayerSW2DState:
+        """The shallow-water tendencies (``reparameterized.py:180-184``)."""
+        return self.swm.vector_field(t, state, args)
 
-    def vector_field(self, t, state, args=None):
-        raise NotImplementedError("the multilayer shallow-water right-hand side is not part of this library; "
-                                  "ReparameterizedQG here provides the geostrophic projection")
+    def apply_boundary_conditions(self, state) -> MultilayerSW2DState:
+        """The SWM wall rules, then the projection (``reparameterized.py:186-189``)."""
+        return self.project(self.swm.apply_boundary_conditions(state))
+
+    def _run(self, y: torch.Tensor, dt: float, n_steps: int, scheme: str, apply_bc: bool):
+        from .swm import _SCHEMES
+
+        sp = self.swm.plan(y.device)
+        qp = self.plan(y.device)
+        pv = self.swm._param_vector(y.device)
+        check(sp._L.qg_reparam_step(sp._h, qp._h, C.c_void_p(y.data_ptr()), C.c_void_p(pv.data_ptr()), float(dt),
+                                    int(n_steps), _SCHEMES[scheme], _lib.K["QG_STEP_APPLY_BC"] if apply_bc else 0,
+                                    _stream_handle(y.device)), "qg_reparam_step")
+        return y
+
+    def step(self, state, dt: float, n_steps: int = 1, solver="tsit5", apply_bc: bool = True) -> MultilayerSW2DState:
+        """``n_steps`` constant steps on the GPU: the projection and the wall rules on every stage
+        input (and on the initial state with ``apply_bc``), the returned state as stepped."""
+        y = self.swm.pack(state).clone().reshape(-1)
+        self._run(y, dt, n_steps, _solver_name(solver), apply_bc)
+        return self.swm.unpack(y)
+
+    def integrate(self, state0, t0: float, t1: float, dt: float, solver=None, saveat=None, **kw):
+        """``SomaxModel.integrate`` with constant steps (``core/model.py:53-88``; Tsit5 default)."""
+        if kw.get("stepsize_controller") not in (None, "constant"):
+            raise ValueError("only constant step sizes are supported")
+        scheme = _solver_name(solver) if solver is not None else "tsit5"
+        saveat = saveat or SaveAt(t1=True)
+        n_total = int(round((t1 - t0) / dt))
+        if abs(n_total * dt - (t1 - t0)) > 1e-9 * max(1.0, abs(t1 - t0)):
+            raise ValueError("(t1 - t0) must be a whole number of steps")
+        targets = [int(round((float(t) - t0) / dt)) for t in saveat.ts] if saveat.ts is not None else [n_total]
+        y = self.swm.pack(state0).clone().reshape(-1)
+        self._run(y, dt, 0, scheme, True)
+        ys, done = [], 0
+        for tgt in targets:
+            if tgt < done:
+                raise ValueError("saveat.ts must be increasing")
+            if tgt > done:
+                self._run(y, dt, tgt - done, scheme, False)
+                done = tgt
+            ys.append(y.clone().view((3,) + self.shape))
+        st = torch.stack(ys)
+        ts = torch.tensor([t0 + k * dt for k in targets], dtype=torch.float64)
+        return Solution(ts=ts, ys=MultilayerSW2DState(h=st[:, 0], u=st[:, 1], v=st[:, 2]))
+
+    def diagnose(self, state: MultilayerSW2DState) -> ReparamQGDiagnostics:
+        """``diagnose`` (``reparameterized.py:191-228``): the shallow-water energies and
+        enstrophies, psi of the state's PV and the ageostrophic velocity u - u_g, v - v_g."""
+        sd = self.swm.diagnose(state)
+        _, ug, vg, psi = self._project(state)
+        return ReparamQGDiagnostics(energy=sd.energy, total_energy=sd.total_energy, enstrophy=sd.enstrophy,
+                                    total_enstrophy=sd.total_enstrophy, potential_vorticity=sd.potential_vorticity,
+                                    relative_vorticity=sd.relative_vorticity,
+                                    kinetic_energy_field=sd.kinetic_energy_field, psi=psi,
+                                    u_ageostrophic=state.u - ug, v_ageostrophic=state.v - vg)
+
+    def status(self) -> int:
+        """The shallow-water plan's non-finite flag (QG_OK or QG_ERR_NONFINITE), cleared."""
+        return self.swm.status()

@@ -138,6 +138,17 @@ class SwmPlan:
         flags = C.c_int(0)
         return self._L.qg_swm_status(self._h, C.byref(flags), _stream_handle(self.device))
 
+    def set_profiling(self, on: bool):
+        """CUDA events around every launch of ``step`` (graphs bypassed); resets the counters."""
+        check(self._L.qg_swm_set_profiling(self._h, int(on)), "qg_swm_set_profiling")
+
+    def kernel_stats(self, kclass: int):
+        """(total ms, launches) of one kernel class (QG_SWM_K_RHS / QG_SWM_K_COMBINE) since
+        profiling was switched on."""
+        t, n = C.c_double(0.0), C.c_int64(0)
+        check(self._L.qg_swm_kernel_stats(self._h, int(kclass), C.byref(t), C.byref(n)), "qg_swm_kernel_stats")
+        return t.value, n.value
+
 
 class MultilayerShallowWater2D(SomaxModel):
     """Multilayer 2D nonlinear shallow water model, vector-invariant form (multilayer.py:98-257)."""

@@ -1,6 +1,7 @@
-"""Seeded synthetic workloads of the QG time step (double-gyre basins).
+"""Seeded synthetic workloads of the QG time step (double-gyre basins) and of the multilayer
+shallow-water model.
 
-Shapes and parameters of the five benchmark configurations; the initial PV is a seeded
+Shapes and parameters of the QG benchmark configurations; the initial PV is a seeded
 Gaussian random field with an isotropic k^-3 spectrum (no dataset is involved).  Wind
 amplitudes follow the reference factory's convention: ``wind_amplitude = tau0 * 2 pi /
 (rho0 * Ly)`` with the ``-sin(2 pi y / Ly)`` double-gyre pattern
@@ -171,3 +172,70 @@ def land_mask(ny: int, nx: int, frac: float = 0.15, seed: int = 0, n_blobs: int 
     mask[1:-1, 1:-1][dmin <= hi] = 0
     mask[0, :] = mask[-1, :] = mask[:, 0] = mask[:, -1] = 0
     return mask
+
+
+# ---- multilayer shallow-water workloads ----------------------------------------------------
+@dataclasses.dataclass
+class SWMConfig:
+    """A shallow-water basin stepped with constant steps; one bench step = ``bench_steps``."""
+
+    name: str
+    n: int
+    L: float
+    H: tuple
+    g_prime: tuple
+    f0: float
+    beta: float
+    lateral_viscosity: float
+    bottom_drag: float
+    wind_amplitude: float
+    bc: str
+    dt: float
+    scheme: str
+    bench_steps: int
+    initial: str  # "jet" (baroclinic_instability_swm) or "bump" (rest + seeded height anomaly)
+
+    @property
+    def nl(self) -> int:
+        return len(self.H)
+
+    def model_kwargs(self) -> dict:
+        return dict(nx=self.n, ny=self.n, Lx=self.L, Ly=self.L, f0=self.f0, beta=self.beta, n_layers=self.nl,
+                    H=tuple(self.H), g_prime=tuple(self.g_prime), lateral_viscosity=self.lateral_viscosity,
+                    bottom_drag=self.bottom_drag, wind_amplitude=self.wind_amplitude, bc=self.bc)
+
+    def oracle_kwargs(self) -> dict:
+        kw = self.model_kwargs()
+        kw.pop("n_layers")
+        return kw
+
+
+# The 2-layer baroclinic jet of the reference's run configuration ``swm_jet`` (64^2 periodic
+# basin of 1000 km, nu = 1000 m^2/s, dt = 20 s, 30 days saved daily; the runner integrates with
+# the default Tsit5): one bench step = one model day = 4320 steps.
+SWM_JET64 = SWMConfig("swm_jet64", 64, 1.0e6, (500.0, 4500.0), (9.81, 0.025), 1e-4, 1.6e-11, 1000.0, 1e-7, 0.0,
+                      "periodic", 20.0, "tsit5", 4320, "jet")
+# A 3-layer 1024^2 wall-bounded double gyre of 4000 km (the reparameterised double gyre's
+# stratification and wind, 3.9 km cells) from rest with a seeded height anomaly; dt = 10 s
+# (0.5 of the external gravity-wave CFL), one bench step = one model hour = 360 steps.
+SWM3_1024 = SWMConfig("swm3_1024", 1024, 4.0e6, (400.0, 1100.0, 2600.0), (9.81, 0.025, 0.0125), F0, BETA, 100.0,
+                      3.6e-8, 8e-5, "wall", 10.0, "tsit5", 360, "bump")
+SWM_CONFIGS = {c.name: c for c in (SWM_JET64, SWM3_1024)}
+
+
+def swm_initial_state(cfg: SWMConfig, seed: int = 0) -> np.ndarray:
+    """(3, nl, n+2, n+2) float32 (h, u, v): the jet of ``baroclinic_instability_swm`` or the
+    rest state plus a k^-3 height anomaly of 2 m peak per layer."""
+    N = cfg.n + 2
+    dx = cfg.L / cfg.n
+    if cfg.initial == "jet":
+        x = np.arange(N) * dx
+        env = np.exp(-0.5 * ((np.arange(N) * dx - cfg.L / 2.0) / 5e4) ** 2)[:, None] * np.ones((1, N))
+        u = np.stack([s * 0.5 * env for s in (1.0, -1.0)])
+        v = np.stack([0.01 * np.sin(4.0 * math.pi * x / cfg.L)[None, :] * env] * 2)
+        h = np.asarray(cfg.H, float)[:, None, None] * np.ones((cfg.nl, N, N))
+        return np.stack([h, u, v]).astype(np.float32)
+    k = kminus3_field(cfg.n, seed, cfg.nl)
+    h = np.asarray(cfg.H, float)[:, None, None] + 2.0 * k / np.abs(k).max()
+    z = np.zeros_like(h)
+    return np.stack([h, z, z]).astype(np.float32)

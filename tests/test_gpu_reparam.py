@@ -88,3 +88,59 @@ def test_project_rejects_barotropic_and_shapes():
                                          v=torch.zeros(2, 17, 18, device="cuda")))
     with pytest.raises(ValueError):
         sg.ReparameterizedQG.create(bc="periodic")
+
+
+def sw_pair(nx, ny, H, g, Lx=4e6, Ly=3.6e6, nu=200.0, kappa=1e-7, tau=8e-5):
+    """The GPU model and the two oracle halves (projection, shallow water) of one basin."""
+    from oracle import swm as W
+
+    kw = dict(nx=nx, ny=ny, Lx=Lx, Ly=Ly, n_layers=len(H), H=H, g_prime=g, lateral_viscosity=nu,
+              bottom_drag=kappa, wind_amplitude=tau)
+    m = sg.ReparameterizedQG.create(**kw)
+    o = O.baroclinic_model(nx=nx, ny=ny, Lx=Lx, Ly=Ly, H=H, g_prime=g)
+    ms = W.create(nx=nx, ny=ny, Lx=Lx, Ly=Ly, f0=9.375e-5, beta=1.754e-11, H=H, g_prime=g, lateral_viscosity=nu,
+                  bottom_drag=kappa, wind_amplitude=tau, bc="wall")
+    return m, o, ms
+
+
+@pytest.mark.parametrize("scheme", ["heun", "tsit5"])
+@pytest.mark.parametrize("nx,ny,H,g", [(16, 16, (500.0, 500.0), (9.81, 0.02)),
+                                       (40, 33, (400.0, 1100.0, 2600.0), (9.81, 0.025, 0.0125))])
+def test_step_matches_oracle(nx, ny, H, g, scheme):
+    """10 constant steps of qg_reparam_step (projection + wall rules on every stage input)
+    against the float64 composition of the oracle's projection and shallow-water RHS.  One
+    projection leaves up to 3e-5 on the h anomaly and 5e-5 on the velocities
+    (test_project_against_oracle); 10 steps project 20 (Heun) or 60 (Tsit5) stage inputs.
+    Measured on GB300 (h - H, u, v): 16x16 Heun 3.9e-5, 3.1e-5, 4.3e-5; Tsit5 4.5e-5, 6.0e-5,
+    6.4e-5; 40x33 Heun 1.7e-4, 4.5e-5, 4.0e-5 (the h anomaly's FP32 storage floor there is
+    1.0e-5).  Bounds: 5e-4 on the h anomaly, 1e-4 on the velocities."""
+    m, o, ms = sw_pair(nx, ny, H, g)
+    h, u, v = (x.astype(np.float32).astype(np.float64) for x in state(o, 3 + nx))
+    y0 = np.stack([h, u, v])
+    dt = 0.2 * min(o.grid.dx, o.grid.dy) / np.sqrt(9.81 * sum(H))
+    got = m.step(sg.MultilayerSW2DState(h=cuda(h), u=cuda(u), v=cuda(v)), dt, 10, scheme)
+    assert m.status() == 0
+    ref = R.integrate(o, ms, y0, dt, 10, scheme)
+    Hb = np.asarray(H)[:, None, None]
+    e = (rel(got.h - torch.tensor(Hb, device="cuda"), ref[0] - Hb), rel(got.u, ref[1]), rel(got.v, ref[2]))
+    print(f"reparam {nx}x{ny} {scheme}: 10-step rel L2 h-H {e[0]:.2e} u {e[1]:.2e} v {e[2]:.2e}")
+    assert e[0] < 5e-4 and max(e[1:]) < 1e-4, e
+
+
+def test_integrate_and_diagnose_reference_properties():
+    """``tests/models/test_qg_reparameterized.py`` on the GPU path: the double-gyre factory
+    integrates to finite fields (t1 = 1000 s, dt = 10 s), the rest state stays at rest without
+    wind, and diagnose returns finite energies with psi of the state."""
+    m, s0 = sg.doublegyre_reparameterized_qg(nx=16, ny=16)
+    sol = m.integrate(s0, t0=0.0, t1=1000.0, dt=10.0)
+    assert torch.isfinite(sol.ys.h).all() and torch.isfinite(sol.ys.u).all()
+    assert float(sol.ys.u.abs().max()) > 0  # the wind spun the top layer up
+    m0 = sg.ReparameterizedQG.create(nx=16, ny=16, n_layers=2, H=(500.0, 500.0), g_prime=(9.81, 0.02))
+    h = torch.ones((2, 18, 18), device="cuda") * torch.tensor([500.0, 500.0], device="cuda")[:, None, None]
+    z = torch.zeros_like(h)
+    rest = m0.step(sg.MultilayerSW2DState(h=h, u=z, v=z), 50.0, 5, "tsit5")
+    assert torch.allclose(rest.h, h, atol=1e-3) and float(rest.u.abs().max()) < 1e-6
+    d = m.diagnose(sol.ys.__class__(h=sol.ys.h[-1], u=sol.ys.u[-1], v=sol.ys.v[-1]))
+    assert torch.isfinite(d.total_energy) and (d.energy >= 0).all() and torch.isfinite(d.psi).all()
+    assert torch.equal(d.u_ageostrophic, sol.ys.u[-1] - m.project(sg.MultilayerSW2DState(
+        h=sol.ys.h[-1], u=sol.ys.u[-1], v=sol.ys.v[-1])).u)
