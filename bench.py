@@ -215,7 +215,7 @@ def describe(name):
 
 
 # ---- the multilayer shallow-water workloads ---------------------------------------------------
-SWM_METRIC = "SWM model-days/sec per GB300; k_swm_stage HBM GB/s"
+SWM_METRIC = "SWM model-days/sec per GB300; k_swm_stage / k_swm_cluster HBM GB/s"
 SWM_DESC = {
     "swm_jet64": ("swm_jet64: the swm_jet run of the reference (baroclinic_instability_swm): 2-layer 64x64 periodic "
                   "multilayer shallow water, Lx=Ly=1000 km, H=(500,4500) m, g'=(9.81,0.025), nu=1000 m^2/s, "
@@ -282,14 +282,18 @@ def swm_parity(cfg, plan, pv, dev):
 
 
 def swm_roofline(cfg, plan, pv, dev, step_ms):
-    """Achieved bandwidth of the fused stage kernel from a profiled pass (CUDA events around
-    every launch, graphs off) of min(bench steps, 64) steps, its time scaled to the timed
-    bench step (the profiled pass's total against the timed time of as many steps).
+    """Achieved bandwidth of the stepping kernel from a profiled pass (CUDA events around every
+    launch, graphs off) of min(bench steps, 64) steps, its time scaled to the timed bench step
+    (the profiled pass's total against the timed time of as many steps).
 
-    Algorithmic HBM bytes of k_swm_stage, per layer-cell (lc = nl Ny Nx): stage s reads the
-    step's state and s earlier stage derivatives (h, u, v each: 12 B per state) and writes one
-    state (its derivative, or the next state on the last stage): (s + 2) x 12 B; a Tsit5 step
-    runs s = 0..5, 324 B."""
+    Algorithmic HBM bytes per layer-cell (lc = nl Ny Nx):
+      k_swm_stage    stage s reads the step's state and s earlier stage derivatives (h, u, v:
+                     12 B per state) and writes one state (its derivative, or the next state on
+                     the last stage): (s + 2) x 12 B; a Tsit5 step runs s = 0..5, 324 B
+      k_swm_cluster  the cluster engine (small basins): the state in and out once per launch,
+                     24 B; every stage input and derivative stays in the cluster's shared
+                     memory, so the kernel is bound by its SMs' latency and cluster barriers,
+                     not by HBM"""
     import torch
 
     from somax_gb300 import _lib
@@ -303,7 +307,8 @@ def swm_roofline(cfg, plan, pv, dev, step_ms):
     plan.set_profiling(True)
     plan.step(y, pv, cfg.dt, P, cfg.scheme, True)
     torch.cuda.synchronize()
-    stats = {"swm_stage": plan.kernel_stats(_lib.K["QG_SWM_K_STAGE"])}
+    stats = {"swm_stage": plan.kernel_stats(_lib.K["QG_SWM_K_STAGE"]),
+             "swm_cluster": plan.kernel_stats(_lib.K["QG_SWM_K_CLUSTER"])}
     plan.set_profiling(False)
     bytes_step = {"swm_stage": 12.0 * lc * sum(s + 2 for s in range(ns))}
     prof_total = sum(ms for ms, _ in stats.values())
@@ -315,8 +320,10 @@ def swm_roofline(cfg, plan, pv, dev, step_ms):
         if not n:
             continue
         ms_t = ms * scale
-        per_launch = bytes_step[name] * P / n
-        gbs = bytes_step[name] * P / (ms_t / 1000.0) / 1e9
+        # the cluster engine moves the state through HBM once in and once out per launch
+        total = bytes_step[name] * P if name in bytes_step else 24.0 * lc * n
+        per_launch = total / n
+        gbs = total / (ms_t / 1000.0) / 1e9
         kernels[name] = {"launches": n, "total_ms": ms_t, "avg_us": ms_t * 1000.0 / n,
                          "bytes_per_launch": per_launch, "achieved_gbs": gbs, "hbm_frac": gbs / pk["hbm_gbs"],
                          "bound": "hbm", "traffic": traffic.get(name)}
@@ -341,7 +348,7 @@ def run_swm(args, dev, world, rank, local):
     from somax_gb300 import testcases as tc
 
     cfg = tc.SWM_CONFIGS[args.config]
-    m = sg.MultilayerShallowWater2D.create(**cfg.model_kwargs())
+    m = sg.MultilayerShallowWater2D.create(**cfg.model_kwargs(), engine=args.swm_engine)
     plan = m.plan(dev)
     pv = m._param_vector(dev)
     y0 = tc.swm_initial_state(cfg, seed=rank)
@@ -397,13 +404,15 @@ def run_swm(args, dev, world, rank, local):
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": SWM_DESC[cfg.name], "l2": "flushed between timed steps (256 MB write)",
-                   "graphs": "8-step CUDA graphs replayed", "status": status,
+                   "engine": plan.engine(cfg.scheme),
+                   "graphs": "8-step CUDA graphs replayed (stage engine); one launch per call (cluster engine)",
+                   "status": status,
                    "replicas": "independent basins per rank" if world > 1 else "one device"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": yh.numel() * 4,
                 "d2h_bytes_per_step": out.numel() * 4,
                 "api": "qg_swm_step (MultilayerShallowWater2D's plan) on a pinned host state copied in and out"},
         "roofline": roof,
-        "gpu_launches": ns * cfg.bench_steps * args.steps,
+        "gpu_launches": (1 if plan.engine(cfg.scheme)["engine"] == "cluster" else ns * cfg.bench_steps) * args.steps,
         "clocks": clk.summary(),
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -799,6 +808,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--groups", type=int, default=1,
                     help="ensemble only: split the members into this many plans stepped concurrently on their own streams")
+    ap.add_argument("--swm-engine", default="auto", choices=["auto", "stages", "cluster"],
+                    help="shallow-water configs: the cluster engine where the basin fits, one launch per stage, "
+                         "or the cluster engine forced")
     ap.add_argument("--cluster", default="auto", choices=["auto", "on", "off"],
                     help="cluster-resident stepping of small members: autotuned, forced on, or off")
     args = ap.parse_args()

@@ -330,9 +330,27 @@ int qg_swm_step(qg_swm_plan* plan, float* state, const float* params, double dt,
    No reference counterpart: the benchmark's per-kernel durations. */
 #define QG_SWM_K_STAGE 0   /* k_swm_stage: stage input, right-hand side, (last stage) next state */
 #define QG_SWM_K_COMBINE 1 /* k_swm_combine: a stage input of qg_reparam_step or its final combination */
-#define QG_SWM_K_COUNT 2
+#define QG_SWM_K_CLUSTER 2 /* k_swm_cluster: every step of a qg_swm_step call (cluster engine) */
+#define QG_SWM_K_COUNT 3
 int qg_swm_set_profiling(qg_swm_plan* plan, int enable);
 int qg_swm_kernel_stats(qg_swm_plan* plan, int kclass, double* total_ms, int64_t* launches);
+/* Stepping engine of qg_swm_step.  The cluster engine runs every step of a call in one launch
+   of one thread-block cluster (16, 8, 4 or 2 CTAs, each holding a band of rows of the state,
+   of the stage derivatives and of the stage inputs in shared memory; the halo rows come from
+   the neighbouring CTAs' shared memory); it applies when the basin fits (small grids, e.g.
+   2 layers of 64^2).  AUTO: the engine that ran 32 steps of a rest state faster, timed on the
+   plan's own buffers at the first qg_swm_step / qg_swm_engine call of each scheme (that call
+   synchronises the device; call qg_swm_engine before capturing qg_swm_step into a graph).
+   No reference counterpart: a switch of this library's launch schedule. */
+#define QG_SWM_ENGINE_AUTO 0
+#define QG_SWM_ENGINE_STAGES 1  /* one k_swm_stage launch per stage, graph-replayed */
+#define QG_SWM_ENGINE_CLUSTER 2 /* the cluster engine; qg_swm_step returns QG_ERR_UNSUPPORTED if it does not fit */
+int qg_swm_set_engine(qg_swm_plan* plan, int engine);
+/* The engine qg_swm_step uses for a scheme (QG_SWM_ENGINE_STAGES or _CLUSTER; a negative
+   QG_ERR_* on bad arguments), the cluster's CTA count (0 without the cluster engine) and,
+   when times_ms is not NULL, the tuning times of 32 steps (times_ms[0] the fastest cluster,
+   times_ms[1] the stage engine; -1 where not timed).  Tunes the scheme if not yet done. */
+int qg_swm_engine(qg_swm_plan* plan, int scheme, int* cluster_ctas, float* times_ms);
 /* ReparameterizedQG (somax/_src/models/qg/reparameterized.py:65-228) stepped like qg_swm_step:
    every stage input gets the model's apply_boundary_conditions (the SWM wall rules, then the
    geostrophic projection of qg_project on qgplan, reparameterized.py:186-189) before the

@@ -33,6 +33,7 @@
 #include <new>
 #include <vector>
 
+#include "qg_device.cuh"
 #include "qg_internal.cuh"
 
 namespace qg {
@@ -67,21 +68,25 @@ __device__ __forceinline__ float ld(const float* __restrict__ a, const SwmDev& d
     return __ldg(a + (int64_t)j * d.Nx + i);
 }
 
-// Source of the stage-input value of field fld (0 = h, 1 = u, 2 = v) at (j, i) after the
-// boundary rules (or as stored when !bc): its offset within the layer plane, or -1 where the
-// wall rules set it to zero.
-__device__ __forceinline__ int64_t src(const SwmDev& d, int fld, int j, int i, bool bc) {
-    if (bc) {
-        if (d.bc == QG_SWM_PERIODIC) {
-            j = j == 0 ? d.Ny - 2 : (j == d.Ny - 1 ? 1 : j);
-            i = i == 0 ? d.Nx - 2 : (i == d.Nx - 1 ? 1 : i);
-        } else {
-            if (fld == 1 && (i == 0 || i >= d.Nx - 2)) return -1;
-            if (fld == 2 && (j == 0 || j >= d.Ny - 2)) return -1;
-            if (fld != 2) j = min(max(j, 1), d.Ny - 2);
-            if (fld != 1) i = min(max(i, 1), d.Nx - 2);
-        }
+// The cell whose value field fld (0 = h, 1 = u, 2 = v) takes at (j, i) under the boundary
+// rules: (j, i) is moved there; false where the wall rules set the value to zero.
+__device__ __forceinline__ bool src_cell(const SwmDev& d, int fld, int& j, int& i) {
+    if (d.bc == QG_SWM_PERIODIC) {
+        j = j == 0 ? d.Ny - 2 : (j == d.Ny - 1 ? 1 : j);
+        i = i == 0 ? d.Nx - 2 : (i == d.Nx - 1 ? 1 : i);
+        return true;
     }
+    if (fld == 1 && (i == 0 || i >= d.Nx - 2)) return false;
+    if (fld == 2 && (j == 0 || j >= d.Ny - 2)) return false;
+    if (fld != 2) j = min(max(j, 1), d.Ny - 2);
+    if (fld != 1) i = min(max(i, 1), d.Nx - 2);
+    return true;
+}
+
+// Source of the stage-input value of field fld at (j, i) after the boundary rules (or as
+// stored when !bc): its offset within the layer plane, or -1 where the wall rules set it to zero.
+__device__ __forceinline__ int64_t src(const SwmDev& d, int fld, int j, int i, bool bc) {
+    if (bc && !src_cell(d, fld, j, i)) return -1;
     return (int64_t)j * d.Nx + i;
 }
 
@@ -170,32 +175,80 @@ __device__ __forceinline__ void store_input(StageTables& t, const StageArgs& a, 
     t.v[e] = y3[2];
 }
 
-// PV, face mass fluxes, kinetic energy and the pressure sum of one point of the haloed tile
-// (row r, column c; T-cell (jj, ii)).  Each is formed where some own cell of the tile reads it.
+// The eight tables of one layer of stage input over a block of points (rows of S points, E
+// points per table): h, u, v of the stage input, PV at the X points, u h at the U points,
+// v h at the V points, the kinetic energy and the cumulative hydrostatic pressure.
+struct Tab {
+    float* b;
+    int E, S;
+    __device__ __forceinline__ float* h() const { return b; }
+    __device__ __forceinline__ float* u() const { return b + E; }
+    __device__ __forceinline__ float* v() const { return b + 2 * E; }
+    __device__ __forceinline__ float* q() const { return b + 3 * E; }
+    __device__ __forceinline__ float* uh() const { return b + 4 * E; }
+    __device__ __forceinline__ float* vh() const { return b + 5 * E; }
+    __device__ __forceinline__ float* ke() const { return b + 6 * E; }
+    __device__ __forceinline__ float* p() const { return b + 7 * E; }
+};
+
+// PV, face mass fluxes, kinetic energy and the pressure sum at table point e (row r of
+// `rows`, column c; T-cell (jj, ii)), each formed where a neighbouring cell reads it; the
+// pressure adds g h to p.  INT: (jj, ii) is known to be strictly inside.
 template <bool INT>
-__device__ __forceinline__ void derive_point(StageTables& t, const SwmDev& d, float g, int r, int c, int jj, int ii,
-                                             float& q, float& uh, float& vh, float& ke, float& p) {
-    const int e = r * kStX + c;
+__device__ __forceinline__ void swm_derive(const Tab& t, const SwmDev& d, float g, int e, int r, int c, int rows,
+                                           int jj, int ii, float& q, float& uh, float& vh, float& ke, float& p) {
+    const int S = t.S;
+    const float *h = t.h(), *u = t.u(), *v = t.v();
     q = 0.f, uh = 0.f, vh = 0.f, ke = 0.f;
     if (INT || (jj >= 1 && jj <= d.Ny - 2 && ii >= 1 && ii <= d.Nx - 2)) {
-        if (r < kStY - 1 && c < kStX - 1) {
-            const float zeta = (t.v[e + 1] - t.v[e]) * d.idx - (t.u[e + kStX] - t.u[e]) * d.idy;
-            const float hX = 0.25f * (t.h[e] + t.h[e + 1] + t.h[e + kStX] + t.h[e + kStX + 1]);
+        if (r < rows - 1 && c < S - 1) {
+            const float zeta = (v[e + 1] - v[e]) * d.idx - (u[e + S] - u[e]) * d.idy;
+            const float hX = 0.25f * (h[e] + h[e + 1] + h[e + S] + h[e + S + 1]);
             q = (zeta + __ldg(d.fx + jj)) / hX;
         }
-        if (c < kStX - 1) uh = 0.5f * (t.h[e] + t.h[e + 1]) * t.u[e];
-        if (r < kStY - 1) vh = 0.5f * (t.h[e] + t.h[e + kStX]) * t.v[e];
+        if (c < S - 1) uh = 0.5f * (h[e] + h[e + 1]) * u[e];
+        if (r < rows - 1) vh = 0.5f * (h[e] + h[e + S]) * v[e];
         if (r > 0 && c > 0) {
-            const float ua = t.u[e], ub = t.u[e - 1], va = t.v[e], vb = t.v[e - kStX];
+            const float ua = u[e], ub = u[e - 1], va = v[e], vb = v[e - S];
             ke = 0.25f * (ua * ua + ub * ub + va * va + vb * vb);
         }
     }
-    p = fmaf(g, t.h[e], p);
-    t.q[e] = q;
-    t.uh[e] = uh;
-    t.vh[e] = vh;
-    t.ke[e] = ke;
-    t.p[e] = p;
+    p = fmaf(g, h[e], p);
+    t.q()[e] = q;
+    t.uh()[e] = uh;
+    t.vh()[e] = vh;
+    t.ke()[e] = ke;
+    t.p()[e] = p;
+}
+
+// dh, du, dv of layer k at table point e of T-cell row j (in: strictly inside) from the tables
+// and the point's own stage input (h0, u0, v0) and derived values (q0, uh0, vh0, ke0, p0).
+__device__ __forceinline__ void swm_tend(const Tab& t, const SwmDev& d, int e, int j, bool in, bool top, bool bottom,
+                                         float nu, float kappa, float tau0, float h0, float u0, float v0, float q0,
+                                         float uh0, float vh0, float ke0, float p0, float& dh, float& du, float& dv) {
+    const int S = t.S;
+    const float *h = t.h(), *u = t.u(), *v = t.v();
+    dh = 0.f;
+    du = (top ? tau0 * __ldg(d.wx + j) * d.invH0 : 0.f) - (bottom ? kappa * u0 : 0.f);
+    dv = bottom ? -kappa * v0 : 0.f;
+    if (!in) return;
+    const float uw = u[e - 1], vs = v[e - S];
+    const float fe = u0 * (u0 > 0.f ? h0 : h[e + 1]);
+    const float fw = uw * (uw > 0.f ? h[e - 1] : h0);
+    const float gn = v0 * (v0 > 0.f ? h0 : h[e + S]);
+    const float gs = vs * (vs > 0.f ? h[e - S] : h0);
+    dh = -((fe - fw) * d.idx + (gn - gs) * d.idy);
+    const float *q = t.q(), *uh = t.uh(), *vh = t.vh(), *ke = t.ke(), *p = t.p();
+    const float qU = 0.5f * (q0 + q[e - S]);
+    const float qV = 0.5f * (q0 + q[e - 1]);
+    const float vhU = 0.25f * (vh0 + vh[e + 1] + vh[e - S] + vh[e - S + 1]);
+    const float uhV = 0.25f * (uh0 + uh[e - 1] + uh[e + S] + uh[e + S - 1]);
+    const float Pc = ke0 + p0, Pe = ke[e + 1] + p[e + 1];
+    const float Pn = ke[e + S] + p[e + S];
+    const float lu = (u[e + 1] - 2.f * u0 + uw) * d.idx2 + (u[e + S] - 2.f * u0 + u[e - S]) * d.idy2;
+    const float lv = (v[e + 1] - 2.f * v0 + v[e - 1]) * d.idx2 + (v[e + S] - 2.f * v0 + vs) * d.idy2;
+    du += qU * vhU - (Pe - Pc) * d.idx + nu * lu;
+    dv += -qV * uhV - (Pn - Pc) * d.idy + nu * lv;
 }
 
 // A CTA owns a 32 x 8 tile of T-cells and walks the layers.  Per layer each thread loads its
@@ -217,6 +270,7 @@ __device__ __forceinline__ void stage_tile(StageTables& t, const SwmDev& d, cons
     int hr = 0, hc = 0;
     if (halo) halo_rc(tid, hr, hc);
     const int he = hr * kStX + hc;
+    const Tab tb{t.h, kStE, kStX};
     bool bad = false;
     float po = 0.f, ph = 0.f;  // cumulative pressure at the own and the halo cell
     for (int k = 0; k < d.nl; ++k) {
@@ -229,36 +283,13 @@ __device__ __forceinline__ void stage_tile(StageTables& t, const SwmDev& d, cons
         __syncthreads();
         const float g = __ldg(d.gp + k);
         float qo = 0.f, uho = 0.f, vho = 0.f, keo = 0.f, x0, x1, x2, x3;
-        if (mine) derive_point<INT>(t, d, g, threadIdx.y + 1, threadIdx.x + 1, j, i, qo, uho, vho, keo, po);
-        if (halo) derive_point<INT>(t, d, g, hr, hc, j0 + hr, i0 + hc, x0, x1, x2, x3, ph);
+        if (mine) swm_derive<INT>(tb, d, g, eo, threadIdx.y + 1, threadIdx.x + 1, kStY, j, i, qo, uho, vho, keo, po);
+        if (halo) swm_derive<INT>(tb, d, g, he, hr, hc, kStY, j0 + hr, i0 + hc, x0, x1, x2, x3, ph);
         __syncthreads();
         if (mine) {
-            const bool top = k == 0, bottom = k == d.nl - 1;
-            const int e = eo;
-            const float uc = yo3[1], vc = yo3[2];
-            float dh = 0.f;
-            float du = (top ? tau0 * __ldg(d.wx + j) * d.invH0 : 0.f) - (bottom ? kappa * uc : 0.f);
-            float dv = bottom ? -kappa * vc : 0.f;
-            if (in) {
-                const float hc0 = yo3[0], uw = t.u[e - 1], vs = t.v[e - kStX];
-                const float fe = uc * (uc > 0.f ? hc0 : t.h[e + 1]);
-                const float fw = uw * (uw > 0.f ? t.h[e - 1] : hc0);
-                const float gn = vc * (vc > 0.f ? hc0 : t.h[e + kStX]);
-                const float gs = vs * (vs > 0.f ? t.h[e - kStX] : hc0);
-                dh = -((fe - fw) * d.idx + (gn - gs) * d.idy);
-                const float qU = 0.5f * (qo + t.q[e - kStX]);
-                const float qV = 0.5f * (qo + t.q[e - 1]);
-                const float vhU = 0.25f * (vho + t.vh[e + 1] + t.vh[e - kStX] + t.vh[e - kStX + 1]);
-                const float uhV = 0.25f * (uho + t.uh[e - 1] + t.uh[e + kStX] + t.uh[e + kStX - 1]);
-                const float Pc = keo + po, Pe = t.ke[e + 1] + t.p[e + 1];
-                const float Pn = t.ke[e + kStX] + t.p[e + kStX];
-                const float lu =
-                    (t.u[e + 1] - 2.f * uc + uw) * d.idx2 + (t.u[e + kStX] - 2.f * uc + t.u[e - kStX]) * d.idy2;
-                const float lv =
-                    (t.v[e + 1] - 2.f * vc + t.v[e - 1]) * d.idx2 + (t.v[e + kStX] - 2.f * vc + vs) * d.idy2;
-                du += qU * vhU - (Pe - Pc) * d.idx + nu * lu;
-                dv += -qV * uhV - (Pn - Pc) * d.idy + nu * lv;
-            }
+            float dh, du, dv;
+            swm_tend(tb, d, eo, j, in, k == 0, k == d.nl - 1, nu, kappa, tau0, yo3[0], yo3[1], yo3[2], qo, uho, vho,
+                     keo, po, dh, du, dv);
             bad |= !isfinite(dh) || !isfinite(du) || !isfinite(dv);
             const int64_t o = lo + (int64_t)j * d.Nx + i;
             const float F[3] = {dh, du, dv};
@@ -298,6 +329,214 @@ __global__ void __launch_bounds__(kSwTX * kSwTY) k_swm_stage(SwmDev d, StageArgs
         stage_tile<NS, LAST, true>(t, d, a);
     else
         stage_tile<NS, LAST, false>(t, d, a);
+}
+
+// ---- cluster-resident engine: every step of a small basin in one thread-block cluster -----
+//
+// The C CTAs of one cluster own bands of R rows of the padded grid (CTA c: rows c R ..
+// c R + R - 1) and keep, in shared memory, their rows of the state, of the stage derivatives
+// K_0 .. K_{ns-2} and of two stage-input buffers.  Per stage a CTA forms its rows' stage input,
+// one cluster barrier publishes it, and each CTA builds its tables from its own rows plus one
+// row above and below, read from the neighbouring CTAs' shared memory (the boundary rules
+// may take a ring row's value from any CTA: distributed shared memory, mapa + ld.shared::cluster).
+// The stage inputs alternate between the two buffers, so one barrier per stage orders both
+// the reads of a buffer and its next overwrite.  The arithmetic per cell is the stage
+// kernel's (swm_derive, swm_tend).
+
+constexpr int kScThreads = 1024;
+
+struct SwmClusterArgs {
+    SwmDev d;
+    float* state;          // packed state, in place
+    const float* params;   // nu, kappa, tau0
+    int* flags;
+    int n_steps, ns, R;
+    float a[kMaxButcher][kMaxButcher];  // dt * Butcher a
+    float b[kMaxButcher];               // dt * Butcher b
+};
+
+__device__ __forceinline__ unsigned sc_rank() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+// All threads of every CTA of the cluster; orders shared (local and remote) and global memory
+// at cluster scope.
+__device__ __forceinline__ void sc_sync() {
+    asm volatile(
+        "barrier.cluster.arrive.release.aligned;\n"
+        "barrier.cluster.wait.acquire.aligned;" ::
+            : "memory");
+}
+// floats of shared memory per CTA: state, ns - 1 derivatives, two stage inputs (3 nl R Nx
+// each) and the eight tables of every layer over (R + 2) x Nx points
+__host__ __device__ inline int64_t swm_cluster_floats(int nl, int R, int Nx, int ns) {
+    return (int64_t)3 * nl * R * Nx * (ns + 2) + (int64_t)8 * nl * (R + 2) * Nx;
+}
+
+// The shared::cluster address of `p` (a location of this CTA's shared memory) in CTA `rank`.
+__device__ __forceinline__ uint32_t sc_map(const float* p, unsigned rank) {
+    uint32_t a;
+    asm("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(a) : "r"(su32(p)), "r"(rank));
+    return a;
+}
+// Reads of the stage inputs that a cluster barrier published; nothing writes them before the
+// next barrier, so the loads need no ordering of their own.
+__device__ __forceinline__ float sc_ld(uint32_t a) {
+    float v;
+    asm("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(a));
+    return v;
+}
+
+// Row (in the padded grid) that field f of row j takes its values from under the boundary
+// rules, or -1 where the wall rules make the whole row zero.
+__device__ __forceinline__ int src_row(const SwmDev& d, int f, int j) {
+    if (d.bc == QG_SWM_PERIODIC) return j == 0 ? d.Ny - 2 : (j == d.Ny - 1 ? 1 : j);
+    if (f == 2) return (j == 0 || j >= d.Ny - 2) ? -1 : j;
+    return min(max(j, 1), d.Ny - 2);
+}
+// Column of the same rule, or -1 where it is zero.
+__device__ __forceinline__ int src_col(const SwmDev& d, int f, int i) {
+    if (d.bc == QG_SWM_PERIODIC) return i == 0 ? d.Nx - 2 : (i == d.Nx - 1 ? 1 : i);
+    if (f == 1) return (i == 0 || i >= d.Nx - 2) ? -1 : i;
+    return min(max(i, 1), d.Nx - 2);
+}
+
+// A thread's walk over the points (k, r, i) of nk x nr x W (i fastest) in strides of
+// kScThreads: the decomposition of its first point once, then carries instead of divisions.
+struct Walk {
+    int k, r, i, dr, di;
+    __device__ __forceinline__ Walk(int x, int nr, int W) {
+        const int kr = x / W;
+        i = x - kr * W;
+        k = kr / nr;
+        r = kr - k * nr;
+        dr = kScThreads / W;
+        di = kScThreads - dr * W;
+    }
+    __device__ __forceinline__ void next(int nr, int W) {
+        i += di;
+        r += dr;
+        if (i >= W) {
+            i -= W;
+            ++r;
+        }
+        while (r >= nr) {
+            r -= nr;
+            ++k;
+        }
+    }
+};
+
+// Per stage: (a) the stage input of the own rows (flat over the own-row arrays), a cluster
+// barrier, (b) every layer's tables (one warp per table row, the rows above and below from the
+// neighbouring CTAs), (c) the derived quantities of every layer at every table point (the
+// cumulative pressure summed over the layers above), (d) the own cells' tendencies
+// and the stage derivative or the next state; each phase hands out one point per thread.
+// Three CTA barriers and one cluster barrier a stage.
+__global__ void __launch_bounds__(kScThreads) k_swm_cluster(SwmClusterArgs a) {
+    extern __shared__ __align__(16) float sm[];
+    const SwmDev& d = a.d;
+    const int W = d.Nx, R = a.R, nl = d.nl, ns = a.ns;
+    const unsigned rank = sc_rank();
+    const int j0 = (int)rank * R;                // first own row
+    const int rows = max(0, min(R, d.Ny - j0));  // own rows (the last CTAs may have fewer)
+    const int F = 3 * nl * R * W;                // floats of the own rows of one state
+    float* Y = sm;                               // the state's own rows, [f][k][r][i]
+    float* K = Y + F;                            // K_0 .. K_{ns-2}
+    float* Yb = K + (ns - 1) * F;                // two stage-input buffers
+    float* Tb = Yb + 2 * F;                      // tables, 8 (R + 2) W floats per layer
+    const int E = (R + 2) * W, ER = rows + 2;
+    const int64_t plane = (int64_t)d.Ny * W;
+    const float nu = a.params[0], kappa = a.params[1], tau0 = a.params[2];
+    const int tid = threadIdx.x;
+    // the own rows in (rows beyond the grid, in the last CTAs, are zero and never read)
+    for (int o = tid; o < F; o += kScThreads) {
+        const int fk = o / (R * W), r = (o / W) % R, i = o % W;
+        Y[o] = r < rows ? a.state[fk * plane + (int64_t)(j0 + r) * W + i] : 0.f;
+    }
+    __syncthreads();
+    bool bad = false;
+    int par = 0;
+    for (int step = 0; step < a.n_steps; ++step) {
+        for (int s = 0; s < ns; ++s, par ^= 1) {
+            float* Yp = Yb + par * F;
+            // (a)
+            for (int o = tid; o < F; o += kScThreads) {
+                float acc = Y[o];
+                for (int m = 0; m < s; ++m) acc = fmaf(a.a[s][m], K[m * F + o], acc);
+                Yp[o] = acc;
+            }
+            sc_sync();
+            // (b) table row re of layer k holds grid row j0 - 1 + re
+            Walk wb(tid, ER, W);
+            for (int x = tid; x < nl * ER * W; x += kScThreads, wb.next(ER, W)) {
+                const int k = wb.k, re = wb.r, i = wb.i, j = j0 - 1 + re;
+                float* tk = Tb + k * 8 * E + re * W + i;  // h; u and v E and 2 E further
+#pragma unroll
+                for (int f = 0; f < 3; ++f) {
+                    const int jj = (j >= 0 && j < d.Ny) ? src_row(d, f, j) : -1;
+                    const int ii = src_col(d, f, i);
+                    float v = 0.f;
+                    if (jj >= 0 && ii >= 0) {
+                        const unsigned owner =
+                            (jj >= j0 && jj < j0 + rows) ? rank : (jj == j0 - 1 ? rank - 1 : (unsigned)(jj / R));
+                        const float* ptr = Yp + ((f * nl + k) * R + (jj - (int)owner * R)) * W + ii;
+                        v = owner == rank ? *ptr : sc_ld(sc_map(ptr, owner));
+                    }
+                    tk[f * E] = v;
+                }
+            }
+            __syncthreads();
+            // (c) one layer-point per thread; the pressure of layer k sums g'_l h_l over l < k first
+            Walk wc(tid, ER, W);
+            for (int x = tid; x < nl * ER * W; x += kScThreads, wc.next(ER, W)) {
+                const int k = wc.k, re = wc.r, i = wc.i, e = re * W + i, j = j0 - 1 + re;
+                float p = 0.f;
+                for (int l = 0; l < k; ++l) p = fmaf(__ldg(d.gp + l), Tb[l * 8 * E + e], p);
+                const Tab t{Tb + k * 8 * E, E, W};
+                float q, uh, vh, ke;
+                swm_derive<false>(t, d, __ldg(d.gp + k), e, re, i, ER, j, i, q, uh, vh, ke, p);
+            }
+            __syncthreads();
+            // (d) one layer-cell per thread
+            const bool last = s == ns - 1;
+            Walk wd(tid, rows > 0 ? rows : 1, W);
+            for (int x = tid; x < nl * rows * W; x += kScThreads, wd.next(rows, W)) {
+                const int k = wd.k, r = wd.r, i = wd.i, j = j0 + r;
+                {
+                    const int e = (r + 1) * W + i;
+                    const bool in = j >= 1 && j <= d.Ny - 2 && i >= 1 && i <= d.Nx - 2;
+                    {
+                        const Tab t{Tb + k * 8 * E, E, W};
+                        float dh, du, dv;
+                        swm_tend(t, d, e, j, in, k == 0, k == nl - 1, nu, kappa, tau0, t.h()[e], t.u()[e], t.v()[e],
+                                 t.q()[e], t.uh()[e], t.vh()[e], t.ke()[e], t.p()[e], dh, du, dv);
+                        bad |= !isfinite(dh) || !isfinite(du) || !isfinite(dv);
+                        const float Fv[3] = {dh, du, dv};
+#pragma unroll
+                        for (int f = 0; f < 3; ++f) {
+                            const int o = ((f * nl + k) * R + r) * W + i;
+                            if (!last) {
+                                K[s * F + o] = Fv[f];
+                            } else {
+                                float y = fmaf(a.b[s], Fv[f], Y[o]);
+                                for (int m = 0; m < s; ++m) y = fmaf(a.b[m], K[m * F + o], y);
+                                Y[o] = y;
+                            }
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (int o = tid; o < F; o += kScThreads) {
+        const int fk = o / (R * W), r = (o / W) % R, i = o % W;
+        if (r < rows) a.state[fk * plane + (int64_t)(j0 + r) * W + i] = Y[o];
+    }
+    if (bad && a.flags) atomicOr(a.flags, 1);
+    sc_sync();  // no CTA leaves while another may still read its stage input
 }
 
 struct Combine {
@@ -350,6 +589,14 @@ struct qg_swm_plan {
     int* flags = nullptr;
     int64_t n = 0;            // floats of one state
     int device = 0;
+    int engine = QG_SWM_ENGINE_AUTO;
+    // cluster configuration per stage count (C CTAs of R rows, dynamic shared memory; C = 0:
+    // does not fit, -1: not yet probed)
+    int cl_C[kMaxButcher + 1] = {-1, -1, -1, -1, -1, -1, -1};
+    int cl_R[kMaxButcher + 1] = {};
+    size_t cl_smem[kMaxButcher + 1] = {};
+    bool cl_auto[kMaxButcher + 1] = {};  // AUTO takes the cluster engine (timed faster)
+    float cl_ms[kMaxButcher + 1] = {}, st_ms[kMaxButcher + 1] = {};  // timed 32 steps, each engine
     // qg_swm_step replays captured graphs of 8 steps and of 1 step, while the state pointer,
     // dt and the scheme repeat
     cudaStream_t cap = nullptr;
@@ -436,6 +683,7 @@ extern "C" int qg_swm_create(const qg_swm_desc* desc, qg_swm_plan** out) {
     if (!e) e = cudaMalloc(&p->stage, p->n * sizeof(float));
     if (!e) e = cudaMalloc(&p->K, (size_t)kMaxButcher * p->n * sizeof(float));
     if (!e) e = cudaMalloc(&p->params, 4 * sizeof(float));
+    if (!e) e = cudaMemset(p->params, 0, 4 * sizeof(float));
     if (!e) e = cudaMalloc(&p->proj, p->n * sizeof(float));
     if (!e) e = cudaMalloc(&p->flags, 16);
     if (!e) e = cudaMemset(p->flags, 0, 16);
@@ -547,12 +795,196 @@ cudaError_t swm_steps(qg_swm_plan* p, float* state, const Tableau* tb, double dt
 }
 }  // namespace
 
+namespace {
+// Whether a cluster of C CTAs holds the basin for a scheme of ns stages: shared memory within
+// the device's opt-in limit and at least one such cluster resident.
+bool swm_cluster_fits(const qg_swm_plan* p, int ns, int C, int* R_out, size_t* bytes_out) {
+    int optin = 0;
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device)) return false;
+    const int R = (p->d.Ny + C - 1) / C;
+    const size_t bytes = (size_t)swm_cluster_floats(p->d.nl, R, p->d.Nx, ns) * sizeof(float);
+    if (bytes > (size_t)optin) return false;
+    if (cudaFuncSetAttribute(k_swm_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes)) return false;
+    if (C > 8 && cudaFuncSetAttribute(k_swm_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1)) return false;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)C);
+    cfg.blockDim = dim3(kScThreads);
+    cfg.dynamicSmemBytes = bytes;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, k_swm_cluster, &cfg) != cudaSuccess || n < 1) return false;
+    *R_out = R;
+    *bytes_out = bytes;
+    return true;
+}
+
+cudaError_t launch_swm_cluster(qg_swm_plan* p, float* state, const Tableau* tb, double dt, int n_steps,
+                               cudaStream_t s);
+
+// Milliseconds of `run` on the plan's capture stream (one warm-up run first), or -1.
+template <class F>
+float swm_time(qg_swm_plan* p, F&& run) {
+    cudaEvent_t a = nullptr, b = nullptr;
+    float ms = -1.f;
+    if (cudaEventCreate(&a) == cudaSuccess && cudaEventCreate(&b) == cudaSuccess && run() == cudaSuccess &&
+        cudaEventRecord(a, p->cap) == cudaSuccess && run() == cudaSuccess &&
+        cudaEventRecord(b, p->cap) == cudaSuccess && cudaEventSynchronize(b) == cudaSuccess)
+        cudaEventElapsedTime(&ms, a, b);
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    cudaGetLastError();
+    return ms;
+}
+
+// Engine choice for a scheme of ns stages, once per ns (synchronises the device): every
+// cluster size that fits (16, 8, 4, 2 CTAs) and the one-launch-per-stage engine (as 8-step
+// graphs) each time 32 steps of the rest state in the plan's projection buffer; the fastest
+// cluster size is kept for the cluster engine, and AUTO takes the cluster engine when it beat
+// the stage engine.
+void swm_tune(qg_swm_plan* p, const Tableau* tb) {
+    const int ns = tb->n;
+    if (p->cl_C[ns] >= 0) return;
+    const bool prof = p->profiling;
+    p->profiling = false;
+    const qg_swm_desc& ds = p->desc;
+    double Hs = 0.0;
+    for (int k = 0; k < ds.n_layers; ++k) Hs += ds.H[k];
+    const double dt = 0.1 * std::min(ds.Lx / ds.nx, ds.Ly / ds.ny) / std::sqrt(9.81 * Hs);
+    std::vector<float> rest((size_t)p->n, 0.f);
+    const size_t lay = (size_t)p->d.Ny * p->d.Nx;
+    for (int k = 0; k < ds.n_layers; ++k)
+        std::fill(rest.begin() + k * lay, rest.begin() + (k + 1) * lay, (float)ds.H[k]);
+    float* y = p->proj;
+    auto reset = [&] {
+        return cudaMemcpyAsync(y, rest.data(), rest.size() * sizeof(float), cudaMemcpyHostToDevice, p->cap);
+    };
+    int bestC = 0, bestR = 0;
+    size_t bestB = 0;
+    float best = -1.f;
+    for (int C = 16; C >= 2; C /= 2) {
+        int R = 0;
+        size_t bytes = 0;
+        if (!swm_cluster_fits(p, ns, C, &R, &bytes)) continue;
+        p->cl_C[ns] = C;  // read by launch_swm_cluster
+        p->cl_R[ns] = R;
+        p->cl_smem[ns] = bytes;
+        const float ms = swm_time(p, [&] {
+            const cudaError_t e = reset();
+            return e ? e : launch_swm_cluster(p, y, tb, dt, 32, p->cap);
+        });
+        if (ms > 0.f && (best < 0.f || ms < best)) {
+            best = ms;
+            bestC = C;
+            bestR = R;
+            bestB = bytes;
+        }
+    }
+    p->cl_C[ns] = bestC;
+    p->cl_R[ns] = bestR;
+    p->cl_smem[ns] = bestB;
+    p->cl_ms[ns] = best;
+    float st = -1.f;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t g = nullptr;
+    if (cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        const cudaError_t e1 = swm_steps(p, y, tb, dt, 8, p->cap);
+        if (cudaStreamEndCapture(p->cap, &graph) == cudaSuccess && e1 == cudaSuccess && graph)
+            if (cudaGraphInstantiate(&g, graph, 0) != cudaSuccess) g = nullptr;
+        if (graph) cudaGraphDestroy(graph);
+    }
+    if (g) {
+        st = swm_time(p, [&] {
+            cudaError_t e = reset();
+            for (int r = 0; r < 4 && !e; ++r) e = cudaGraphLaunch(g, p->cap);
+            return e;
+        });
+        cudaGraphExecDestroy(g);
+    }
+    p->st_ms[ns] = st;
+    p->cl_auto[ns] = bestC > 0 && (st < 0.f || best < st);
+    p->profiling = prof;
+    cudaGetLastError();
+}
+
+// Every step of one qg_swm_step call in one cluster launch.
+cudaError_t launch_swm_cluster(qg_swm_plan* p, float* state, const Tableau* tb, double dt, int n_steps,
+                               cudaStream_t s) {
+    const int ns = tb->n, C = p->cl_C[ns];
+    // plans of other sizes may have set the kernel's shared-memory limit since
+    cudaError_t e = cudaFuncSetAttribute(k_swm_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)p->cl_smem[ns]);
+    if (e) return e;
+    SwmClusterArgs a{};
+    a.d = p->d;
+    a.state = state;
+    a.params = p->params;
+    a.flags = p->flags;
+    a.n_steps = n_steps;
+    a.ns = ns;
+    a.R = p->cl_R[ns];
+    for (int i = 0; i < ns; ++i) {
+        for (int m = 0; m < i; ++m) a.a[i][m] = (float)(dt * tb->a[i][m]);
+        a.b[i] = (float)(dt * tb->b[i]);
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)C);
+    cfg.blockDim = dim3(kScThreads);
+    cfg.dynamicSmemBytes = p->cl_smem[ns];
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return swm_timed(p, QG_SWM_K_CLUSTER, s, [&] { return cudaLaunchKernelEx(&cfg, k_swm_cluster, a); });
+}
+}  // namespace
+
+extern "C" int qg_swm_set_engine(qg_swm_plan* p, int engine) {
+    if (!p) return QG_ERR_NULL;
+    if (engine < QG_SWM_ENGINE_AUTO || engine > QG_SWM_ENGINE_CLUSTER) return QG_ERR_ARG;
+    p->engine = engine;
+    return QG_OK;
+}
+
+namespace {
+// Whether qg_swm_step runs a scheme on the cluster engine (tunes the scheme first).
+bool swm_use_cluster(qg_swm_plan* p, const Tableau* tb) {
+    if (p->engine == QG_SWM_ENGINE_STAGES) return false;
+    swm_tune(p, tb);
+    return p->engine == QG_SWM_ENGINE_CLUSTER ? p->cl_C[tb->n] > 0 : p->cl_auto[tb->n];
+}
+}  // namespace
+
+extern "C" int qg_swm_engine(qg_swm_plan* p, int scheme, int* cluster_ctas, float* times_ms) {
+    if (!p) return -QG_ERR_NULL;
+    const Tableau* tb = swm_tableau(scheme);
+    if (!tb) return -QG_ERR_ARG;
+    const bool cl = swm_use_cluster(p, tb);
+    if (cluster_ctas) *cluster_ctas = cl ? p->cl_C[tb->n] : 0;
+    if (times_ms) {
+        times_ms[0] = p->cl_C[tb->n] >= 0 ? p->cl_ms[tb->n] : -1.f;
+        times_ms[1] = p->cl_C[tb->n] >= 0 ? p->st_ms[tb->n] : -1.f;
+    }
+    return cl ? QG_SWM_ENGINE_CLUSTER : QG_SWM_ENGINE_STAGES;
+}
+
 extern "C" int qg_swm_step(qg_swm_plan* p, float* state, const float* params, double dt, int n_steps, int scheme,
                            int flags, void* stream) {
     if (!p || !state || !params) return QG_ERR_NULL;
     if (n_steps < 0 || (flags & ~QG_STEP_APPLY_BC) || !(dt == dt)) return QG_ERR_ARG;
     const Tableau* tb = swm_tableau(scheme);
     if (!tb) return QG_ERR_ARG;
+    const bool cluster = swm_use_cluster(p, tb);
+    if (p->engine == QG_SWM_ENGINE_CLUSTER && !cluster) return QG_ERR_UNSUPPORTED;
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = cudaMemcpyAsync(p->params, params, 3 * sizeof(float), cudaMemcpyDeviceToDevice, s);
     if (!e && (flags & QG_STEP_APPLY_BC)) {
@@ -560,6 +992,7 @@ extern "C" int qg_swm_step(qg_swm_plan* p, float* state, const float* params, do
         e = cudaGetLastError();
     }
     if (e || n_steps == 0) return e ? QG_ERR_CUDA : QG_OK;
+    if (cluster) return launch_swm_cluster(p, state, tb, dt, n_steps, s) ? QG_ERR_CUDA : QG_OK;
     if (p->g_state != state || p->g_dt != dt || p->g_scheme != scheme) {
         for (cudaGraphExec_t* x : {&p->g8, &p->g1})
             if (*x) {

@@ -29,6 +29,8 @@ from .transforms import ModalTransform, StratificationProfile
 K = _lib.K
 _SCHEMES = {"euler": K["QG_SCHEME_EULER"], "heun": K["QG_SCHEME_HEUN"], "ssprk3": K["QG_SCHEME_SSPRK3"],
             "tsit5": K["QG_SCHEME_TSIT5"]}
+_ENGINES = {"auto": K["QG_SWM_ENGINE_AUTO"], "stages": K["QG_SWM_ENGINE_STAGES"],
+            "cluster": K["QG_SWM_ENGINE_CLUSTER"]}
 
 
 @dataclasses.dataclass
@@ -138,6 +140,23 @@ class SwmPlan:
         flags = C.c_int(0)
         return self._L.qg_swm_status(self._h, C.byref(flags), _stream_handle(self.device))
 
+    def set_engine(self, engine: str):
+        """``"auto"`` (the cluster engine where the basin fits), ``"stages"`` (one launch per
+        stage) or ``"cluster"`` (every step of a call in one thread-block cluster)."""
+        check(self._L.qg_swm_set_engine(self._h, _ENGINES[engine]), "qg_swm_set_engine")
+
+    def engine(self, scheme: str = "tsit5") -> dict:
+        """The engine ``step`` uses for ``scheme``, the cluster's CTA count and the tuning times
+        of 32 steps (ms; the fastest cluster size and the stage engine)."""
+        c = C.c_int(0)
+        t = (C.c_float * 2)()
+        with torch.cuda.device(self.device):
+            r = self._L.qg_swm_engine(self._h, _SCHEMES[scheme], C.byref(c), t)
+        if r < 0:
+            check(-r, "qg_swm_engine")
+        return {"engine": "cluster" if r == K["QG_SWM_ENGINE_CLUSTER"] else "stages", "cluster_ctas": c.value,
+                "tuning_ms": {"cluster": t[0], "stages": t[1]}}
+
     def set_profiling(self, on: bool):
         """CUDA events around every launch of ``step`` (graphs bypassed); resets the counters."""
         check(self._L.qg_swm_set_profiling(self._h, int(on)), "qg_swm_set_profiling")
@@ -155,7 +174,10 @@ class MultilayerShallowWater2D(SomaxModel):
 
     state_cls = MultilayerSW2DState
 
-    def __init__(self, params, consts, grid, strat, modal, wind_profile, bc, method):
+    def __init__(self, params, consts, grid, strat, modal, wind_profile, bc, method, engine="auto"):
+        if engine not in _ENGINES:
+            raise ValueError(f"engine must be one of {sorted(_ENGINES)}, got {engine!r}")
+        self.engine = engine
         self.params = params
         self.consts = consts
         self.grid = grid
@@ -171,8 +193,10 @@ class MultilayerShallowWater2D(SomaxModel):
                f0: float = 9.375e-5, beta: float = 1.754e-11, n_layers: int = 3,
                H=(400.0, 1100.0, 2600.0), g_prime=(9.81, 0.025, 0.0125), stratification=None,
                lateral_viscosity: float = 0.0, bottom_drag: float = 0.0, wind_amplitude: float = 0.0,
-               wind_profile: str = "doublegyre", bc: str = "periodic", method: str = "upwind1"):
-        """``MultilayerShallowWater2D.create`` with the same keyword arguments."""
+               wind_profile: str = "doublegyre", bc: str = "periodic", method: str = "upwind1",
+               engine: str = "auto"):
+        """``MultilayerShallowWater2D.create`` with the same keyword arguments, plus the stepping
+        engine of ``step`` / ``integrate`` (``SwmPlan.set_engine``)."""
         if stratification is not None:
             strat = stratification
         else:
@@ -189,7 +213,7 @@ class MultilayerShallowWater2D(SomaxModel):
                                                                         wind_amplitude)))
         consts = MultilayerSW2DPhysConsts(gravity=g, f0=f0, beta=beta, n_layers=strat.nl)
         return MultilayerShallowWater2D(params, consts, SWGrid(nx, ny, Lx, Ly), strat, modal, wind_profile, bc,
-                                        method)
+                                        method, engine)
 
     # ---- plumbing -------------------------------------------------------------------------
     @property
@@ -217,6 +241,7 @@ class MultilayerShallowWater2D(SomaxModel):
         key = dev.index
         if key not in self._plans:
             self._plans[key] = SwmPlan(self._desc(), dev)
+            self._plans[key].set_engine(self.engine)
         return self._plans[key]
 
     def _param_vector(self, device) -> torch.Tensor:

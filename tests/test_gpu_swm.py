@@ -24,10 +24,10 @@ CASES = [((16, 16), (500.0, 500.0), (9.81, 0.02)),
          ((30, 30), (200.0, 356.0, 632.0, 1125.0, 2000.0), (9.81, 0.03, 0.02, 0.0125, 0.008))]
 
 
-def pair(n, H, gp, bc, nu=300.0, kappa=1e-5, tau=2e-3, Lx=1.2e6, Ly=0.9e6):
+def pair(n, H, gp, bc, nu=300.0, kappa=1e-5, tau=2e-3, Lx=1.2e6, Ly=0.9e6, engine="auto"):
     kw = dict(nx=n[0], ny=n[1], Lx=Lx, Ly=Ly, f0=1e-4, beta=1.6e-11, H=H, g_prime=gp, lateral_viscosity=nu,
               bottom_drag=kappa, wind_amplitude=tau, bc=bc)
-    m = sg.MultilayerShallowWater2D.create(n_layers=len(H), **kw)
+    m = sg.MultilayerShallowWater2D.create(n_layers=len(H), engine=engine, **kw)
     return m, W.create(**kw)
 
 
@@ -93,11 +93,13 @@ def test_apply_bc_bit_equal(bc):
     assert np.array_equal(got.astype(np.float32), ref.astype(np.float32))
 
 
+@pytest.mark.parametrize("engine", ["stages", "cluster"])
 @pytest.mark.parametrize("scheme", ["heun", "ssprk3", "tsit5"])
 @pytest.mark.parametrize("bc", ["periodic", "wall"])
-def test_steps_match_oracle(scheme, bc):
+def test_steps_match_oracle(scheme, bc, engine):
     n, H, gp = CASES[1]
-    m, o = pair(n, H, gp, bc)
+    m, o = pair(n, H, gp, bc, engine=engine)
+    assert m.plan().engine(scheme)["engine"] == engine
     y = state(o, 20)
     dt = 0.2 * min(o.dx, o.dy) / np.sqrt(9.81 * sum(H))
     got = as_np(m.step(gpu_state(m, y), dt, 20, scheme))
@@ -149,3 +151,51 @@ def test_integrate_saveat_equals_steps_and_nonfinite_flag():
     m.step(gpu_state(m, bad), dt, 1, "heun")
     assert m.status() == _lib.K["QG_ERR_NONFINITE"]
     assert m.status() == 0
+
+
+@pytest.mark.parametrize("scheme", ["euler", "heun", "ssprk3", "tsit5"])
+@pytest.mark.parametrize("bc", ["periodic", "wall"])
+@pytest.mark.parametrize("case", range(len(CASES)))
+def test_cluster_engine_matches_stages(case, bc, scheme):
+    """The cluster engine (every step in one thread-block cluster, halo rows from the
+    neighbouring CTAs' shared memory) against one launch per stage: the same arithmetic per
+    cell, so within 1e-6 after 13 steps (one call of 8 + 5, then one more call)."""
+    n, H, gp = CASES[case]
+    ms, o = pair(n, H, gp, bc, engine="stages")
+    mc, _ = pair(n, H, gp, bc, engine="cluster")
+    y = state(o, 40 + case)
+    dt = 0.1 * min(o.dx, o.dy) / np.sqrt(9.81 * sum(H))
+    a = ms.step(ms.step(gpu_state(ms, y), dt, 13, scheme), dt, 1, scheme, apply_bc=False)
+    b = mc.step(mc.step(gpu_state(mc, y), dt, 13, scheme), dt, 1, scheme, apply_bc=False)
+    assert ms.status() == 0 and mc.status() == 0
+    for x, z in ((a.h, b.h), (a.u, b.u), (a.v, b.v)):
+        r = float((x - z).norm() / max(float(x.norm()), 1e-30))
+        assert r < 1e-6, r
+
+
+def test_engine_choice_and_nonfinite_flag():
+    """AUTO takes the engine that ran the tuning steps faster; the reference's swm_jet basin
+    (2 layers, 64^2) fits a cluster; a 3-layer 512^2 basin does not and steps one launch per
+    stage (forcing the cluster engine there is an error); a NaN planted in the state raises
+    the non-finite flag through the cluster engine."""
+    jet0, s0 = sg.baroclinic_instability_swm(nx=64, ny=64, lateral_viscosity=1000.0)
+    eng = jet0.plan().engine("tsit5")
+    tm = eng["tuning_ms"]
+    assert tm["cluster"] > 0 and tm["stages"] > 0, eng
+    assert eng["engine"] == ("cluster" if tm["cluster"] < tm["stages"] else "stages"), eng
+    print(f"swm_jet64 engine tuning, 32 Tsit5 steps: {eng}")
+    jet = sg.MultilayerShallowWater2D.create(nx=64, ny=64, Lx=1e6, Ly=1e6, f0=1e-4, beta=1.6e-11, n_layers=2,
+                                             H=(500.0, 4500.0), g_prime=(9.81, 0.025), lateral_viscosity=1000.0,
+                                             bottom_drag=1e-7, engine="cluster")
+    assert jet.plan().engine("tsit5")["cluster_ctas"] in (16, 8, 4, 2)
+    big = sg.MultilayerShallowWater2D.create(nx=512, ny=512, n_layers=3)
+    assert big.plan().engine("tsit5")["engine"] == "stages"
+    forced = sg.MultilayerShallowWater2D.create(nx=512, ny=512, n_layers=3, engine="cluster")
+    z = torch.zeros((3,) + forced.shape, device="cuda")
+    with pytest.raises(RuntimeError):
+        forced.step(sg.MultilayerSW2DState(z[0] + 500.0, z[1], z[2]), 1.0, 1, "tsit5")
+    bad = sg.MultilayerSW2DState(s0.h.clone(), s0.u.clone(), s0.v.clone())
+    bad.u[1, 30, 30] = float("nan")
+    jet.step(bad, 20.0, 3, "tsit5")
+    assert jet.status() == _lib.K["QG_ERR_NONFINITE"]
+    assert jet.status() == 0
