@@ -359,6 +359,10 @@ int qg_swm_engine(qg_swm_plan* plan, int scheme, int* cluster_ctas, float* times
    grid and layers (QG_ERR_SHAPE).  Launched directly (no graph). */
 int qg_reparam_step(qg_swm_plan* plan, qg_plan* qgplan, float* state, const float* params, double dt,
                     int n_steps, int scheme, int flags, void* stream);
+/* The runner's state statistics (cli/_run.py:408-432) of n floats at x (one field of a state,
+   or several): stats[0..3] = min, mean, max over the finite entries and the count of
+   non-finite entries, as device doubles. */
+int qg_swm_state_stats(qg_swm_plan* plan, const float* x, int64_t n, double* stats, void* stream);
 /* QG_OK or QG_ERR_NONFINITE (a tendency was not finite since the last call); clears the flag. */
 int qg_swm_status(qg_swm_plan* plan, int* flags, void* stream);
 

@@ -586,6 +586,7 @@ struct qg_swm_plan {
     float* K = nullptr;       // kMaxButcher stage derivatives
     float* params = nullptr;  // plan-owned copy of the params (graph-stable)
     float* proj = nullptr;    // projected stage input of qg_reparam_step
+    void* stats_acc = nullptr;  // qg_swm_state_stats accumulators
     int* flags = nullptr;
     int64_t n = 0;            // floats of one state
     int device = 0;
@@ -685,6 +686,7 @@ extern "C" int qg_swm_create(const qg_swm_desc* desc, qg_swm_plan** out) {
     if (!e) e = cudaMalloc(&p->params, 4 * sizeof(float));
     if (!e) e = cudaMemset(p->params, 0, 4 * sizeof(float));
     if (!e) e = cudaMalloc(&p->proj, p->n * sizeof(float));
+    if (!e) e = cudaMalloc(&p->stats_acc, 64);
     if (!e) e = cudaMalloc(&p->flags, 16);
     if (!e) e = cudaMemset(p->flags, 0, 16);
     if (!e) e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);
@@ -711,7 +713,7 @@ extern "C" void qg_swm_destroy(qg_swm_plan* p) {
         }
     if (p->cap) cudaStreamDestroy(p->cap);
     for (void* a : {(void*)p->consts, (void*)p->stage, (void*)p->K, (void*)p->params, (void*)p->proj,
-                    (void*)p->flags})
+                    p->stats_acc, (void*)p->flags})
         if (a) cudaFree(a);
     delete p;
 }
@@ -1096,6 +1098,16 @@ extern "C" int qg_reparam_step(qg_swm_plan* p, qg_plan* qp, float* state, const 
         if (cudaGetLastError() != cudaSuccess) return QG_ERR_CUDA;
     }
     return r;
+}
+
+extern "C" int qg_swm_state_stats(qg_swm_plan* p, const float* x, int64_t n, double* stats, void* stream) {
+    if (!p || !x || !stats) return QG_ERR_NULL;
+    if (n < 1) return QG_ERR_ARG;
+    int dev = 0, n_sm = 0;
+    if (cudaGetDevice(&dev) || cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev)) return QG_ERR_CUDA;
+    const int grid = std::max(1, std::min(n_sm * 4, (int)((n / 4 + 255) / 256)));
+    return launch_state_stats(x, n, p->stats_acc, stats, grid, (cudaStream_t)stream) == cudaSuccess ? QG_OK
+                                                                                                   : QG_ERR_CUDA;
 }
 
 extern "C" int qg_swm_status(qg_swm_plan* p, int* flags, void* stream) {

@@ -53,6 +53,8 @@ class ReparameterizedQG:
     """``ReparameterizedQG`` (``reparameterized.py:65-315``): multilayer SWM + the geostrophic
     projection."""
 
+    state_cls = MultilayerSW2DState
+
     def __init__(self, swm, spec: MemberSpec, strat: StratificationProfile, modal: ModalTransform,
                  precision="fp32", refine=0):
         self.swm = swm

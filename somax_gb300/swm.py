@@ -140,6 +140,17 @@ class SwmPlan:
         flags = C.c_int(0)
         return self._L.qg_swm_status(self._h, C.byref(flags), _stream_handle(self.device))
 
+    def field_stats(self, x: torch.Tensor) -> torch.Tensor:
+        """(min, mean, max) over the finite entries of the float32 CUDA tensor x and the count of
+        its non-finite entries, as a float64 device tensor of 4 values (``qg_swm_state_stats``)."""
+        if not isinstance(x, torch.Tensor) or x.device.type != "cuda" or x.dtype != torch.float32:
+            raise TypeError("x must be a float32 CUDA tensor")
+        x = x.contiguous()
+        out = torch.empty(4, device=x.device, dtype=torch.float64)
+        check(self._L.qg_swm_state_stats(self._h, C.c_void_p(x.data_ptr()), int(x.numel()),
+                                         C.c_void_p(out.data_ptr()), _stream_handle(x.device)), "qg_swm_state_stats")
+        return out
+
     def set_engine(self, engine: str):
         """``"auto"`` (the cluster engine where the basin fits), ``"stages"`` (one launch per
         stage) or ``"cluster"`` (every step of a call in one thread-block cluster)."""
