@@ -273,14 +273,29 @@ __device__ __forceinline__ void stage_tile(StageTables& t, const SwmDev& d, cons
     const Tab tb{t.h, kStE, kStX};
     bool bad = false;
     float po = 0.f, ph = 0.f;  // cumulative pressure at the own and the halo cell
+    // without stage derivatives to combine, the next layer's loads are issued before this layer's
+    // arithmetic, so that their latency overlaps it
+    constexpr bool kPrefetch = NS == 0;
+    float vo[3][NS + 1], vh[3][NS + 1];
+    if (kPrefetch) {
+        if (mine) load_point<NS, INT>(d, a, field, 0, j, i, vo);
+        if (halo) load_point<NS, INT>(d, a, field, 0, j0 + hr, i0 + hc, vh);
+    }
     for (int k = 0; k < d.nl; ++k) {
         const int64_t lo = k * plane;
-        float vo[3][NS + 1], vh[3][NS + 1], yo3[3], yh3[3];
-        if (mine) load_point<NS, INT>(d, a, field, lo, j, i, vo);
-        if (halo) load_point<NS, INT>(d, a, field, lo, j0 + hr, i0 + hc, vh);
+        float yo3[3], yh3[3];
+        if (!kPrefetch) {
+            if (mine) load_point<NS, INT>(d, a, field, lo, j, i, vo);
+            if (halo) load_point<NS, INT>(d, a, field, lo, j0 + hr, i0 + hc, vh);
+        }
         if (mine) store_input<NS>(t, a, eo, vo, yo3);
         if (halo) store_input<NS>(t, a, he, vh, yh3);
         __syncthreads();
+        float vn[3][NS + 1], vhn[3][NS + 1];
+        if (kPrefetch && k + 1 < d.nl) {
+            if (mine) load_point<NS, INT>(d, a, field, lo + plane, j, i, vn);
+            if (halo) load_point<NS, INT>(d, a, field, lo + plane, j0 + hr, i0 + hc, vhn);
+        }
         const float g = __ldg(d.gp + k);
         float qo = 0.f, uho = 0.f, vho = 0.f, keo = 0.f, x0, x1, x2, x3;
         if (mine) swm_derive<INT>(tb, d, g, eo, threadIdx.y + 1, threadIdx.x + 1, kStY, j, i, qo, uho, vho, keo, po);
@@ -288,8 +303,8 @@ __device__ __forceinline__ void stage_tile(StageTables& t, const SwmDev& d, cons
         __syncthreads();
         if (mine) {
             float dh, du, dv;
-            swm_tend(tb, d, eo, j, in, k == 0, k == d.nl - 1, nu, kappa, tau0, yo3[0], yo3[1], yo3[2], qo, uho, vho,
-                     keo, po, dh, du, dv);
+            swm_tend(tb, d, eo, j, in, k == 0, k == d.nl - 1, nu, kappa, tau0, t.h[eo], t.u[eo], t.v[eo], t.q[eo],
+                     t.uh[eo], t.vh[eo], t.ke[eo], t.p[eo], dh, du, dv);
             bad |= !isfinite(dh) || !isfinite(du) || !isfinite(dv);
             const int64_t o = lo + (int64_t)j * d.Nx + i;
             const float F[3] = {dh, du, dv};
@@ -316,6 +331,15 @@ __device__ __forceinline__ void stage_tile(StageTables& t, const SwmDev& d, cons
             }
         }
         __syncthreads();
+        if (kPrefetch && k + 1 < d.nl) {
+#pragma unroll
+            for (int f = 0; f < 3; ++f)
+#pragma unroll
+                for (int m = 0; m <= NS; ++m) {
+                    vo[f][m] = vn[f][m];
+                    vh[f][m] = vhn[f][m];
+                }
+        }
     }
     if (bad && a.flags) atomicOr(a.flags, 1);
 }
