@@ -199,3 +199,32 @@ def test_engine_choice_and_nonfinite_flag():
     jet.step(bad, 20.0, 3, "tsit5")
     assert jet.status() == _lib.K["QG_ERR_NONFINITE"]
     assert jet.status() == 0
+
+
+def test_field_stats_and_profiling_counters():
+    """qg_swm_state_stats against a float64 host reduction with NaN / inf planted, and the
+    per-launch profiling counters of qg_swm_step: one k_swm_stage launch per stage on the stage
+    engine, one k_swm_cluster launch per call on the cluster engine."""
+    n, H, gp = CASES[1]
+    m, o = pair(n, H, gp, "wall", engine="stages")
+    pl = m.plan()
+    x = torch.tensor(state(o, 50)[1], dtype=torch.float32, device="cuda").reshape(-1)
+    x[3] = float("nan")
+    x[40] = float("inf")
+    got = pl.field_stats(x).cpu().numpy()
+    h = x.cpu().double().numpy()
+    f = h[np.isfinite(h)]
+    assert got[0] == f.min() and got[2] == f.max() and got[3] == 2
+    assert abs(got[1] - f.mean()) <= 1e-12 * np.abs(f).max()
+    y = torch.tensor(state(o, 51), dtype=torch.float32, device="cuda").reshape(-1)
+    pv = m._param_vector(y.device)
+    for engine, want in (("stages", {0: 3 * 6, 2: 0}), ("cluster", {0: 0, 2: 1})):
+        pl.set_engine(engine)
+        pl.set_profiling(True)
+        pl.step(y, pv, 5.0, 3, "tsit5", True)
+        torch.cuda.synchronize()
+        for k, launches in want.items():
+            ms, cnt = pl.kernel_stats(_lib.K["QG_SWM_K_STAGE"] if k == 0 else _lib.K["QG_SWM_K_CLUSTER"])
+            assert cnt == launches and (ms > 0) == (launches > 0), (engine, k, cnt, ms)
+        pl.set_profiling(False)
+    assert pl.status() == 0
