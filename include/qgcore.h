@@ -359,6 +359,22 @@ int qg_swm_engine(qg_swm_plan* plan, int scheme, int* cluster_ctas, float* times
    grid and layers (QG_ERR_SHAPE).  Launched directly (no graph). */
 int qg_reparam_step(qg_swm_plan* plan, qg_plan* qgplan, float* state, const float* params, double dt,
                     int n_steps, int scheme, int flags, void* stream);
+/* Reverse mode of the shallow-water model (what the reference takes with JAX autodiff through
+   vector_field and integrate: tests/models/test_swm_multilayer.py:239-252).
+   qg_swm_rhs_vjp: state_bar = J^T tend_bar for tend = vector_field(state) (with
+   QG_RHS_APPLY_BC: of the boundary rules applied on read, so state_bar is the cotangent of
+   the raw state), params_bar[0..2] = the cotangents of nu, kappa, tau0 (overwritten).  The
+   upwind switch is differentiated as a fixed choice of upwind cell.
+   qg_swm_bc_vjp: the transpose of apply_boundary_conditions on a cotangent, in place.
+   qg_swm_step_vjp: the adjoint of one qg_swm_step step from y0: y_bar holds the cotangent of
+   the step's result on entry and that of y0 on return; params_bar receives the parameter
+   cotangents (overwritten); work holds qg_swm_step_vjp_workspace(plan, scheme) floats. */
+int qg_swm_rhs_vjp(qg_swm_plan* plan, const float* state, const float* params, const float* tend_bar,
+                   float* state_bar, float* params_bar, int flags, void* stream);
+int qg_swm_bc_vjp(qg_swm_plan* plan, float* state_bar, void* stream);
+int64_t qg_swm_step_vjp_workspace(const qg_swm_plan* plan, int scheme);
+int qg_swm_step_vjp(qg_swm_plan* plan, const float* y0, const float* params, double dt, int scheme, float* y_bar,
+                    float* params_bar, float* work, void* stream);
 /* The runner's state statistics (cli/_run.py:408-432) of n floats at x (one field of a state,
    or several): stats[0..3] = min, mean, max over the finite entries and the count of
    non-finite entries, as device doubles. */

@@ -278,3 +278,75 @@ def diagnose(m: SWModel, h, u, v) -> dict:
     ens = 0.5 * np.sum(q[S] ** 2 * hX[S], axis=(-2, -1)) * area
     return dict(energy=energy, total_energy=energy.sum(), enstrophy=ens, total_enstrophy=ens.sum(),
                 potential_vorticity=q, relative_vorticity=zeta, kinetic_energy_field=ke)
+
+
+# ---- float64 derivatives (the checker of the hand-written shallow-water adjoint) -------------
+SWM_PARAMS = ("lateral_viscosity", "bottom_drag", "wind_amplitude")
+
+
+def _rhs_flat(m: SWModel, y: np.ndarray, params: dict | None, apply_bc: bool) -> np.ndarray:
+    if apply_bc:
+        return rhs(m, y, params).reshape(-1)
+    return np.stack(vector_field(m, y[0], y[1], y[2], params)).reshape(-1)
+
+
+def rhs_jacobian(m: SWModel, y: np.ndarray, params: dict | None = None, apply_bc: bool = True,
+                 rel: float = 1e-6) -> np.ndarray:
+    """Dense Jacobian of ``rhs`` (apply_bc: the boundary rules applied to y first) by central
+    differences with a step of ``rel`` times each field's largest magnitude.  The right-hand side
+    is smooth away from the upwind switch (u = 0 on a face), which the tests' states avoid; the
+    differences are then exact to O(step^2)."""
+    y = np.asarray(y, dtype=np.float64)
+    n = y.size
+    scale = [max(np.abs(y[f]).max(), 1e-3) * rel for f in range(3)]
+    per_field = n // 3
+    J = np.empty((n, n))
+    flat = y.reshape(-1)
+    for c in range(n):
+        h = scale[c // per_field]
+        yp = flat.copy()
+        ym = flat.copy()
+        yp[c] += h
+        ym[c] -= h
+        J[:, c] = (_rhs_flat(m, yp.reshape(y.shape), params, apply_bc) -
+                   _rhs_flat(m, ym.reshape(y.shape), params, apply_bc)) / (2.0 * h)
+    return J
+
+
+def rhs_param_derivatives(m: SWModel, y: np.ndarray, apply_bc: bool = True) -> np.ndarray:
+    """d rhs / d (nu, kappa, tau0), (3, n): the right-hand side is affine in each parameter, so
+    a forward difference of a unit step is exact up to rounding."""
+    base = {k: float(getattr(m, k)) for k in SWM_PARAMS}
+    f0 = _rhs_flat(m, y, base, apply_bc)
+    out = []
+    for k in SWM_PARAMS:
+        p = dict(base)
+        p[k] += 1.0
+        out.append(_rhs_flat(m, y, p, apply_bc) - f0)
+    return np.stack(out)
+
+
+def step_jacobian(m: SWModel, y: np.ndarray, dt: float, n_steps: int, scheme: str, rel: float = 1e-6) -> np.ndarray:
+    """Dense Jacobian of n_steps constant steps (no initial boundary rules: a step continues an
+    integration) by central differences, as ``rhs_jacobian``."""
+    y = np.asarray(y, dtype=np.float64)
+    n = y.size
+    scale = [max(np.abs(y[f]).max(), 1e-3) * rel for f in range(3)]
+    per_field = n // 3
+    flat = y.reshape(-1)
+
+    def run(z):
+        z = z.reshape(y.shape)
+        for _ in range(n_steps):
+            z = _qg.rk_step(lambda w: rhs(m, w), z, dt, scheme)
+        return z.reshape(-1)
+
+    J = np.empty((n, n))
+    for c in range(n):
+        h = scale[c // per_field]
+        yp = flat.copy()
+        ym = flat.copy()
+        yp[c] += h
+        ym[c] -= h
+        J[:, c] = (run(yp) - run(ym)) / (2.0 * h)
+    return J

@@ -563,6 +563,259 @@ __global__ void __launch_bounds__(kScThreads) k_swm_cluster(SwmClusterArgs a) {
     sc_sync();  // no CTA leaves while another may still read its stage input
 }
 
+// ---- adjoint of the right-hand side --------------------------------------------------------
+//
+// The transpose of vector_field's Jacobian at a stage input Y, applied to a cotangent
+// gbar = (dh_bar, du_bar, dv_bar), as gathers in two passes:
+//  k_swm_vjp_mid  the cotangents of the intermediate quantities at every point: PV at the X
+//                 points (q_bar), the face mass fluxes of the PV flux (vh_bar at V points,
+//                 uh_bar at U points), the Bernoulli potential at T points (P_bar = ke_bar, and
+//                 the pressure sum's), and the upwind mass fluxes (Fx_bar on east faces, Fy_bar
+//                 on north faces), each gathered from the tendencies that read it;
+//  k_swm_vjp_in   the cotangent of the stage input (after the boundary rules) at every point,
+//                 gathered from those and the direct terms (Laplacians, drag); the pressure sum
+//                 sum_{l<=k} g'_l h_l becomes a reverse cumulative sum over the layers; and the
+//                 parameter cotangents (nu, kappa, tau0) summed over the grid;
+//  k_swm_bc_vjp   the transpose of the boundary rules: every ring or wall-face value that
+//                 copied a source cell passes its cotangent on to it (zeroed values drop theirs).
+// The upwind switch and the PV division are differentiated where they are smooth (the switch
+// as a constant choice of upwind cell).
+
+// Forward values of the right-hand side at any point of layer k of the stage input y, with
+// the boundary rules on read when bc (the same expressions as the stage kernel's).
+struct SwmAt {
+    const SwmDev& d;
+    const float* y;
+    int64_t plane, field;
+    bool bc;
+    __device__ __forceinline__ bool inside(int a, int b) const {
+        return a >= 1 && a <= d.Ny - 2 && b >= 1 && b <= d.Nx - 2;
+    }
+    __device__ __forceinline__ float H(int k, int a, int b) const { return ld(y + k * plane, d, 0, a, b, bc); }
+    __device__ __forceinline__ float U(int k, int a, int b) const { return ld(y + field + k * plane, d, 1, a, b, bc); }
+    __device__ __forceinline__ float V(int k, int a, int b) const {
+        return ld(y + 2 * field + k * plane, d, 2, a, b, bc);
+    }
+    __device__ __forceinline__ float hX(int k, int a, int b) const {
+        return 0.25f * (H(k, a, b) + H(k, a, b + 1) + H(k, a + 1, b) + H(k, a + 1, b + 1));
+    }
+    __device__ __forceinline__ float qX(int k, int a, int b) const {
+        if (!inside(a, b)) return 0.f;
+        const float zeta = (V(k, a, b + 1) - V(k, a, b)) * d.idx - (U(k, a + 1, b) - U(k, a, b)) * d.idy;
+        return (zeta + __ldg(d.fx + a)) / hX(k, a, b);
+    }
+    __device__ __forceinline__ float uh(int k, int a, int b) const {
+        return inside(a, b) ? 0.5f * (H(k, a, b) + H(k, a, b + 1)) * U(k, a, b) : 0.f;
+    }
+    __device__ __forceinline__ float vh(int k, int a, int b) const {
+        return inside(a, b) ? 0.5f * (H(k, a, b) + H(k, a + 1, b)) * V(k, a, b) : 0.f;
+    }
+    // at an interior output cell (j, i)
+    __device__ __forceinline__ float qU(int k, int j, int i) const { return 0.5f * (qX(k, j, i) + qX(k, j - 1, i)); }
+    __device__ __forceinline__ float qV(int k, int j, int i) const { return 0.5f * (qX(k, j, i) + qX(k, j, i - 1)); }
+    __device__ __forceinline__ float vhU(int k, int j, int i) const {
+        return 0.25f * (vh(k, j, i) + vh(k, j, i + 1) + vh(k, j - 1, i) + vh(k, j - 1, i + 1));
+    }
+    __device__ __forceinline__ float uhV(int k, int j, int i) const {
+        return 0.25f * (uh(k, j, i) + uh(k, j, i - 1) + uh(k, j + 1, i) + uh(k, j + 1, i - 1));
+    }
+};
+
+// Mid-point cotangents: six planes per layer in `mid` ([k][0..5][Ny][Nx]: q_bar, vh_bar,
+// uh_bar, P_bar, Fx_bar, Fy_bar).
+__global__ void __launch_bounds__(kSwTX * kSwTY) k_swm_vjp_mid(SwmDev d, const float* __restrict__ y,
+                                                                const float* __restrict__ gbar, float* __restrict__ mid,
+                                                                int bc) {
+    const int b = blockIdx.x * kSwTX + threadIdx.x;
+    const int a = blockIdx.y * kSwTY + threadIdx.y;
+    if (b >= d.Nx || a >= d.Ny) return;
+    const int64_t plane = (int64_t)d.Ny * d.Nx, field = plane * d.nl;
+    const SwmAt F{d, y, plane, field, bc != 0};
+    const int64_t o = (int64_t)a * d.Nx + b;
+    for (int k = 0; k < d.nl; ++k) {
+        const float* gh = gbar + k * plane;
+        const float* gu = gbar + field + k * plane;
+        const float* gv = gbar + 2 * field + k * plane;
+        auto G = [&](const float* g, int j, int i) { return g[(int64_t)j * d.Nx + i]; };
+        float qb = 0.f, vhb = 0.f, uhb = 0.f;
+        if (F.inside(a, b)) {
+            // q(a, b) feeds qU of U(a, b), U(a + 1, b) and qV of V(a, b), V(a, b + 1)
+            qb += 0.5f * (G(gu, a, b) * F.vhU(k, a, b) - G(gv, a, b) * F.uhV(k, a, b));
+            if (F.inside(a + 1, b)) qb += 0.5f * G(gu, a + 1, b) * F.vhU(k, a + 1, b);
+            if (F.inside(a, b + 1)) qb -= 0.5f * G(gv, a, b + 1) * F.uhV(k, a, b + 1);
+            // vh(a, b) feeds vhU of U(a, b), U(a, b - 1), U(a + 1, b), U(a + 1, b - 1)
+            const int uj[4] = {a, a, a + 1, a + 1}, ui[4] = {b, b - 1, b, b - 1};
+#pragma unroll
+            for (int t = 0; t < 4; ++t)
+                if (F.inside(uj[t], ui[t])) vhb += 0.25f * G(gu, uj[t], ui[t]) * F.qU(k, uj[t], ui[t]);
+            // uh(a, b) feeds uhV of V(a, b), V(a, b + 1), V(a - 1, b), V(a - 1, b + 1)
+            const int vj[4] = {a, a, a - 1, a - 1}, vi[4] = {b, b + 1, b, b + 1};
+#pragma unroll
+            for (int t = 0; t < 4; ++t)
+                if (F.inside(vj[t], vi[t])) uhb -= 0.25f * G(gv, vj[t], vi[t]) * F.qV(k, vj[t], vi[t]);
+        }
+        // P(a, b): Pc of U(a, b) and V(a, b), Pe of U(a, b - 1), Pn of V(a - 1, b)
+        float Pb = 0.f;
+        if (F.inside(a, b)) Pb += G(gu, a, b) * d.idx + G(gv, a, b) * d.idy;
+        if (F.inside(a, b - 1)) Pb -= G(gu, a, b - 1) * d.idx;
+        if (F.inside(a - 1, b)) Pb -= G(gv, a - 1, b) * d.idy;
+        // the upwind mass flux through the east face of (a, b) (fe of (a, b), fw of (a, b + 1))
+        // and through its north face (gn of (a, b), gs of (a + 1, b))
+        float Fx = 0.f, Fy = 0.f;
+        if (F.inside(a, b)) {
+            Fx -= G(gh, a, b) * d.idx;
+            Fy -= G(gh, a, b) * d.idy;
+        }
+        if (F.inside(a, b + 1)) Fx += G(gh, a, b + 1) * d.idx;
+        if (F.inside(a + 1, b)) Fy += G(gh, a + 1, b) * d.idy;
+        float* m = mid + (int64_t)k * 6 * plane + o;
+        m[0] = qb;
+        m[plane] = vhb;
+        m[2 * plane] = uhb;
+        m[3 * plane] = Pb;
+        m[4 * plane] = Fx;
+        m[5 * plane] = Fy;
+    }
+}
+
+// The stage-input cotangent at (a, b) of every layer and the parameter cotangents
+// (accumulated in pacc[0..2] as doubles: nu, kappa, tau0).
+__global__ void __launch_bounds__(kSwTX * kSwTY) k_swm_vjp_in(SwmDev d, const float* __restrict__ y,
+                                                               const float* __restrict__ gbar,
+                                                               const float* __restrict__ mid,
+                                                               const float* __restrict__ params, float* ybar,
+                                                               double* pacc, int bc) {
+    const int b = blockIdx.x * kSwTX + threadIdx.x;
+    const int a = blockIdx.y * kSwTY + threadIdx.y;
+    const bool mine = b < d.Nx && a < d.Ny;
+    const int64_t plane = (int64_t)d.Ny * d.Nx, field = plane * d.nl;
+    const float nu = params[0], kappa = params[1];
+    float pnu = 0.f, pkap = 0.f, ptau = 0.f;
+    if (mine) {
+        const SwmAt F{d, y, plane, field, bc != 0};
+        const int64_t o = (int64_t)a * d.Nx + b;
+        auto M = [&](int k, int c, int j, int i) { return mid[((int64_t)k * 6 + c) * plane + (int64_t)j * d.Nx + i]; };
+        float pcum = 0.f;  // sum over the layers k >= l of P_bar_k(a, b)
+        for (int k = d.nl - 1; k >= 0; --k) {
+            const float* gu = gbar + field + k * plane;
+            const float* gv = gbar + 2 * field + k * plane;
+            auto G = [&](const float* g, int j, int i) { return F.inside(j, i) ? g[(int64_t)j * d.Nx + i] : 0.f; };
+            const float h0 = F.H(k, a, b), u0 = F.U(k, a, b), v0 = F.V(k, a, b);
+            const bool east = b + 1 < d.Nx, west = b >= 1, north = a + 1 < d.Ny, south = a >= 1;
+            pcum += M(k, 3, a, b);
+            float hb = 0.f;  // the pressure sum's share g'_k sum_{k' >= k} P_bar_k' is added last
+            // upwind mass fluxes: face (a, b) takes h(a, b) when u(a, b) > 0, face (a, b - 1) takes
+            // h(a, b) when u(a, b - 1) <= 0 (the same in y)
+            float ub = 0.f, vb = 0.f;
+            if (east) {
+                const float fx = M(k, 4, a, b);
+                if (u0 > 0.f) hb += fx * u0;
+                ub += fx * (u0 > 0.f ? h0 : F.H(k, a, b + 1));
+            }
+            if (west) {
+                const float uw = F.U(k, a, b - 1);
+                if (!(uw > 0.f)) hb += M(k, 4, a, b - 1) * uw;
+            }
+            if (north) {
+                const float fy = M(k, 5, a, b);
+                if (v0 > 0.f) hb += fy * v0;
+                vb += fy * (v0 > 0.f ? h0 : F.H(k, a + 1, b));
+            }
+            if (south) {
+                const float vs = F.V(k, a - 1, b);
+                if (!(vs > 0.f)) hb += M(k, 5, a - 1, b) * vs;
+            }
+            // PV: q = (zeta + f) / hX at the X points (a, b), (a, b - 1), (a - 1, b), (a - 1, b - 1)
+            auto zb = [&](int j, int i) {  // zeta_bar = q_bar / hX
+                return F.inside(j, i) ? M(k, 0, j, i) / F.hX(k, j, i) : 0.f;
+            };
+            const int xj[4] = {a, a, a - 1, a - 1}, xi[4] = {b, b - 1, b, b - 1};
+#pragma unroll
+            for (int t = 0; t < 4; ++t)
+                if (F.inside(xj[t], xi[t])) hb -= 0.25f * M(k, 0, xj[t], xi[t]) * F.qX(k, xj[t], xi[t]) / F.hX(k, xj[t], xi[t]);
+            ub += (zb(a, b) - (south ? zb(a - 1, b) : 0.f)) * d.idy;
+            vb += ((west ? zb(a, b - 1) : 0.f) - zb(a, b)) * d.idx;
+            // face mass fluxes of the PV flux: vh(a, b), vh(a - 1, b), uh(a, b), uh(a, b - 1)
+            hb += 0.5f * (M(k, 1, a, b) * v0 + (south ? M(k, 1, a - 1, b) * F.V(k, a - 1, b) : 0.f));
+            hb += 0.5f * (M(k, 2, a, b) * u0 + (west ? M(k, 2, a, b - 1) * F.U(k, a, b - 1) : 0.f));
+            if (north) vb += M(k, 1, a, b) * 0.5f * (h0 + F.H(k, a + 1, b));
+            if (east) ub += M(k, 2, a, b) * 0.5f * (h0 + F.H(k, a, b + 1));
+            // kinetic energy (interior T points): ke(a, b) and ke(a, b + 1) read u(a, b),
+            // ke(a, b) and ke(a + 1, b) read v(a, b)
+            const float pab = F.inside(a, b) ? M(k, 3, a, b) : 0.f;
+            ub += 0.5f * u0 * (pab + (east && F.inside(a, b + 1) ? M(k, 3, a, b + 1) : 0.f));
+            vb += 0.5f * v0 * (pab + (north && F.inside(a + 1, b) ? M(k, 3, a + 1, b) : 0.f));
+            // Laplacians of the interior outputs (their transpose), and nu's cotangent
+            const float gc = G(gu, a, b), gvc = G(gv, a, b);
+            ub += nu * (((west ? G(gu, a, b - 1) : 0.f) + (east ? G(gu, a, b + 1) : 0.f) - 2.f * gc) * d.idx2 +
+                        ((south ? G(gu, a - 1, b) : 0.f) + (north ? G(gu, a + 1, b) : 0.f) - 2.f * gc) * d.idy2);
+            vb += nu * (((west ? G(gv, a, b - 1) : 0.f) + (east ? G(gv, a, b + 1) : 0.f) - 2.f * gvc) * d.idx2 +
+                        ((south ? G(gv, a - 1, b) : 0.f) + (north ? G(gv, a + 1, b) : 0.f) - 2.f * gvc) * d.idy2);
+            if (F.inside(a, b)) {
+                const float lu = (F.U(k, a, b + 1) - 2.f * u0 + F.U(k, a, b - 1)) * d.idx2 +
+                                 (F.U(k, a + 1, b) - 2.f * u0 + F.U(k, a - 1, b)) * d.idy2;
+                const float lv = (F.V(k, a, b + 1) - 2.f * v0 + F.V(k, a, b - 1)) * d.idx2 +
+                                 (F.V(k, a + 1, b) - 2.f * v0 + F.V(k, a - 1, b)) * d.idy2;
+                pnu += gc * lu + gvc * lv;
+            }
+            // drag (bottom layer, every cell) and wind (top layer, every cell)
+            const float guo = gu[o], gvo = gv[o];
+            if (k == d.nl - 1) {
+                ub -= kappa * guo;
+                vb -= kappa * gvo;
+                pkap -= guo * u0 + gvo * v0;
+            }
+            if (k == 0) ptau += guo * __ldg(d.wx + a) * d.invH0;
+            hb += __ldg(d.gp + k) * pcum;
+            ybar[k * plane + o] = hb;
+            ybar[field + k * plane + o] = ub;
+            ybar[2 * field + k * plane + o] = vb;
+        }
+    }
+    // parameter cotangents: warp sums, one double atomic per warp
+    for (int sh = 16; sh > 0; sh >>= 1) {
+        pnu += __shfl_down_sync(0xffffffffu, pnu, sh);
+        pkap += __shfl_down_sync(0xffffffffu, pkap, sh);
+        ptau += __shfl_down_sync(0xffffffffu, ptau, sh);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(pacc + 0, (double)pnu);
+        atomicAdd(pacc + 1, (double)pkap);
+        atomicAdd(pacc + 2, (double)ptau);
+    }
+}
+
+// The transpose of the boundary rules on a cotangent, in place: each value the rules take
+// from another cell passes its cotangent on to that cell; values they set to zero drop it.
+__global__ void k_swm_bc_vjp(SwmDev d, float* ybar) {
+    const int i = blockIdx.x * kSwTX + threadIdx.x;
+    const int j = blockIdx.y * kSwTY + threadIdx.y;
+    if (i >= d.Nx || j >= d.Ny) return;
+    const int64_t plane = (int64_t)d.Ny * d.Nx, field = plane * d.nl;
+    for (int f = 0; f < 3; ++f) {
+        int jj = j, ii = i;
+        const bool keep = src_cell(d, f, jj, ii);
+        if (keep && jj == j && ii == i) continue;
+        for (int k = 0; k < d.nl; ++k) {
+            float* g = ybar + f * field + k * plane;
+            const float v = g[(int64_t)j * d.Nx + i];
+            g[(int64_t)j * d.Nx + i] = 0.f;
+            if (keep && v != 0.f) atomicAdd(g + (int64_t)jj * d.Nx + ii, v);
+        }
+    }
+}
+
+// y += alpha x, and y = alpha x, over n floats
+__global__ void k_swm_axpy(float* y, const float* __restrict__ x, float alpha, int64_t n, int overwrite) {
+    const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += nth)
+        y[t] = overwrite ? alpha * x[t] : fmaf(alpha, x[t], y[t]);
+}
+
+__global__ void k_swm_pbar(const double* pacc, float* pbar, int accumulate) {
+    if (threadIdx.x < QG_SWM_NPARAMS) pbar[threadIdx.x] = (float)pacc[threadIdx.x] + (accumulate ? pbar[threadIdx.x] : 0.f);
+}
+
 struct Combine {
     float c[kMaxButcher];
 };
@@ -611,6 +864,8 @@ struct qg_swm_plan {
     float* params = nullptr;  // plan-owned copy of the params (graph-stable)
     float* proj = nullptr;    // projected stage input of qg_reparam_step
     void* stats_acc = nullptr;  // qg_swm_state_stats accumulators
+    float* mid = nullptr;       // the VJP's mid-point cotangents (6 planes per layer)
+    double* pacc = nullptr;     // the VJP's parameter cotangent sums
     int* flags = nullptr;
     int64_t n = 0;            // floats of one state
     int device = 0;
@@ -711,6 +966,8 @@ extern "C" int qg_swm_create(const qg_swm_desc* desc, qg_swm_plan** out) {
     if (!e) e = cudaMemset(p->params, 0, 4 * sizeof(float));
     if (!e) e = cudaMalloc(&p->proj, p->n * sizeof(float));
     if (!e) e = cudaMalloc(&p->stats_acc, 64);
+    if (!e) e = cudaMalloc(&p->mid, (size_t)6 * d.nl * d.Ny * d.Nx * sizeof(float));
+    if (!e) e = cudaMalloc(&p->pacc, 4 * sizeof(double));
     if (!e) e = cudaMalloc(&p->flags, 16);
     if (!e) e = cudaMemset(p->flags, 0, 16);
     if (!e) e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);
@@ -737,7 +994,7 @@ extern "C" void qg_swm_destroy(qg_swm_plan* p) {
         }
     if (p->cap) cudaStreamDestroy(p->cap);
     for (void* a : {(void*)p->consts, (void*)p->stage, (void*)p->K, (void*)p->params, (void*)p->proj,
-                    p->stats_acc, (void*)p->flags})
+                    p->stats_acc, (void*)p->mid, (void*)p->pacc, (void*)p->flags})
         if (a) cudaFree(a);
     delete p;
 }
@@ -1122,6 +1379,96 @@ extern "C" int qg_reparam_step(qg_swm_plan* p, qg_plan* qp, float* state, const 
         if (cudaGetLastError() != cudaSuccess) return QG_ERR_CUDA;
     }
     return r;
+}
+
+namespace {
+// ybar = (the transpose of vector_field's Jacobian at y, with the boundary rules on read when bc)
+// applied to gbar; the parameter cotangents added to p->pacc.
+cudaError_t swm_vjp(qg_swm_plan* p, const float* y, const float* params, const float* gbar, float* ybar, int bc,
+                    cudaStream_t s) {
+    const dim3 g = swm_grid(p->d), b(kSwTX, kSwTY);
+    k_swm_vjp_mid<<<g, b, 0, s>>>(p->d, y, gbar, p->mid, bc);
+    k_swm_vjp_in<<<g, b, 0, s>>>(p->d, y, gbar, p->mid, params, ybar, p->pacc, bc);
+    if (bc) k_swm_bc_vjp<<<g, b, 0, s>>>(p->d, ybar);
+    return cudaGetLastError();
+}
+
+const Tableau* swm_scheme(int scheme) { return swm_tableau(scheme); }
+}  // namespace
+
+extern "C" int qg_swm_rhs_vjp(qg_swm_plan* p, const float* state, const float* params, const float* tend_bar,
+                              float* state_bar, float* params_bar, int flags, void* stream) {
+    if (!p || !state || !params || !tend_bar || !state_bar || !params_bar) return QG_ERR_NULL;
+    if (flags & ~QG_RHS_APPLY_BC) return QG_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = cudaMemsetAsync(p->pacc, 0, 4 * sizeof(double), s);
+    if (!e) e = swm_vjp(p, state, params, tend_bar, state_bar, flags & QG_RHS_APPLY_BC, s);
+    if (!e) {
+        k_swm_pbar<<<1, 32, 0, s>>>(p->pacc, params_bar, 0);
+        e = cudaGetLastError();
+    }
+    return e ? QG_ERR_CUDA : QG_OK;
+}
+
+extern "C" int qg_swm_bc_vjp(qg_swm_plan* p, float* state_bar, void* stream) {
+    if (!p || !state_bar) return QG_ERR_NULL;
+    k_swm_bc_vjp<<<swm_grid(p->d), dim3(kSwTX, kSwTY), 0, (cudaStream_t)stream>>>(p->d, state_bar);
+    return cudaGetLastError() == cudaSuccess ? QG_OK : QG_ERR_CUDA;
+}
+
+extern "C" int64_t qg_swm_step_vjp_workspace(const qg_swm_plan* p, int scheme) {
+    const Tableau* tb = swm_scheme(scheme);
+    if (!p || !tb) return -1;
+    return (int64_t)(3 * tb->n - 1) * p->n;
+}
+
+extern "C" int qg_swm_step_vjp(qg_swm_plan* p, const float* y0, const float* params, double dt, int scheme,
+                               float* y_bar, float* params_bar, float* work, void* stream) {
+    if (!p || !y0 || !params || !y_bar || !params_bar || !work) return QG_ERR_NULL;
+    const Tableau* tb = swm_scheme(scheme);
+    if (!tb || !(dt == dt)) return QG_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int ns = tb->n;
+    const int64_t n = p->n;
+    const int cgrid = (int)std::min<int64_t>(4096, (n + 255) / 256);
+    // work: stage inputs Y_1 .. Y_{ns-1}, stage derivatives K_0 .. K_{ns-2} (contiguous), their
+    // cotangents Kbar_0 .. Kbar_{ns-1}, one stage-input cotangent
+    const float* Y[kMaxButcher];
+    Y[0] = y0;
+    for (int i = 1; i < ns; ++i) Y[i] = work + (int64_t)(i - 1) * n;
+    float* K = work + (int64_t)(ns - 1) * n;
+    float* Kb = work + (int64_t)(2 * ns - 2) * n;
+    float* Yb = work + (int64_t)(3 * ns - 2) * n;
+    cudaError_t e = cudaSuccess;
+    // the step's stage inputs again: Y_s = y0 + dt sum_m a_sm K_m, K_m = F(B(Y_m))
+    for (int st = 0; st + 1 < ns && !e; ++st) {
+        e = launch_stage(p, stage_args(p, Y[st], K + st * n, params, 1), s);
+        if (e) break;
+        Combine c{};
+        for (int m = 0; m <= st; ++m) c.c[m] = (float)(dt * tb->a[st + 1][m]);
+        k_swm_combine<<<cgrid, 256, 0, s>>>(const_cast<float*>(Y[st + 1]), y0, K, n, st + 1, c);
+        e = cudaGetLastError();
+    }
+    // Kbar_s = dt b_s ybar, then the stages in reverse: Ybar = F_vjp(Y_s; Kbar_s),
+    // y0_bar += Ybar, Kbar_m += dt a_sm Ybar
+    for (int st = 0; st < ns && !e; ++st) {
+        k_swm_axpy<<<cgrid, 256, 0, s>>>(Kb + st * n, y_bar, (float)(dt * tb->b[st]), n, 1);
+        e = cudaGetLastError();
+    }
+    if (!e) e = cudaMemsetAsync(p->pacc, 0, 4 * sizeof(double), s);
+    for (int st = ns - 1; st >= 0 && !e; --st) {
+        e = swm_vjp(p, Y[st], params, Kb + st * n, Yb, 1, s);
+        if (e) break;
+        k_swm_axpy<<<cgrid, 256, 0, s>>>(y_bar, Yb, 1.f, n, 0);
+        for (int m = 0; m < st; ++m)
+            if (tb->a[st][m] != 0.0) k_swm_axpy<<<cgrid, 256, 0, s>>>(Kb + m * n, Yb, (float)(dt * tb->a[st][m]), n, 0);
+        e = cudaGetLastError();
+    }
+    if (!e) {
+        k_swm_pbar<<<1, 32, 0, s>>>(p->pacc, params_bar, 0);
+        e = cudaGetLastError();
+    }
+    return e ? QG_ERR_CUDA : QG_OK;
 }
 
 extern "C" int qg_swm_state_stats(qg_swm_plan* p, const float* x, int64_t n, double* stats, void* stream) {

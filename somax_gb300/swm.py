@@ -10,7 +10,9 @@ the same C-grid operators on the device (torch, not a hot path).
 
 The state is a ``MultilayerSW2DState`` (h, u, v, each (nl, Ny, Nx) with the ghost ring);
 the library sees it packed as one (3, nl, Ny, Nx) float32 array.  Only the first-order upwind
-mass flux (``method="upwind1"``, the reference's default) is implemented.
+mass flux (``method="upwind1"``, the reference's default) is implemented.  ``vector_field`` and
+``integrate`` are differentiable in the state and the parameters (``swm_adjoint``: the
+hand-written VJPs of the library, checkpointed recomputation through ``integrate``).
 """
 
 from __future__ import annotations
@@ -140,6 +142,44 @@ class SwmPlan:
         flags = C.c_int(0)
         return self._L.qg_swm_status(self._h, C.byref(flags), _stream_handle(self.device))
 
+    def rhs_vjp(self, y: torch.Tensor, params: torch.Tensor, tend_bar: torch.Tensor, apply_bc: bool):
+        """(state_bar, params_bar) = the VJP of ``rhs(y, params, apply_bc)`` for the cotangent
+        ``tend_bar`` (``qg_swm_rhs_vjp``)."""
+        self._check(y, "state")
+        self._check(tend_bar, "tend_bar")
+        out = torch.empty_like(y)
+        pb = torch.empty(3, dtype=torch.float32, device=y.device)
+        check(self._L.qg_swm_rhs_vjp(self._h, C.c_void_p(y.data_ptr()), C.c_void_p(params.data_ptr()),
+                                     C.c_void_p(tend_bar.data_ptr()), C.c_void_p(out.data_ptr()),
+                                     C.c_void_p(pb.data_ptr()), K["QG_RHS_APPLY_BC"] if apply_bc else 0,
+                                     _stream_handle(y.device)), "qg_swm_rhs_vjp")
+        return out, pb
+
+    def bc_vjp(self, y_bar: torch.Tensor) -> torch.Tensor:
+        """The transpose of ``apply_bc`` on a cotangent, in place (``qg_swm_bc_vjp``)."""
+        self._check(y_bar, "state_bar")
+        check(self._L.qg_swm_bc_vjp(self._h, C.c_void_p(y_bar.data_ptr()), _stream_handle(y_bar.device)),
+              "qg_swm_bc_vjp")
+        return y_bar
+
+    def step_vjp(self, y0: torch.Tensor, params: torch.Tensor, dt: float, scheme: str, g: torch.Tensor):
+        """(y0_bar, params_bar) of one step of ``scheme`` from ``y0`` for the cotangent ``g`` of its
+        result (``qg_swm_step_vjp``; the workspace is kept per scheme)."""
+        self._check(y0, "state")
+        self._check(g, "cotangent")
+        ws = getattr(self, "_vjp_work", {})
+        self._vjp_work = ws
+        need = int(self._L.qg_swm_step_vjp_workspace(self._h, _SCHEMES[scheme]))
+        if scheme not in ws or ws[scheme].numel() < need or ws[scheme].device != y0.device:
+            ws[scheme] = torch.empty(need, dtype=torch.float32, device=y0.device)
+        yb = g.clone()
+        pb = torch.empty(3, dtype=torch.float32, device=y0.device)
+        check(self._L.qg_swm_step_vjp(self._h, C.c_void_p(y0.data_ptr()), C.c_void_p(params.data_ptr()), float(dt),
+                                      _SCHEMES[scheme], C.c_void_p(yb.data_ptr()), C.c_void_p(pb.data_ptr()),
+                                      C.c_void_p(ws[scheme].data_ptr()), _stream_handle(y0.device)),
+              "qg_swm_step_vjp")
+        return yb, pb
+
     def field_stats(self, x: torch.Tensor) -> torch.Tensor:
         """(min, mean, max) over the finite entries of the float32 CUDA tensor x and the count of
         its non-finite entries, as a float64 device tensor of 4 values (``qg_swm_state_stats``)."""
@@ -260,6 +300,18 @@ class MultilayerShallowWater2D(SomaxModel):
         return torch.tensor([float(p.lateral_viscosity), float(p.bottom_drag), float(p.wind_amplitude)],
                             dtype=torch.float32, device=device)
 
+    def _param_tensor(self, device) -> torch.Tensor:
+        """(nu, kappa, tau0) as a float32 device tensor that keeps the parameters' autograd graph."""
+        p = self.params
+        vals = [v if isinstance(v, torch.Tensor) else torch.tensor(float(v))
+                for v in (p.lateral_viscosity, p.bottom_drag, p.wind_amplitude)]
+        return torch.stack([v.reshape(()).to(device=device, dtype=torch.float32) for v in vals])
+
+    def _grad(self, *ts) -> bool:
+        p = self.params
+        vals = list(ts) + [p.lateral_viscosity, p.bottom_drag, p.wind_amplitude]
+        return torch.is_grad_enabled() and any(isinstance(v, torch.Tensor) and v.requires_grad for v in vals)
+
     def pack(self, state) -> torch.Tensor:
         for name in ("h", "u", "v"):
             t = getattr(state, name)
@@ -277,6 +329,10 @@ class MultilayerShallowWater2D(SomaxModel):
         """Tendencies (dh, du, dv) of the state as given (multilayer.py:150-200)."""
         y = self.pack(state)
         plan = self.plan(y.device)
+        if self._grad(state.h, state.u, state.v):
+            from . import swm_adjoint
+
+            return self.unpack(swm_adjoint.rhs(plan, y.reshape(-1), self._param_tensor(y.device), apply_bc=False))
         return self.unpack(plan.rhs(y.reshape(-1), self._param_vector(y.device), apply_bc=False))
 
     def apply_boundary_conditions(self, state) -> MultilayerSW2DState:
@@ -303,6 +359,8 @@ class MultilayerShallowWater2D(SomaxModel):
         if abs(n_total * dt - (t1 - t0)) > 1e-9 * max(1.0, abs(t1 - t0)):
             raise ValueError("(t1 - t0) must be a whole number of steps")
         targets = [int(round((float(t) - t0) / dt)) for t in saveat.ts] if saveat.ts is not None else [n_total]
+        if self._grad(state0.h, state0.u, state0.v):
+            return self._integrate_grad(state0, t0, dt, targets, scheme, int(kw.get("checkpoint_every", 10)))
         y = self.pack(state0).clone().reshape(-1)
         plan = self.plan(y.device)
         pv = self._param_vector(y.device)
@@ -315,6 +373,26 @@ class MultilayerShallowWater2D(SomaxModel):
                 plan.step(y, pv, dt, tgt - done, scheme, False)
                 done = tgt
             ys.append(y.clone().view((3,) + self.shape))
+        st = torch.stack(ys)
+        ts = torch.tensor([t0 + k * dt for k in targets], dtype=torch.float64)
+        return Solution(ts=ts, ys=MultilayerSW2DState(h=st[:, 0], u=st[:, 1], v=st[:, 2]))
+
+    def _integrate_grad(self, state0, t0, dt, targets, scheme, every) -> Solution:
+        """``integrate`` through the checkpointed adjoint (``swm_adjoint.Integrate``): the saved
+        states are differentiable in the initial state and the parameters."""
+        from . import swm_adjoint
+
+        y = self.pack(state0).reshape(-1)
+        plan = self.plan(y.device)
+        pv = self._param_tensor(y.device)
+        ys, done, first = [], 0, True
+        for tgt in targets:
+            if tgt < done:
+                raise ValueError("saveat.ts must be increasing")
+            if tgt > done or first:
+                y = swm_adjoint.integrate(plan, y, pv, dt, tgt - done, scheme, apply_bc=first, checkpoint_every=every)
+                done, first = tgt, False
+            ys.append(y.view((3,) + self.shape))
         st = torch.stack(ys)
         ts = torch.tensor([t0 + k * dt for k in targets], dtype=torch.float64)
         return Solution(ts=ts, ys=MultilayerSW2DState(h=st[:, 0], u=st[:, 1], v=st[:, 2]))
