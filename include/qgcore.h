@@ -192,6 +192,11 @@ int qg_step_vjp(qg_plan* plan, const float* y0, const float* params, double dt, 
    the plan's stage planes serve as scratch, so calls on one plan are not concurrent. */
 int qg_project(qg_plan* plan, const float* h, const float* u, const float* v, float* h_g, float* u_g,
                float* v_g, float* psi, void* stream);
+/* The reverse mode of qg_project: (h_bar, u_bar, v_bar) = P^T (h_g_bar, u_g_bar, v_g_bar) for
+   P = G (Q G)^-1 Q, the transposes of the reconstruction and PV kernels around one adjoint
+   inversion (qg_invert_vjp).  The same members as qg_project. */
+int qg_project_vjp(qg_plan* plan, const float* h_g_bar, const float* u_g_bar, const float* v_g_bar, float* h_bar,
+                   float* u_bar, float* v_bar, void* stream);
 
 /* Kinetic energy and enstrophy per layer: ke, ens each sum(n_layers) floats (device). */
 int qg_diagnose(qg_plan* plan, const float* q, float* ke, float* ens, void* stream);
@@ -379,6 +384,17 @@ int qg_swm_step_vjp(qg_swm_plan* plan, const float* y0, const float* params, dou
    or several): stats[0..3] = min, mean, max over the finite entries and the count of
    non-finite entries, as device doubles. */
 int qg_swm_state_stats(qg_swm_plan* plan, const float* x, int64_t n, double* stats, void* stream);
+/* Reverse mode of the reparameterised model (reparameterized.py's gradient test,
+   tests/models/test_qg_reparameterized.py:193-206), the same plans as qg_reparam_step:
+   qg_reparam_bc_vjp: y_bar <- B^T P^T y_bar, the transpose of its apply_boundary_conditions
+   (wall rules B, then the projection P), in place;
+   qg_reparam_step_vjp: the adjoint of one qg_reparam_step step from y0 (y_bar: the result's
+   cotangent in, y0's out; params_bar: (nu, kappa, tau0), overwritten; work:
+   qg_reparam_step_vjp_workspace(plan, scheme) floats). */
+int qg_reparam_bc_vjp(qg_swm_plan* plan, qg_plan* qgplan, float* y_bar, void* stream);
+int64_t qg_reparam_step_vjp_workspace(const qg_swm_plan* plan, int scheme);
+int qg_reparam_step_vjp(qg_swm_plan* plan, qg_plan* qgplan, const float* y0, const float* params, double dt,
+                        int scheme, float* y_bar, float* params_bar, float* work, void* stream);
 /* QG_OK or QG_ERR_NONFINITE (a tendency was not finite since the last call); clears the flag. */
 int qg_swm_status(qg_swm_plan* plan, int* flags, void* stream);
 

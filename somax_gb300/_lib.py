@@ -119,6 +119,10 @@ def lib() -> C.CDLL:
         "qg_swm_bc_vjp": (C.c_int, [vp, vp, vp]),
         "qg_swm_step_vjp_workspace": (C.c_int64, [vp, C.c_int]),
         "qg_swm_step_vjp": (C.c_int, [vp, vp, vp, C.c_double, C.c_int, vp, vp, vp, vp]),
+        "qg_project_vjp": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, vp]),
+        "qg_reparam_bc_vjp": (C.c_int, [vp, vp, vp, vp]),
+        "qg_reparam_step_vjp_workspace": (C.c_int64, [vp, C.c_int]),
+        "qg_reparam_step_vjp": (C.c_int, [vp, vp, vp, vp, C.c_double, C.c_int, vp, vp, vp, vp]),
         "qg_swm_engine": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float)]),
         "qg_swm_kernel_stats": (C.c_int, [vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
         "qg_swm_status": (C.c_int, [vp, C.POINTER(C.c_int), vp]),

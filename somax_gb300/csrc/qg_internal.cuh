@@ -247,6 +247,10 @@ cudaError_t launch_project_q(const MemberDev* members, const StencilTile* tiles,
                              const float* h, const float* u, const float* v, float* q, cudaStream_t s);
 cudaError_t launch_project_g(const MemberDev* members, const StencilTile* tiles, int ntiles, int large,
                              const float* psi, float* hg, float* ug, float* vg, cudaStream_t s);
+cudaError_t launch_project_g_vjp(const MemberDev* members, const StencilTile* tiles, int ntiles, int large,
+                                 const float* hgb, const float* ugb, const float* vgb, float* psib, cudaStream_t s);
+cudaError_t launch_project_q_vjp(const MemberDev* members, const StencilTile* tiles, int ntiles, int large,
+                                 const float* qb, float* hb, float* ub, float* vb, cudaStream_t s);
 cudaError_t launch_residual(const MemberDev* members, const StencilTile* tiles, int ntiles, int large,
                             const float* qm, const float* psi_hat, void* out, int out_fmt,
                             int64_t xplane, cudaStream_t s, bool pdl);

@@ -1318,6 +1318,28 @@ int qg_project(qg_plan* p, const float* h, const float* u, const float* v, float
     return cuda_err(e);
 }
 
+int qg_project_vjp(qg_plan* p, const float* hg_bar, const float* ug_bar, const float* vg_bar, float* h_bar,
+                   float* u_bar, float* v_bar, void* stream) {
+    if (!p || !hg_bar || !ug_bar || !vg_bar || !h_bar || !u_bar || !v_bar) return QG_ERR_NULL;
+    if (p->n_cap > 0) return QG_ERR_UNSUPPORTED;
+    for (const MemberDev& M : p->mh)
+        if (M.barotropic) return QG_ERR_UNSUPPORTED;
+    cudaStream_t s = (cudaStream_t)stream;
+    // psi_bar and q_bar in two Butcher stage planes the forward projection does not use
+    float* psib = p->K + 2 * p->state_size;
+    float* qb = p->K + 3 * p->state_size;
+    cudaError_t e = timed(p, QG_K_OTHER, s, [&] {
+        return launch_project_g_vjp(p->md, p->st_tiles, p->n_st, p->st_large, hg_bar, ug_bar, vg_bar, psib, s);
+    });
+    if (e) return cuda_err(e);
+    const int r = qg_invert_vjp(p, psib, qb, stream);
+    if (r != QG_OK) return r;
+    e = timed(p, QG_K_OTHER, s, [&] {
+        return launch_project_q_vjp(p->md, p->st_tiles, p->n_st, p->st_large, qb, h_bar, u_bar, v_bar, s);
+    });
+    return cuda_err(e);
+}
+
 namespace {
 // dq = vector_field(q) (with the BC on read when bc), every member, on stream s.
 cudaError_t rhs_core(qg_plan* p, const float* q, float* dq, const float* params, int bc, cudaStream_t s) {

@@ -207,6 +207,75 @@ __global__ void __launch_bounds__(NTHREADS) k_project_g(const MemberDev* __restr
     }
 }
 
+// The transposes of the two projection kernels (the reverse mode of ReparameterizedQG.project):
+//   k_project_g_vjp: psi_bar = G^T (h_g_bar, u_g_bar, v_g_bar): per cell Cl2m^T diag(f0 eig)
+//                    Cm2l^T (H h_g_bar), plus the transposed grad_perp differences
+//   k_project_q_vjp: (h_bar, u_bar, v_bar) = Q^T q_bar: h_bar = -f0 q_bar / H_l, the transposed
+//                    curl differences for u_bar and v_bar
+__global__ void __launch_bounds__(NTHREADS) k_project_g_vjp(const MemberDev* __restrict__ members,
+                                                            const StencilTile* __restrict__ tiles, int TX, int TY,
+                                                            const float* __restrict__ hgb, const float* __restrict__ ugb,
+                                                            const float* __restrict__ vgb, float* __restrict__ psib) {
+    __shared__ MemberDev M;
+    const StencilTile t = tiles[blockIdx.x];
+    load_member(&M, members + t.member);
+    __syncthreads();
+    const int nl = M.nl;
+    const float idx = 1.f / M.dx, idy = 1.f / M.dy, if0 = 1.f / M.f0;
+    for (int c = threadIdx.x; c < TX * TY; c += blockDim.x) {
+        const int j = t.ty * TY + c / TX, i = t.tx * TX + c % TX;
+        if (j >= M.Ny || i >= M.Nx) continue;
+        auto interior = [&](int a, int b) { return a >= 1 && a <= M.Ny - 2 && b >= 1 && b <= M.Nx - 2; };
+        float w[kMaxLayers], wm[kMaxLayers];
+        for (int l = 0; l < nl; ++l) w[l] = M.H[l] * hgb[caller_idx(M, l, j, i)];
+        for (int m = 0; m < nl; ++m) {  // (Cm2l^T w)_m scaled by f0 eig_m
+            float s = 0.f;
+            for (int l = 0; l < nl; ++l) s = fmaf(M.Cm2l[l * kMaxLayers + m], w[l], s);
+            wm[m] = s * (M.lam[m] * if0);
+        }
+        for (int k = 0; k < nl; ++k) {
+            float s = 0.f;
+            for (int m = 0; m < nl; ++m) s = fmaf(M.Cl2m[m * kMaxLayers + k], wm[m], s);
+            const int64_t o = caller_idx(M, k, j, i);
+            // u_g(a, b) = -(psi(a, b) - psi(a - 1, b)) / dy, v_g(a, b) = (psi(a, b) - psi(a, b - 1)) / dx
+            if (interior(j, i)) s += -ugb[o] * idy + vgb[o] * idx;
+            if (interior(j + 1, i)) s += ugb[o + M.Nx] * idy;
+            if (interior(j, i + 1)) s -= vgb[o + 1] * idx;
+            psib[o] = s;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(NTHREADS) k_project_q_vjp(const MemberDev* __restrict__ members,
+                                                            const StencilTile* __restrict__ tiles, int TX, int TY,
+                                                            const float* __restrict__ qb, float* __restrict__ hb,
+                                                            float* __restrict__ ub, float* __restrict__ vb) {
+    __shared__ MemberDev M;
+    const StencilTile t = tiles[blockIdx.x];
+    load_member(&M, members + t.member);
+    __syncthreads();
+    const float idx = 1.f / M.dx, idy = 1.f / M.dy;
+    for (int c = threadIdx.x; c < TX * TY; c += blockDim.x) {
+        const int j = t.ty * TY + c / TX, i = t.tx * TX + c % TX;
+        if (j >= M.Ny || i >= M.Nx) continue;
+        auto interior = [&](int a, int b) { return a >= 1 && a <= M.Ny - 2 && b >= 1 && b <= M.Nx - 2; };
+        for (int l = 0; l < M.nl; ++l) {
+            const int64_t o = caller_idx(M, l, j, i);
+            // zeta(a, b) = (v(a, b + 1) - v(a, b)) / dx - (u(a + 1, b) - u(a, b)) / dy
+            float u = 0.f, v = 0.f;
+            if (interior(j, i)) {
+                u += qb[o] * idy;
+                v -= qb[o] * idx;
+            }
+            if (interior(j - 1, i)) u -= qb[o - M.Nx] * idy;
+            if (interior(j, i - 1)) v += qb[o - 1] * idx;
+            hb[o] = -M.f0 * qb[o] / M.H[l];
+            ub[o] = u;
+            vb[o] = v;
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------------------
 // Helmholtz residual in modal space for one refinement sweep:
 //   r_m = qm_m - (lap_full psi_hat_m - lam_m psi_hat_m)
@@ -507,6 +576,18 @@ cudaError_t launch_project_g(const MemberDev* members, const StencilTile* tiles,
                              const float* psi, float* hg, float* ug, float* vg, cudaStream_t s) {
     return launch_k(k_project_g, ntiles, NTHREADS, 0, s, false, members, tiles, large ? TileL::TX : TileS::TX,
                     large ? TileL::TY : TileS::TY, psi, hg, ug, vg);
+}
+
+cudaError_t launch_project_g_vjp(const MemberDev* members, const StencilTile* tiles, int ntiles, int large,
+                                 const float* hgb, const float* ugb, const float* vgb, float* psib, cudaStream_t s) {
+    return launch_k(k_project_g_vjp, ntiles, NTHREADS, 0, s, false, members, tiles, large ? TileL::TX : TileS::TX,
+                    large ? TileL::TY : TileS::TY, hgb, ugb, vgb, psib);
+}
+
+cudaError_t launch_project_q_vjp(const MemberDev* members, const StencilTile* tiles, int ntiles, int large,
+                                 const float* qb, float* hb, float* ub, float* vb, cudaStream_t s) {
+    return launch_k(k_project_q_vjp, ntiles, NTHREADS, 0, s, false, members, tiles, large ? TileL::TX : TileS::TX,
+                    large ? TileL::TY : TileS::TY, qb, hb, ub, vb);
 }
 
 cudaError_t launch_residual(const MemberDev* members, const StencilTile* tiles, int ntiles, int large,

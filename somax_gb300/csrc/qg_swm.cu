@@ -1481,6 +1481,101 @@ extern "C" int qg_swm_state_stats(qg_swm_plan* p, const float* x, int64_t n, dou
                                                                                                    : QG_ERR_CUDA;
 }
 
+namespace {
+// t = P(B(y)) (the reparameterised model's boundary conditions) through scratch t (a copy of
+// y with the wall rules) into out
+int reparam_bc_project(qg_swm_plan* p, qg_plan* qp, const float* y, float* t, float* out, cudaStream_t s) {
+    const int64_t lay = p->n / 3;
+    if (cudaMemcpyAsync(t, y, p->n * sizeof(float), cudaMemcpyDeviceToDevice, s)) return QG_ERR_CUDA;
+    k_swm_bc<<<swm_grid(p->d), dim3(kSwTX, kSwTY), 0, s>>>(p->d, t);
+    if (cudaGetLastError() != cudaSuccess) return QG_ERR_CUDA;
+    return qg_project(qp, t, t + lay, t + 2 * lay, out, out + lay, out + 2 * lay, nullptr, s);
+}
+
+// out = B^T P^T g (the transpose of reparam_bc_project)
+int reparam_bc_project_vjp(qg_swm_plan* p, qg_plan* qp, const float* g, float* out, cudaStream_t s) {
+    const int64_t lay = p->n / 3;
+    const int r = qg_project_vjp(qp, g, g + lay, g + 2 * lay, out, out + lay, out + 2 * lay, s);
+    if (r != QG_OK) return r;
+    k_swm_bc_vjp<<<swm_grid(p->d), dim3(kSwTX, kSwTY), 0, s>>>(p->d, out);
+    return cudaGetLastError() == cudaSuccess ? QG_OK : QG_ERR_CUDA;
+}
+}  // namespace
+
+extern "C" int qg_reparam_bc_vjp(qg_swm_plan* p, qg_plan* qp, float* y_bar, void* stream) {
+    if (!p || !qp || !y_bar) return QG_ERR_NULL;
+    if (p->desc.bc != QG_SWM_WALL) return QG_ERR_ARG;
+    if (qg_plan_state_size(qp) != p->n / 3) return QG_ERR_SHAPE;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int r = reparam_bc_project_vjp(p, qp, y_bar, p->stage, s);
+    if (r != QG_OK) return r;
+    return cudaMemcpyAsync(y_bar, p->stage, p->n * sizeof(float), cudaMemcpyDeviceToDevice, s) == cudaSuccess
+               ? QG_OK
+               : QG_ERR_CUDA;
+}
+
+extern "C" int64_t qg_reparam_step_vjp_workspace(const qg_swm_plan* p, int scheme) {
+    const Tableau* tb = swm_scheme(scheme);
+    if (!p || !tb) return -1;
+    return (int64_t)(4 * tb->n) * p->n;
+}
+
+extern "C" int qg_reparam_step_vjp(qg_swm_plan* p, qg_plan* qp, const float* y0, const float* params, double dt,
+                                   int scheme, float* y_bar, float* params_bar, float* work, void* stream) {
+    if (!p || !qp || !y0 || !params || !y_bar || !params_bar || !work) return QG_ERR_NULL;
+    const Tableau* tb = swm_scheme(scheme);
+    if (!tb || !(dt == dt)) return QG_ERR_ARG;
+    if (p->desc.bc != QG_SWM_WALL) return QG_ERR_ARG;
+    if (qg_plan_state_size(qp) != p->n / 3) return QG_ERR_SHAPE;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int ns = tb->n;
+    const int64_t n = p->n;
+    const int cgrid = (int)std::min<int64_t>(4096, (n + 255) / 256);
+    // work: raw stage inputs Y_1 .. Y_{ns-1}, projected stage inputs Z_0 .. Z_{ns-1}, stage
+    // derivatives K_0 .. K_{ns-2} (contiguous), their cotangents Kbar_0 .. Kbar_{ns-1}, and two
+    // scratch states
+    const float* Y[kMaxButcher];
+    Y[0] = y0;
+    for (int i = 1; i < ns; ++i) Y[i] = work + (int64_t)(i - 1) * n;
+    float* Z = work + (int64_t)(ns - 1) * n;
+    float* K = work + (int64_t)(2 * ns - 1) * n;
+    float* Kb = work + (int64_t)(3 * ns - 2) * n;
+    float* Zb = work + (int64_t)(4 * ns - 2) * n;
+    float* T = work + (int64_t)(4 * ns - 1) * n;
+    int r = QG_OK;
+    cudaError_t e = cudaSuccess;
+    for (int st = 0; st < ns && r == QG_OK; ++st) {
+        r = reparam_bc_project(p, qp, Y[st], T, Z + st * n, s);
+        if (r != QG_OK || st + 1 == ns) break;
+        if (launch_stage(p, stage_args(p, Z + st * n, K + st * n, params, 0), s)) return QG_ERR_CUDA;
+        Combine c{};
+        for (int m = 0; m <= st; ++m) c.c[m] = (float)(dt * tb->a[st + 1][m]);
+        k_swm_combine<<<cgrid, 256, 0, s>>>(const_cast<float*>(Y[st + 1]), y0, K, n, st + 1, c);
+        if (cudaGetLastError() != cudaSuccess) return QG_ERR_CUDA;
+    }
+    if (r != QG_OK) return r;
+    for (int st = 0; st < ns && !e; ++st) {
+        k_swm_axpy<<<cgrid, 256, 0, s>>>(Kb + st * n, y_bar, (float)(dt * tb->b[st]), n, 1);
+        e = cudaGetLastError();
+    }
+    if (!e) e = cudaMemsetAsync(p->pacc, 0, 4 * sizeof(double), s);
+    for (int st = ns - 1; st >= 0 && !e; --st) {
+        e = swm_vjp(p, Z + st * n, params, Kb + st * n, Zb, 0, s);
+        if (e) break;
+        r = reparam_bc_project_vjp(p, qp, Zb, T, s);
+        if (r != QG_OK) return r;
+        k_swm_axpy<<<cgrid, 256, 0, s>>>(y_bar, T, 1.f, n, 0);
+        for (int m = 0; m < st; ++m)
+            if (tb->a[st][m] != 0.0) k_swm_axpy<<<cgrid, 256, 0, s>>>(Kb + m * n, T, (float)(dt * tb->a[st][m]), n, 0);
+        e = cudaGetLastError();
+    }
+    if (!e) {
+        k_swm_pbar<<<1, 32, 0, s>>>(p->pacc, params_bar, 0);
+        e = cudaGetLastError();
+    }
+    return e ? QG_ERR_CUDA : QG_OK;
+}
+
 extern "C" int qg_swm_status(qg_swm_plan* p, int* flags, void* stream) {
     if (!p) return QG_ERR_NULL;
     cudaStream_t s = (cudaStream_t)stream;

@@ -186,6 +186,9 @@ class ReparameterizedQG:
         self._run(y, dt, n_steps, _solver_name(solver), apply_bc)
         return self.swm.unpack(y)
 
+    def _grad(self, *ts) -> bool:
+        return self.swm._grad(*ts)
+
     def integrate(self, state0, t0: float, t1: float, dt: float, solver=None, saveat=None, **kw):
         """``SomaxModel.integrate`` with constant steps (``core/model.py:53-88``; Tsit5 default)."""
         if kw.get("stepsize_controller") not in (None, "constant"):
@@ -196,6 +199,8 @@ class ReparameterizedQG:
         if abs(n_total * dt - (t1 - t0)) > 1e-9 * max(1.0, abs(t1 - t0)):
             raise ValueError("(t1 - t0) must be a whole number of steps")
         targets = [int(round((float(t) - t0) / dt)) for t in saveat.ts] if saveat.ts is not None else [n_total]
+        if self._grad(state0.h, state0.u, state0.v):
+            return self._integrate_grad(state0, t0, dt, targets, scheme, int(kw.get("checkpoint_every", 10)))
         y = self.swm.pack(state0).clone().reshape(-1)
         self._run(y, dt, 0, scheme, True)
         ys, done = [], 0
@@ -206,6 +211,27 @@ class ReparameterizedQG:
                 self._run(y, dt, tgt - done, scheme, False)
                 done = tgt
             ys.append(y.clone().view((3,) + self.shape))
+        st = torch.stack(ys)
+        ts = torch.tensor([t0 + k * dt for k in targets], dtype=torch.float64)
+        return Solution(ts=ts, ys=MultilayerSW2DState(h=st[:, 0], u=st[:, 1], v=st[:, 2]))
+
+    def _integrate_grad(self, state0, t0, dt, targets, scheme, every) -> Solution:
+        """``integrate`` through the checkpointed adjoint: ``qg_reparam_step_vjp`` per step,
+        ``qg_reparam_bc_vjp`` for the boundary conditions applied to the initial state."""
+        from . import swm_adjoint
+
+        y = self.swm.pack(state0).reshape(-1)
+        stepper = _ReparamStepper(self, y.device)
+        pv = self.swm._param_tensor(y.device)
+        ys, done, first = [], 0, True
+        for tgt in targets:
+            if tgt < done:
+                raise ValueError("saveat.ts must be increasing")
+            if tgt > done or first:
+                y = swm_adjoint.integrate(stepper, y, pv, dt, tgt - done, scheme, apply_bc=first,
+                                          checkpoint_every=every)
+                done, first = tgt, False
+            ys.append(y.view((3,) + self.shape))
         st = torch.stack(ys)
         ts = torch.tensor([t0 + k * dt for k in targets], dtype=torch.float64)
         return Solution(ts=ts, ys=MultilayerSW2DState(h=st[:, 0], u=st[:, 1], v=st[:, 2]))
@@ -224,3 +250,51 @@ class ReparameterizedQG:
     def status(self) -> int:
         """The shallow-water plan's non-finite flag (QG_OK or QG_ERR_NONFINITE), cleared."""
         return self.swm.status()
+
+
+class _ReparamStepper:
+    """The stepping interface of ``swm_adjoint.Integrate`` (apply_bc, step, step_vjp, bc_vjp) for
+    the reparameterised model: ``qg_reparam_step`` / ``qg_reparam_step_vjp`` /
+    ``qg_reparam_bc_vjp`` on the model's shallow-water and inversion plans."""
+
+    def __init__(self, model: ReparameterizedQG, device):
+        self.sp = model.swm.plan(device)
+        self.qp = model.plan(device)
+        self.L = self.sp._L
+        self.ws = {}
+
+    def _h(self):
+        return self.sp._h, self.qp._h
+
+    def apply_bc(self, y):
+        return self.step(y, torch.zeros(3, dtype=torch.float32, device=y.device), 1.0, 0, "tsit5", True)
+
+    def step(self, y, p, dt, k, scheme, apply_bc):
+        from .swm import _SCHEMES
+
+        sp, qp = self._h()
+        check(self.L.qg_reparam_step(sp, qp, C.c_void_p(y.data_ptr()), C.c_void_p(p.data_ptr()), float(dt), int(k),
+                                     _SCHEMES[scheme], _lib.K["QG_STEP_APPLY_BC"] if apply_bc else 0,
+                                     _stream_handle(y.device)), "qg_reparam_step")
+        return y
+
+    def step_vjp(self, y0, p, dt, scheme, g):
+        from .swm import _SCHEMES
+
+        sp, qp = self._h()
+        need = int(self.L.qg_reparam_step_vjp_workspace(sp, _SCHEMES[scheme]))
+        if scheme not in self.ws or self.ws[scheme].numel() < need:
+            self.ws[scheme] = torch.empty(need, dtype=torch.float32, device=y0.device)
+        yb = g.clone()
+        pb = torch.empty(3, dtype=torch.float32, device=y0.device)
+        check(self.L.qg_reparam_step_vjp(sp, qp, C.c_void_p(y0.data_ptr()), C.c_void_p(p.data_ptr()), float(dt),
+                                         _SCHEMES[scheme], C.c_void_p(yb.data_ptr()), C.c_void_p(pb.data_ptr()),
+                                         C.c_void_p(self.ws[scheme].data_ptr()), _stream_handle(y0.device)),
+              "qg_reparam_step_vjp")
+        return yb, pb
+
+    def bc_vjp(self, g):
+        sp, qp = self._h()
+        check(self.L.qg_reparam_bc_vjp(sp, qp, C.c_void_p(g.data_ptr()), _stream_handle(g.device)),
+              "qg_reparam_bc_vjp")
+        return g
