@@ -10,8 +10,10 @@ from .qg import (  # noqa: F401
 from .reparameterized import MultilayerSW2DState, ReparameterizedQG, ReparamQGDiagnostics  # noqa: F401
 from .swm import (  # noqa: F401
     MultilayerShallowWater2D, MultilayerSW2DDiagnostics, MultilayerSW2DParams, MultilayerSW2DPhysConsts,
+    NonlinearShallowWater2D, NonlinearSW2DDiagnostics, NonlinearSW2DParams, NonlinearSW2DPhysConsts, NonlinearSW2DState,
 )
 from .transforms import ModalTransform, StratificationProfile  # noqa: F401
 from .gfd_testcases import (  # noqa: F401
-    baroclinic_instability_swm, doublegyre_baroclinic_qg, doublegyre_qg, doublegyre_reparameterized_qg,
+    baroclinic_instability_swm, barotropic_jet_instability, doublegyre_baroclinic_qg, doublegyre_qg,
+    doublegyre_reparameterized_qg,
 )

@@ -3,8 +3,7 @@
 
 Each factory returns the GPU model and its initial state as float32 tensors on ``device``
 (default: the current CUDA device); any extra keyword (``precision``, ``refine``, ...) goes to
-the model's ``create``.  ``barotropic_jet_instability`` builds the single-layer
-``NonlinearShallowWater2D``, which this package does not implement.
+the model's ``create``.
 """
 
 from __future__ import annotations
@@ -15,13 +14,29 @@ import torch
 
 from .qg import BaroclinicQG, BaroclinicQGState, BarotropicQG, BarotropicQGState
 from .reparameterized import MultilayerSW2DState, ReparameterizedQG
-from .swm import MultilayerShallowWater2D
+from .swm import MultilayerShallowWater2D, NonlinearShallowWater2D, NonlinearSW2DState
 
 
 def _device(device):
     if device is not None:
         return torch.device(device)
     return torch.device("cuda", torch.cuda.current_device()) if torch.cuda.is_available() else torch.device("cpu")
+
+
+def barotropic_jet_instability(nx: int = 128, ny: int = 128, Lx: float = 1e6, Ly: float = 1e6, f0: float = 1e-4,
+                               beta: float = 1.6e-11, H0: float = 1000.0, jet_speed: float = 1.0,
+                               jet_width: float = 5e4, perturbation: float = 0.01, lateral_viscosity: float = 100.0,
+                               device=None, **model_kw):
+    """A Gaussian zonal jet with a sin(4 pi x / Lx) perturbation in a periodic single-layer
+    basin (gfd_testcases.py:121-181)."""
+    model = NonlinearShallowWater2D.create(nx=nx, ny=ny, Lx=Lx, Ly=Ly, f0=f0, beta=beta, H0=H0,
+                                           lateral_viscosity=lateral_viscosity, bc="periodic", **model_kw)
+    g = model.grid
+    u0, v0 = jet_fields(g.Nx, g.Ny, g.dx, g.dy, Lx, Ly, jet_speed, jet_width, perturbation, (1.0,))
+    dev = _device(device)
+    h0 = torch.full((g.Ny, g.Nx), float(H0), dtype=torch.float32, device=dev)
+    return model, NonlinearSW2DState(h=h0, u=u0[0].to(device=dev, dtype=torch.float32),
+                                     v=v0[0].to(device=dev, dtype=torch.float32))
 
 
 def doublegyre_qg(nx: int = 64, ny: int = 64, Lx: float = 1e6, Ly: float = 1e6, f0: float = 1e-4,
@@ -50,7 +65,7 @@ def doublegyre_baroclinic_qg(nx: int = 128, ny: int = 128, Lx: float = 4e6, Ly: 
 
 def jet_fields(Nx: int, Ny: int, dx: float, dy: float, Lx: float, Ly: float, jet_speed: float, jet_width: float,
                perturbation: float, signs):
-    """(u0, v0) of the 2-layer jet in float64 on the host: a Gaussian zonal jet about y = Ly / 2
+    """(u0, v0) of a layered jet in float64 on the host: a Gaussian zonal jet about y = Ly / 2
     with the given sign per layer and a sin(4 pi x / Lx) meridional perturbation under the same
     envelope, on every point of the padded grid (x_i = i dx, y_j = j dy)."""
     x = torch.arange(Nx, dtype=torch.float64) * dx
@@ -100,4 +115,5 @@ def doublegyre_reparameterized_qg(nx: int = 128, ny: int = 128, Lx: float = 4e6,
     return model, MultilayerSW2DState(h=h0, u=z, v=z.clone())
 
 
-__all__ = ["doublegyre_qg", "doublegyre_baroclinic_qg", "baroclinic_instability_swm", "doublegyre_reparameterized_qg"]
+__all__ = ["barotropic_jet_instability", "doublegyre_qg", "doublegyre_baroclinic_qg", "baroclinic_instability_swm",
+           "doublegyre_reparameterized_qg"]

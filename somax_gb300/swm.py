@@ -432,4 +432,132 @@ class MultilayerShallowWater2D(SomaxModel):
 
 
 __all__ = ["MultilayerShallowWater2D", "MultilayerSW2DParams", "MultilayerSW2DPhysConsts", "MultilayerSW2DDiagnostics",
-           "MultilayerSW2DState"]
+           "MultilayerSW2DState", "NonlinearShallowWater2D", "NonlinearSW2DState", "NonlinearSW2DParams",
+           "NonlinearSW2DPhysConsts", "NonlinearSW2DDiagnostics"]
+
+
+# ---- the single-layer nonlinear model ---------------------------------------------------------
+@dataclasses.dataclass
+class NonlinearSW2DState:
+    """``NonlinearSW2DState`` (``swm/nonlinear_2d.py:25-36``): h, u, v, each (Ny, Nx)."""
+
+    h: torch.Tensor
+    u: torch.Tensor
+    v: torch.Tensor
+
+
+@dataclasses.dataclass
+class NonlinearSW2DParams:
+    """Differentiable parameters (``nonlinear_2d.py:39-50``)."""
+
+    lateral_viscosity: torch.Tensor
+    bottom_drag: torch.Tensor
+    wind_amplitude: torch.Tensor
+
+
+@dataclasses.dataclass(frozen=True)
+class NonlinearSW2DPhysConsts:
+    """Frozen constants (``nonlinear_2d.py:53-66``)."""
+
+    gravity: float = 9.81
+    f0: float = 1e-4
+    beta: float = 0.0
+    H0: float = 100.0
+
+
+@dataclasses.dataclass
+class NonlinearSW2DDiagnostics:
+    """Diagnostics (``nonlinear_2d.py:69-86``)."""
+
+    energy: torch.Tensor
+    enstrophy: torch.Tensor
+    potential_vorticity: torch.Tensor
+    relative_vorticity: torch.Tensor
+    kinetic_energy_field: torch.Tensor
+
+
+class NonlinearShallowWater2D(SomaxModel):
+    """The single-layer nonlinear shallow-water model (``swm/nonlinear_2d.py:89-318``) on the
+    multilayer engine: it is the one-layer case with g' = g and the wind stress applied to u
+    without the division by the layer depth (the engine divides by H[0], which this model
+    sets to 1; the mean depth H0 is a constant of the model, not of its right-hand side).
+    States are (Ny, Nx) fields; every method converts to the one-layer packing and back."""
+
+    state_cls = NonlinearSW2DState
+
+    def __init__(self, swm: MultilayerShallowWater2D, consts: NonlinearSW2DPhysConsts):
+        self.swm = swm
+        self.consts = consts
+
+    @staticmethod
+    def create(nx: int = 64, ny: int = 64, Lx: float = 1e6, Ly: float = 1e6, g: float = 9.81, f0: float = 1e-4,
+               beta: float = 0.0, H0: float = 100.0, lateral_viscosity: float = 0.0, bottom_drag: float = 0.0,
+               wind_amplitude: float = 0.0, wind_profile: str = "doublegyre", bc: str = "periodic",
+               method: str = "upwind1", engine: str = "auto") -> "NonlinearShallowWater2D":
+        """``NonlinearShallowWater2D.create`` (``nonlinear_2d.py:236-318``) with the same keywords."""
+        swm = MultilayerShallowWater2D.create(nx=nx, ny=ny, Lx=Lx, Ly=Ly, g=g, f0=f0, beta=beta, n_layers=1, H=(1.0,),
+                                              g_prime=(g,), lateral_viscosity=lateral_viscosity,
+                                              bottom_drag=bottom_drag, wind_amplitude=wind_amplitude,
+                                              wind_profile=wind_profile, bc=bc, method=method, engine=engine)
+        return NonlinearShallowWater2D(swm, NonlinearSW2DPhysConsts(gravity=g, f0=f0, beta=beta, H0=H0))
+
+    @property
+    def params(self):
+        p = self.swm.params
+        return NonlinearSW2DParams(p.lateral_viscosity, p.bottom_drag, p.wind_amplitude)
+
+    @params.setter
+    def params(self, value):
+        self.swm.params = MultilayerSW2DParams(value.lateral_viscosity, value.bottom_drag, value.wind_amplitude)
+
+    @property
+    def grid(self):
+        return self.swm.grid
+
+    @property
+    def shape(self):
+        return (self.grid.Ny, self.grid.Nx)
+
+    def plan(self, device=None) -> SwmPlan:
+        return self.swm.plan(device)
+
+    def _to3(self, state) -> MultilayerSW2DState:
+        for name in ("h", "u", "v"):
+            t = getattr(state, name)
+            if tuple(t.shape) != self.shape:
+                raise ValueError(f"{name} must have shape {self.shape}, got {tuple(t.shape)}")
+        return MultilayerSW2DState(h=state.h[None], u=state.u[None], v=state.v[None])
+
+    @staticmethod
+    def _to2(state) -> NonlinearSW2DState:
+        return NonlinearSW2DState(h=state.h[..., 0, :, :], u=state.u[..., 0, :, :], v=state.v[..., 0, :, :])
+
+    def vector_field(self, t, state, args=None) -> NonlinearSW2DState:
+        """Tendencies of the state as given (``nonlinear_2d.py:132-181``)."""
+        return self._to2(self.swm.vector_field(t, self._to3(state), args))
+
+    def apply_boundary_conditions(self, state) -> NonlinearSW2DState:
+        """Periodic wrap or the wall rules (``nonlinear_2d.py:183-208``)."""
+        return self._to2(self.swm.apply_boundary_conditions(self._to3(state)))
+
+    def step(self, state, dt: float, n_steps: int = 1, solver="tsit5", apply_bc: bool = True) -> NonlinearSW2DState:
+        return self._to2(self.swm.step(self._to3(state), dt, n_steps, solver, apply_bc))
+
+    def integrate(self, state0, t0: float, t1: float, dt: float, solver=None, saveat=None, **kw) -> Solution:
+        """``SomaxModel.integrate`` with constant steps (Tsit5 default); differentiable in the
+        state and the parameters."""
+        sol = self.swm.integrate(self._to3(state0), t0, t1, dt, solver=solver, saveat=saveat, **kw)
+        return Solution(ts=sol.ts, ys=self._to2(sol.ys))
+
+    def diagnose(self, state) -> NonlinearSW2DDiagnostics:
+        """Energy (KE + g h^2 / 2) and potential enstrophy (q^2 h_X / 2) summed over the interior
+        with the cell area, PV and relative vorticity at the X points, KE at the T points
+        (``nonlinear_2d.py:209-233``)."""
+        d = self.swm.diagnose(self._to3(state))
+        return NonlinearSW2DDiagnostics(energy=d.total_energy, enstrophy=d.total_enstrophy,
+                                        potential_vorticity=d.potential_vorticity[0],
+                                        relative_vorticity=d.relative_vorticity[0],
+                                        kinetic_energy_field=d.kinetic_energy_field[0])
+
+    def status(self) -> int:
+        return self.swm.status()

@@ -30,6 +30,18 @@ def test_factories_types_and_shapes():
     assert s.h.shape[0] == 2 and torch.equal(s.h[:, 0, 0], torch.tensor([500.0, 4500.0]))
 
 
+def test_barotropic_jet_factory():
+    """gfd_testcases.py:121-181: one periodic layer of depth H0, the Gaussian jet in u and the
+    sin(4 pi x / Lx) perturbation in v."""
+    m, s = sg.barotropic_jet_instability(nx=32, ny=32, device="cpu")
+    assert isinstance(m, sg.NonlinearShallowWater2D) and isinstance(s, sg.NonlinearSW2DState)
+    assert s.h.shape == (34, 34) and float(s.h.min()) == float(s.h.max()) == 1000.0
+    g = m.grid
+    env = np.exp(-0.5 * ((np.arange(g.Ny) * g.dy - g.Ly / 2) / 5e4) ** 2)
+    assert np.allclose(s.u[:, 5].double().numpy(), env, rtol=1e-6, atol=1e-9)
+    assert m.consts.H0 == 1000.0 and m.swm.bc_type == "periodic"
+
+
 def test_jet_fields():
     """Opposite Gaussian jets about Ly / 2 and a sin(4 pi x / Lx) perturbation under the same
     envelope (gfd_testcases.py:344-359), on the padded grid (x_i = i dx, y_j = j dy)."""
