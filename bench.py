@@ -425,6 +425,121 @@ def run_swm(args, dev, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+SWM_GRAD_DESC = ("swm_grad_jet64: one gradient per bench step of the misfit 0.5 |h(T) - h_target|^2 of the "
+                 "reference's swm_jet basin (2-layer 64x64 periodic, nu=1000) after 360 tsit5 steps (dt=20s, 2 model "
+                 "hours; seeded 0.5 m target anomaly) with respect to h0, nu, kappa and tau0: forward with checkpoints "
+                 "every 30 steps, reverse sweep with segment recomputation and qg_swm_step_vjp per step; value = model-"
+                 "days of forward + reverse integration per second")
+
+
+def swm_grad_launches(engine: str, n_steps: int, every: int, ns: int = 6) -> int:
+    """Kernel launches of one Tsit5 gradient: the forward (boundary rules, then a call per
+    checkpoint segment), the backward's recomputation (a one-step call per step of a segment
+    but its first), one qg_swm_step_vjp per step (ns - 1 stage and combine launches, ns
+    cotangent initialisations, per stage the three VJP kernels and the y_bar update, one update
+    per non-zero a_sm, the parameter write-out) and the final transposed boundary rules."""
+    segs = -(-n_steps // every)
+    per_call = 1 if engine == "cluster" else None
+    fwd = 1 + (segs if per_call else n_steps * ns)
+    recompute = (n_steps - segs) * (1 if per_call else ns)
+    vjp = 2 * (ns - 1) + ns + 4 * ns + ns * (ns - 1) // 2 + 1
+    return fwd + recompute + n_steps * vjp + 1
+
+
+def run_swm_grad(args, dev, world, rank, local):
+    """The shallow-water adjoint's bench line (``--config swm_grad_jet64``)."""
+    import torch
+
+    import somax_gb300 as sg
+    from somax_gb300 import testcases as tc
+
+    cfg = tc.SWM_JET64
+    n_steps, every = 360, 30
+    m = sg.MultilayerShallowWater2D.create(**cfg.model_kwargs(), engine=args.swm_engine)
+    y0 = tc.swm_initial_state(cfg, seed=rank)
+    rng = np.random.default_rng(100 + rank)
+    target = torch.tensor(y0[0] + 0.5 * rng.standard_normal(y0[0].shape), dtype=torch.float64, device=dev)
+    base = (float(cfg.lateral_viscosity), float(cfg.bottom_drag), float(cfg.wind_amplitude))
+
+    def gradient(h0):
+        m.params = sg.MultilayerSW2DParams(*(torch.tensor(x, requires_grad=True) for x in base))
+        h = h0.detach().clone().requires_grad_(True)
+        u = torch.tensor(y0[1], device=dev)
+        v = torch.tensor(y0[2], device=dev)
+        sol = m.integrate(sg.MultilayerSW2DState(h=h, u=u, v=v), 0.0, n_steps * cfg.dt, cfg.dt, checkpoint_every=every)
+        loss = 0.5 * ((sol.ys.h[-1].double() - target) ** 2).sum()
+        loss.backward()
+        return h.grad, m.params.lateral_viscosity.grad
+
+    h0 = torch.tensor(y0[0], device=dev)
+    for _ in range(args.warmup):
+        gradient(h0)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        for k in range(args.steps):
+            ev[k][0].record()
+            gradient(h0)
+            ev[k][1].record()
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    dev_ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in ev), world, dev)
+    days = n_steps * cfg.dt / 86400.0
+    value = world * args.steps * days / (dev_ms / 1000.0)
+    # e2e: h0 from pinned host memory, the gradient back to pinned host memory
+    hh = torch.tensor(y0[0]).pin_memory()
+    out = torch.empty_like(hh).pin_memory()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        g, _ = gradient(hh.to(dev, non_blocking=True))
+        out.copy_(g, non_blocking=True)
+        torch.cuda.current_stream(dev).synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world, dev)
+    line = {
+        "metric": SWM_METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": SWM_GRAD_DESC, "engine": m.plan(dev).engine(cfg.scheme)},
+        "e2e": {"value": world * args.steps * days / e2e_s, "unit": UNIT, "h2d_bytes_per_step": hh.numel() * 4,
+                "d2h_bytes_per_step": out.numel() * 4, "api": "MultilayerShallowWater2D.integrate + autograd"},
+        "gpu_launches": args.steps * swm_grad_launches(m.plan(dev).engine(cfg.scheme)["engine"], n_steps, every),
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import swm as W
+
+        v, n, el = swm_cpu_rate(cfg, 10.0)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+                                "sample": f"{n} tsit5 steps of swm_jet64 forward only (the float32 restatement has no "
+                                          f"reverse mode; {el:.1f} s)"}
+        # d/d nu of 0.5 sum u^2 after 10 steps against float64 central differences of the
+        # restatement (u is what nu acts on; the h misfit's derivative in nu is a small
+        # difference of terms that FP32 holds to ~1e-3 and is not a parity measure)
+        n10 = 10
+
+        def oloss(nu):
+            o = W.create(**dict(cfg.oracle_kwargs(), lateral_viscosity=nu))
+            z = W.integrate(o, y0.astype(np.float64), cfg.dt, n10, "tsit5")
+            return 0.5 * (z[1] ** 2).sum()
+
+        m.params = sg.MultilayerSW2DParams(*(torch.tensor(x, requires_grad=True) for x in base))
+        sol = m.integrate(sg.MultilayerSW2DState(*(torch.tensor(y0[k], device=dev) for k in range(3))), 0.0,
+                          n10 * cfg.dt, cfg.dt)
+        (0.5 * (sol.ys.u[-1].double() ** 2).sum()).backward()
+        hnu = base[0] * 1e-4
+        fd = (oloss(base[0] + hnu) - oloss(base[0] - hnu)) / (2 * hnu)
+        got = float(m.params.lateral_viscosity.grad)
+        line["parity"] = {"d_half_sum_u2_d_nu_10_steps": got, "float64_difference": fd,
+                          "rel": abs(got - fd) / abs(fd), "bound": 1e-3,
+                          "against": "float64 central differences of the NumPy restatement"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def max_over_ranks(x: float, world: int, device) -> float:
     """The largest of every rank's x: a multi-rank job takes as long as its slowest rank."""
     if world <= 1:
@@ -452,8 +567,8 @@ def run_reference(args):
     if rank != 0:
         return
     threads = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
-    if args.config in tc.SWM_CONFIGS:
-        cfg = tc.SWM_CONFIGS[args.config]
+    if args.config in tc.SWM_CONFIGS or args.config == "swm_grad_jet64":
+        cfg = tc.SWM_CONFIGS.get(args.config, tc.SWM_JET64)
         vals, samples = [], []
         for k in range(args.warmup + args.steps):
             v, n, el = swm_cpu_rate(cfg, 5.0 if k >= args.warmup else 1.0)
@@ -467,7 +582,8 @@ def run_reference(args):
             "impl": "reference", "metric": SWM_METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": SWM_DESC[cfg.name], "sample": sample},
+            "config": {"workload": SWM_GRAD_DESC if args.config == "swm_grad_jet64" else SWM_DESC[cfg.name],
+                       "sample": sample},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}), flush=True)
         return
@@ -796,7 +912,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="ensemble256",
                     help="ensemble256 (default) | baroclinic3_128 | barotropic_64 | baroclinic3_256 | "
-                         "baroclinic3_512 | baroclinic3_1024 | masked3_512 | adjoint256 | swm_jet64 | swm3_1024")
+                         "baroclinic3_512 | baroclinic3_1024 | masked3_512 | adjoint256 | swm_jet64 | swm3_1024 | "
+                         "swm_grad_jet64")
     ap.add_argument("--precision", default="bf16x3", help="DST-I GEMM arithmetic: fp32 | tf32 | bf16x3")
     ap.add_argument("--persistent", type=int, default=0,
                     help="1: all steps of a call in one persistent cooperative launch (tensor-core precisions)")
@@ -832,6 +949,11 @@ def main():
     if world > 1:
         dist.init_process_group("nccl", device_id=dev)
 
+    if args.config == "swm_grad_jet64":
+        run_swm_grad(args, dev, world, rank, local)
+        if world > 1:
+            dist.destroy_process_group()
+        return
     if args.config in tc.SWM_CONFIGS:
         run_swm(args, dev, world, rank, local)
         if world > 1:
