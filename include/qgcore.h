@@ -373,11 +373,21 @@ int qg_reparam_step(qg_swm_plan* plan, qg_plan* qgplan, float* state, const floa
    qg_swm_bc_vjp: the transpose of apply_boundary_conditions on a cotangent, in place.
    qg_swm_step_vjp: the adjoint of one qg_swm_step step from y0: y_bar holds the cotangent of
    the step's result on entry and that of y0 on return; params_bar receives the parameter
-   cotangents (overwritten); work holds qg_swm_step_vjp_workspace(plan, scheme) floats. */
+   cotangents (overwritten); work holds qg_swm_step_vjp_workspace(plan, scheme) floats.  The
+   step's adjoint is captured as a CUDA graph and replayed while its five pointers, dt and the
+   scheme repeat (recaptured otherwise). */
 int qg_swm_rhs_vjp(qg_swm_plan* plan, const float* state, const float* params, const float* tend_bar,
                    float* state_bar, float* params_bar, int flags, void* stream);
 int qg_swm_bc_vjp(qg_swm_plan* plan, float* state_bar, void* stream);
 int64_t qg_swm_step_vjp_workspace(const qg_swm_plan* plan, int scheme);
+/* The adjoint of k steps from the checkpoint y_start in one call: the segment's states are
+   recomputed into work (qg_swm_segment_vjp_workspace(plan, scheme, k) floats), then every
+   step's adjoint runs in reverse; y_bar holds the cotangent of the k-th state on entry and
+   that of y_start on return, params_bar the parameter cotangents summed over the k steps.
+   Replayed as one captured graph while its pointers, dt, k and the scheme repeat. */
+int64_t qg_swm_segment_vjp_workspace(const qg_swm_plan* plan, int scheme, int k);
+int qg_swm_segment_vjp(qg_swm_plan* plan, const float* y_start, const float* params, double dt, int k, int scheme,
+                       float* y_bar, float* params_bar, float* work, void* stream);
 int qg_swm_step_vjp(qg_swm_plan* plan, const float* y0, const float* params, double dt, int scheme, float* y_bar,
                     float* params_bar, float* work, void* stream);
 /* The runner's state statistics (cli/_run.py:408-432) of n floats at x (one field of a state,

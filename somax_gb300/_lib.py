@@ -119,6 +119,8 @@ def lib() -> C.CDLL:
         "qg_swm_bc_vjp": (C.c_int, [vp, vp, vp]),
         "qg_swm_step_vjp_workspace": (C.c_int64, [vp, C.c_int]),
         "qg_swm_step_vjp": (C.c_int, [vp, vp, vp, C.c_double, C.c_int, vp, vp, vp, vp]),
+        "qg_swm_segment_vjp_workspace": (C.c_int64, [vp, C.c_int, C.c_int]),
+        "qg_swm_segment_vjp": (C.c_int, [vp, vp, vp, C.c_double, C.c_int, C.c_int, vp, vp, vp, vp]),
         "qg_project_vjp": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, vp]),
         "qg_reparam_bc_vjp": (C.c_int, [vp, vp, vp, vp]),
         "qg_reparam_step_vjp_workspace": (C.c_int64, [vp, C.c_int]),

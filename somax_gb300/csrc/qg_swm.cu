@@ -866,6 +866,16 @@ struct qg_swm_plan {
     void* stats_acc = nullptr;  // qg_swm_state_stats accumulators
     float* mid = nullptr;       // the VJP's mid-point cotangents (6 planes per layer)
     double* pacc = nullptr;     // the VJP's parameter cotangent sums
+    // qg_swm_step_vjp replayed as a captured graph while its pointers, dt and scheme repeat
+    cudaGraphExec_t vjp_exec = nullptr;
+    const void* vjp_ptr[5] = {};
+    double vjp_dt = 0.0;
+    int vjp_scheme = -1;
+    // qg_swm_segment_vjp replayed as a captured graph while its arguments repeat
+    cudaGraphExec_t seg_exec = nullptr;
+    const void* seg_ptr[5] = {};
+    double seg_dt = 0.0;
+    int seg_scheme = -1, seg_k = -1;
     int* flags = nullptr;
     int64_t n = 0;            // floats of one state
     int device = 0;
@@ -985,7 +995,7 @@ extern "C" int qg_swm_create(const qg_swm_desc* desc, qg_swm_plan** out) {
 extern "C" void qg_swm_destroy(qg_swm_plan* p) {
     if (!p) return;
     cudaDeviceSynchronize();
-    for (cudaGraphExec_t x : {p->g8, p->g1})
+    for (cudaGraphExec_t x : {p->g8, p->g1, p->vjp_exec, p->seg_exec})
         if (x) cudaGraphExecDestroy(x);
     for (auto& v : p->ev)
         for (auto& pr : v) {
@@ -1422,12 +1432,10 @@ extern "C" int64_t qg_swm_step_vjp_workspace(const qg_swm_plan* p, int scheme) {
     return (int64_t)(3 * tb->n - 1) * p->n;
 }
 
-extern "C" int qg_swm_step_vjp(qg_swm_plan* p, const float* y0, const float* params, double dt, int scheme,
-                               float* y_bar, float* params_bar, float* work, void* stream) {
-    if (!p || !y0 || !params || !y_bar || !params_bar || !work) return QG_ERR_NULL;
-    const Tableau* tb = swm_scheme(scheme);
-    if (!tb || !(dt == dt)) return QG_ERR_ARG;
-    cudaStream_t s = (cudaStream_t)stream;
+namespace {
+// The launches of one step's adjoint on stream s (see qg_swm_step_vjp).
+cudaError_t swm_step_vjp_body(qg_swm_plan* p, const float* y0, const float* params, double dt, const Tableau* tb,
+                              float* y_bar, float* params_bar, float* work, cudaStream_t s, bool own_pacc = true) {
     const int ns = tb->n;
     const int64_t n = p->n;
     const int cgrid = (int)std::min<int64_t>(4096, (n + 255) / 256);
@@ -1455,7 +1463,7 @@ extern "C" int qg_swm_step_vjp(qg_swm_plan* p, const float* y0, const float* par
         k_swm_axpy<<<cgrid, 256, 0, s>>>(Kb + st * n, y_bar, (float)(dt * tb->b[st]), n, 1);
         e = cudaGetLastError();
     }
-    if (!e) e = cudaMemsetAsync(p->pacc, 0, 4 * sizeof(double), s);
+    if (!e && own_pacc) e = cudaMemsetAsync(p->pacc, 0, 4 * sizeof(double), s);
     for (int st = ns - 1; st >= 0 && !e; --st) {
         e = swm_vjp(p, Y[st], params, Kb + st * n, Yb, 1, s);
         if (e) break;
@@ -1464,11 +1472,120 @@ extern "C" int qg_swm_step_vjp(qg_swm_plan* p, const float* y0, const float* par
             if (tb->a[st][m] != 0.0) k_swm_axpy<<<cgrid, 256, 0, s>>>(Kb + m * n, Yb, (float)(dt * tb->a[st][m]), n, 0);
         e = cudaGetLastError();
     }
+    if (!e && own_pacc) {
+        k_swm_pbar<<<1, 32, 0, s>>>(p->pacc, params_bar, 0);
+        e = cudaGetLastError();
+    }
+    return e;
+}
+
+// The adjoint of k steps from y_start on stream s: the k - 1 later states recomputed into
+// work (one step each, the stage engine), then each step's adjoint in reverse, the parameter
+// cotangents summed over the steps into params_bar.
+cudaError_t swm_segment_vjp_body(qg_swm_plan* p, const float* y_start, const float* params, double dt,
+                                 const Tableau* tb, int k, float* y_bar, float* params_bar, float* work,
+                                 cudaStream_t s) {
+    const int64_t n = p->n;
+    float* states = work;                        // y_1 .. y_{k-1}
+    float* vwork = work + (int64_t)(k - 1) * n;  // one step's adjoint workspace
+    cudaError_t e = cudaSuccess;
+    for (int i = 1; i < k && !e; ++i) {
+        float* y = states + (int64_t)(i - 1) * n;
+        e = cudaMemcpyAsync(y, i == 1 ? y_start : y - n, n * sizeof(float), cudaMemcpyDeviceToDevice, s);
+        if (!e) e = swm_steps(p, y, tb, dt, 1, s);
+    }
+    if (!e) e = cudaMemsetAsync(p->pacc, 0, 4 * sizeof(double), s);
+    for (int i = k - 1; i >= 0 && !e; --i) {
+        const float* y = i == 0 ? y_start : states + (int64_t)(i - 1) * n;
+        e = swm_step_vjp_body(p, y, params, dt, tb, y_bar, params_bar, vwork, s, false);
+    }
     if (!e) {
         k_swm_pbar<<<1, 32, 0, s>>>(p->pacc, params_bar, 0);
         e = cudaGetLastError();
     }
-    return e ? QG_ERR_CUDA : QG_OK;
+    return e;
+}
+}  // namespace
+
+extern "C" int qg_swm_step_vjp(qg_swm_plan* p, const float* y0, const float* params, double dt, int scheme,
+                               float* y_bar, float* params_bar, float* work, void* stream) {
+    if (!p || !y0 || !params || !y_bar || !params_bar || !work) return QG_ERR_NULL;
+    const Tableau* tb = swm_scheme(scheme);
+    if (!tb || !(dt == dt)) return QG_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (p->profiling) return swm_step_vjp_body(p, y0, params, dt, tb, y_bar, params_bar, work, s) ? QG_ERR_CUDA : QG_OK;
+    // ~9 launches per stage: captured once per set of arguments and replayed while they repeat
+    // (callers that stage every step's state and cotangent in the same buffers replay it every step)
+    const void* ptr[5] = {y0, params, y_bar, params_bar, work};
+    bool same = p->vjp_exec && p->vjp_dt == dt && p->vjp_scheme == scheme;
+    for (int k = 0; k < 5 && same; ++k) same = p->vjp_ptr[k] == ptr[k];
+    cudaError_t e = cudaSuccess;
+    if (!same) {
+        if (p->vjp_exec) {
+            cudaGraphExecDestroy(p->vjp_exec);
+            p->vjp_exec = nullptr;
+        }
+        cudaGraph_t graph = nullptr;
+        e = cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal);
+        if (!e) {
+            const cudaError_t e1 = swm_step_vjp_body(p, y0, params, dt, tb, y_bar, params_bar, work, p->cap);
+            e = cudaStreamEndCapture(p->cap, &graph);
+            if (!e) e = e1;
+        }
+        if (!e) e = cudaGraphInstantiate(&p->vjp_exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (e) {
+            p->vjp_exec = nullptr;
+            return QG_ERR_CUDA;
+        }
+        for (int k = 0; k < 5; ++k) p->vjp_ptr[k] = ptr[k];
+        p->vjp_dt = dt;
+        p->vjp_scheme = scheme;
+    }
+    return cudaGraphLaunch(p->vjp_exec, s) == cudaSuccess ? QG_OK : QG_ERR_CUDA;
+}
+
+extern "C" int64_t qg_swm_segment_vjp_workspace(const qg_swm_plan* p, int scheme, int k) {
+    const Tableau* tb = swm_scheme(scheme);
+    if (!p || !tb || k < 1) return -1;
+    return (int64_t)(k - 1 + 3 * tb->n - 1) * p->n;
+}
+
+extern "C" int qg_swm_segment_vjp(qg_swm_plan* p, const float* y_start, const float* params, double dt, int k,
+                                  int scheme, float* y_bar, float* params_bar, float* work, void* stream) {
+    if (!p || !y_start || !params || !y_bar || !params_bar || !work) return QG_ERR_NULL;
+    const Tableau* tb = swm_scheme(scheme);
+    if (!tb || !(dt == dt) || k < 1) return QG_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (p->profiling)
+        return swm_segment_vjp_body(p, y_start, params, dt, tb, k, y_bar, params_bar, work, s) ? QG_ERR_CUDA : QG_OK;
+    const void* ptr[5] = {y_start, params, y_bar, params_bar, work};
+    bool same = p->seg_exec && p->seg_dt == dt && p->seg_scheme == scheme && p->seg_k == k;
+    for (int i = 0; i < 5 && same; ++i) same = p->seg_ptr[i] == ptr[i];
+    if (!same) {
+        if (p->seg_exec) {
+            cudaGraphExecDestroy(p->seg_exec);
+            p->seg_exec = nullptr;
+        }
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal);
+        if (!e) {
+            const cudaError_t e1 = swm_segment_vjp_body(p, y_start, params, dt, tb, k, y_bar, params_bar, work, p->cap);
+            e = cudaStreamEndCapture(p->cap, &graph);
+            if (!e) e = e1;
+        }
+        if (!e) e = cudaGraphInstantiate(&p->seg_exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (e) {
+            p->seg_exec = nullptr;
+            return QG_ERR_CUDA;
+        }
+        for (int i = 0; i < 5; ++i) p->seg_ptr[i] = ptr[i];
+        p->seg_dt = dt;
+        p->seg_scheme = scheme;
+        p->seg_k = k;
+    }
+    return cudaGraphLaunch(p->seg_exec, s) == cudaSuccess ? QG_OK : QG_ERR_CUDA;
 }
 
 extern "C" int qg_swm_state_stats(qg_swm_plan* p, const float* x, int64_t n, double* stats, void* stream) {

@@ -167,18 +167,51 @@ class SwmPlan:
         result (``qg_swm_step_vjp``; the workspace is kept per scheme)."""
         self._check(y0, "state")
         self._check(g, "cotangent")
-        ws = getattr(self, "_vjp_work", {})
-        self._vjp_work = ws
+        # the state and the cotangent are staged in fixed buffers (with the workspace, per
+        # scheme), so that the library replays the step's captured adjoint graph every step
+        bufs = getattr(self, "_vjp_bufs", {})
+        self._vjp_bufs = bufs
         need = int(self._L.qg_swm_step_vjp_workspace(self._h, _SCHEMES[scheme]))
-        if scheme not in ws or ws[scheme].numel() < need or ws[scheme].device != y0.device:
-            ws[scheme] = torch.empty(need, dtype=torch.float32, device=y0.device)
-        yb = g.clone()
-        pb = torch.empty(3, dtype=torch.float32, device=y0.device)
-        check(self._L.qg_swm_step_vjp(self._h, C.c_void_p(y0.data_ptr()), C.c_void_p(params.data_ptr()), float(dt),
+        b = bufs.get(scheme)
+        if b is None or b[3].numel() < need or b[3].device != y0.device:
+            b = (torch.empty_like(y0), torch.empty_like(y0), torch.empty(3, dtype=torch.float32, device=y0.device),
+                 torch.empty(need, dtype=torch.float32, device=y0.device))
+            bufs[scheme] = b
+        yin, yb, pb, work = b
+        yin.copy_(y0)
+        yb.copy_(g)
+        check(self._L.qg_swm_step_vjp(self._h, C.c_void_p(yin.data_ptr()), C.c_void_p(params.data_ptr()), float(dt),
                                       _SCHEMES[scheme], C.c_void_p(yb.data_ptr()), C.c_void_p(pb.data_ptr()),
-                                      C.c_void_p(ws[scheme].data_ptr()), _stream_handle(y0.device)),
+                                      C.c_void_p(work.data_ptr()), _stream_handle(y0.device)),
               "qg_swm_step_vjp")
-        return yb, pb
+        return yb.clone(), pb.clone()
+
+    def segment_vjp(self, y_start: torch.Tensor, params: torch.Tensor, dt: float, k: int, scheme: str,
+                    g: torch.Tensor):
+        """(y_start_bar, params_bar) of k steps of ``scheme`` from the checkpoint ``y_start`` for the
+        cotangent ``g`` of the k-th state, in one call (``qg_swm_segment_vjp``: the segment's
+        states recomputed and every step's adjoint in reverse, replayed as one graph while the
+        staged buffers, dt, k and the scheme repeat)."""
+        self._check(y_start, "state")
+        self._check(g, "cotangent")
+        bufs = getattr(self, "_seg_bufs", {})
+        self._seg_bufs = bufs
+        key = (scheme, int(k))
+        need = int(self._L.qg_swm_segment_vjp_workspace(self._h, _SCHEMES[scheme], int(k)))
+        b = bufs.get(key)
+        if b is None or b[3].device != y_start.device:
+            b = (torch.empty_like(y_start), torch.empty_like(y_start),
+                 torch.empty(3, dtype=torch.float32, device=y_start.device),
+                 torch.empty(need, dtype=torch.float32, device=y_start.device))
+            bufs[key] = b
+        yin, yb, pb, work = b
+        yin.copy_(y_start)
+        yb.copy_(g)
+        check(self._L.qg_swm_segment_vjp(self._h, C.c_void_p(yin.data_ptr()), C.c_void_p(params.data_ptr()),
+                                         float(dt), int(k), _SCHEMES[scheme], C.c_void_p(yb.data_ptr()),
+                                         C.c_void_p(pb.data_ptr()), C.c_void_p(work.data_ptr()),
+                                         _stream_handle(y_start.device)), "qg_swm_segment_vjp")
+        return yb.clone(), pb.clone()
 
     def field_stats(self, x: torch.Tensor) -> torch.Tensor:
         """(min, mean, max) over the finite entries of the float32 CUDA tensor x and the count of

@@ -3,10 +3,12 @@ VJPs of libqgcore (what the reference takes with JAX autodiff through ``vector_f
 ``integrate``: ``tests/models/test_swm_multilayer.py:239-252``).
 
 * :class:`RHS`       -> ``qg_swm_rhs_vjp`` (the state's and the parameters' cotangents)
-* :class:`Integrate` -> ``qg_swm_step_vjp`` per step (the step's stage inputs recomputed and the
-  stages reversed in one C-ABI call), the state kept every ``checkpoint_every`` steps and each
-  segment recomputed during the backward sweep; with ``apply_bc`` the boundary rules applied
-  to the initial state are transposed last (``qg_swm_bc_vjp``).
+* :class:`Integrate` -> the state kept every ``checkpoint_every`` steps; the backward sweep runs
+  each segment's adjoint in one C-ABI call (``qg_swm_segment_vjp``: the segment's states
+  recomputed, then ``qg_swm_step_vjp``'s launches for every step in reverse, replayed as one
+  graph), or, for steppers without it (the reparameterised model), one ``step_vjp`` per
+  recomputed step; with ``apply_bc`` the boundary conditions applied to the initial state are
+  transposed last (``qg_swm_bc_vjp``).
 
 A step is ``y1 = y0 + dt sum_i b_i k_i``, ``k_i = F(B(y0 + dt sum_j a_ij k_j))`` with B the
 boundary rules; its adjoint for the cotangent ``g`` of ``y1`` is ``k_bar_i = dt b_i g``, then
@@ -75,6 +77,10 @@ class Integrate(torch.autograd.Function):
         for s in reversed(range(len(cps))):
             k = min(every, ctx.n - s * every)
             if k <= 0:
+                continue
+            if hasattr(plan, "segment_vjp"):  # the whole segment's reverse sweep in one call
+                gy, dp = plan.segment_vjp(cps[s], p, dt, k, scheme, gy)
+                gp += dp
                 continue
             ys = [cps[s]]
             for _ in range(k - 1):
