@@ -173,6 +173,21 @@ def test_cluster_engine_matches_stages(case, bc, scheme):
         assert r < 1e-6, r
 
 
+@pytest.mark.parametrize("bc", ["periodic", "wall"])
+def test_cluster_engine_tiny_grid(bc):
+    """A 3 x 5 basin on a 16-CTA cluster leaves most CTAs without rows (they still take part in
+    every cluster barrier): the cluster engine against the stage engine."""
+    ms, o = pair((3, 5), (500.0, 800.0), (9.81, 0.02), bc, engine="stages")
+    mc, _ = pair((3, 5), (500.0, 800.0), (9.81, 0.02), bc, engine="cluster")
+    y = state(o, 60)
+    dt = 0.05 * min(o.dx, o.dy) / np.sqrt(9.81 * 1300.0)
+    a = ms.step(gpu_state(ms, y), dt, 9, "ssprk3")
+    b = mc.step(gpu_state(mc, y), dt, 9, "ssprk3")
+    assert mc.plan().engine("ssprk3")["cluster_ctas"] >= 2
+    for x, z in ((a.h, b.h), (a.u, b.u), (a.v, b.v)):
+        assert float((x - z).norm()) <= 1e-6 * max(float(x.norm()), 1e-30)
+
+
 def test_engine_choice_and_nonfinite_flag():
     """AUTO takes the engine that ran the tuning steps faster; the reference's swm_jet basin
     (2 layers, 64^2) fits a cluster; a 3-layer 512^2 basin does not and steps one launch per
