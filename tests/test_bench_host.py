@@ -66,3 +66,28 @@ def test_lsweep_strip_classes(nx, ny, rows, expected):
 
 def test_lsweep_masked_member_is_its_own_class():
     assert lsweep_classes(Spec(nx=30, ny=30, mask=object()), 16) == {2}
+
+
+def test_swm_workloads_and_launch_accounting():
+    """The shallow-water bench workloads: the reference's swm_jet run (4320 Tsit5 steps of
+    20 s = one model day per bench step) and the 1024^2 basin; their initial states (the jet of
+    baroclinic_instability_swm; rest plus a 2 m anomaly); the gradient's launch count."""
+    import numpy as np
+
+    import somax_gb300 as sg
+    from somax_gb300 import testcases as tc
+
+    jet = tc.SWM_CONFIGS["swm_jet64"]
+    assert jet.bench_steps * jet.dt == 86400.0 and jet.scheme == "tsit5" and jet.nl == 2
+    y = tc.swm_initial_state(jet)
+    m, s = sg.baroclinic_instability_swm(lateral_viscosity=1000.0, device="cpu")
+    assert np.array_equal(y[1], s.u.numpy()) and np.array_equal(y[2], s.v.numpy())
+    big = tc.swm_initial_state(tc.SWM_CONFIGS["swm3_1024"])
+    assert big.shape == (3, 3, 1026, 1026) and big.dtype == np.float32
+    anomaly = big[0] - np.asarray(tc.SWM3_1024.H, np.float32)[:, None, None]
+    assert abs(float(np.abs(anomaly).max()) - 2.0) < 1e-3 and float(np.abs(big[1:]).max()) == 0.0
+    assert np.array_equal(tc.swm_initial_state(tc.SWM3_1024, seed=0), big)
+    # one Tsit5 step's adjoint: 5 stage + 5 combine launches, 6 cotangent initialisations,
+    # 4 per stage (three VJP kernels and the y_bar update), 15 a_sm updates, the parameters
+    assert bench.swm_grad_launches("cluster", 360, 30) == (1 + 12) + (360 - 12) + 360 * 56 + 1
+    assert bench.swm_grad_launches("stages", 360, 30) == (1 + 360 * 6) + (360 - 12) * 6 + 360 * 56 + 1

@@ -127,3 +127,30 @@ def test_float32_restatement_close_to_float64():
     assert b.dtype == np.float32
     for k in range(3):
         assert np.linalg.norm(b[k] - a[k]) / np.linalg.norm(a[k]) < 1e-4
+
+
+def test_oracle_derivatives_are_consistent():
+    """The float64 derivatives the adjoint tests use (test infrastructure): the dense
+    Jacobian applied to a direction equals a central difference along it, and the parameter
+    derivatives (the right-hand side is affine in each) equal differences of any step."""
+    import numpy as np
+
+    from oracle import swm as W
+
+    m = W.create(nx=5, ny=4, Lx=5e5, Ly=4e5, f0=1e-4, beta=1.6e-11, H=(500.0, 800.0), g_prime=(9.81, 0.02),
+                 lateral_viscosity=300.0, bottom_drag=1e-5, wind_amplitude=2e-3, bc="wall")
+    rng = np.random.default_rng(0)
+    y = np.stack([np.asarray(m.H)[:, None, None] + rng.standard_normal((2, 6, 7)),
+                  0.3 + 0.1 * rng.standard_normal((2, 6, 7)), -0.2 + 0.1 * rng.standard_normal((2, 6, 7))])
+    J = W.rhs_jacobian(m, y)
+    d = rng.standard_normal(y.shape)
+    eps = 1e-5
+    fd = (W.rhs(m, y + eps * d) - W.rhs(m, y - eps * d)).reshape(-1) / (2 * eps)
+    assert np.linalg.norm(J @ d.reshape(-1) - fd) < 1e-7 * np.linalg.norm(fd)
+    P = W.rhs_param_derivatives(m, y)
+    base = {k: float(getattr(m, k)) for k in W.SWM_PARAMS}
+    for i, k in enumerate(W.SWM_PARAMS):
+        p = dict(base)
+        p[k] += 7.0
+        diff = (W.rhs(m, y, p) - W.rhs(m, y, base)).reshape(-1) / 7.0
+        assert np.allclose(P[i], diff, rtol=1e-9, atol=1e-12 * np.abs(diff).max())
