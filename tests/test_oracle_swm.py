@@ -153,4 +153,5 @@ def test_oracle_derivatives_are_consistent():
         p = dict(base)
         p[k] += 7.0
         diff = (W.rhs(m, y, p) - W.rhs(m, y, base)).reshape(-1) / 7.0
-        assert np.allclose(P[i], diff, rtol=1e-9, atol=1e-12 * np.abs(diff).max())
+        # the differences carry the rounding of the whole right-hand side (|F| >> dF/dnu)
+        assert np.abs(P[i] - diff).max() <= 1e-5 * np.abs(diff).max()
