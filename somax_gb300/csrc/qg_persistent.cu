@@ -23,10 +23,11 @@ namespace qg {
 namespace {
 
 constexpr int PT = 256;  // threads per CTA (the stencil tile needs exactly 256)
-// The one-pass GEMM launch runs eight epilogue warps (warps 4-11, two per TMEM lane quarter,
-// each draining every other 32-column chunk): the drain of a tile, not its loads or MMAs,
-// bounds the pass when the stores split BF16 hi/lo or divide.
-constexpr int GEMM_EPI_WARPS = 8;
+// The one-pass GEMM launch runs sixteen epilogue warps (warps 4-19, four per TMEM lane
+// quarter, each draining every fourth 32-column chunk): the drain of a tile, not its loads or
+// MMAs, bounds the pass when the stores split BF16 hi/lo or divide.  640 threads leave 96
+// registers a thread, which the drain fits without spills.
+constexpr int GEMM_EPI_WARPS = 16;
 constexpr int PT_GEMM = 128 + 32 * GEMM_EPI_WARPS;
 static_assert(st::NTHREADS == PT, "stencil tile thread count");
 
@@ -152,18 +153,25 @@ __device__ void gemm_phase(const PersistArgs& a, uint8_t* smem, Shared& sh, uint
         }
     } else if (warp >= 4 && warp < 4 + EPI) {
         const int part = (warp - 4) >> 2;  // column chunks part, part + EPI / 4, ...
-        for (int t = blockIdx.x; t < n; t += gridDim.x) {
-            const GemmTile tl = tiles[t];
+        const int step = gridDim.x;
+        // Two-deep software pipeline over the CTA's tiles: the schedule entry two tiles ahead
+        // and the next tile's member geometry load while the current tile drains, so that a
+        // drain never starts with a chain of dependent global loads.
+        int t = blockIdx.x;
+        GemmTile ahead = t + step < n ? tiles[t + step] : GemmTile{-1, 0, 0};
+        TcTile nxt = t < n ? tc_tile<PASS>(a.members, tiles[t], a.xplane, a.yplane, a.tile_n) : TcTile{};
+        for (; t < n; t += step) {
+            const TcTile tl = nxt;
+            if (t + step < n) nxt = tc_tile<PASS>(a.members, ahead, a.xplane, a.yplane, a.tile_n);
+            if (t + 2 * step < n) ahead = tiles[t + 2 * step];
             if (tl.member < 0) continue;  // a padding entry of the balanced schedule
-            const MemberDev& M = a.members[tl.member];
-            const TcGeom g = tc_geom<PASS>(M, a.xplane, a.yplane);
+            const float rowterm = tc_rowterm<PASS>(tl, warp & 3, lane);
             const uint32_t buf = c.epi_tiles & 1, use = c.epi_tiles >> 1;
             const bool have = mbar_wait(&sh.tfull[buf], use & 1, abort);
             if (!have) break;
             tc_fence_after();
-            tc_epilogue<PASS>(M, g, Cv, c_fmt, PASS == G4_INV_Y ? a.g4_accumulate : 0, tl.mt * TC_BM,
-                              tl.nt * a.tile_n, tc_tile_width(g.Nn, tl.nt, a.tile_n), tmem + buf * TC_TMEM_BUF,
-                              warp & 3, lane, true, part, EPI / 4);
+            tc_epilogue<PASS>(tl, Cv, c_fmt, PASS == G4_INV_Y ? a.g4_accumulate : 0, tmem + buf * TC_TMEM_BUF,
+                              warp & 3, lane, true, rowterm, part, EPI / 4);
             tc_fence_before();
             mbar_arrive(&sh.tempty[buf]);
             ++c.epi_tiles;

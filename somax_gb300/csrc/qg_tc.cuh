@@ -147,6 +147,43 @@ __device__ __forceinline__ TcGeom tc_geom(const MemberDev& M, int64_t xplane, in
     return g;
 }
 
+// What the drain of one output tile reads besides its accumulator: the pass geometry, the
+// tile's first row and column and width, and (G2) the member's eigenvalue tables.
+struct TcTile {
+    TcGeom g;
+    const float* ex;   // DST-I eigenvalues along the output rows' axis (G2)
+    const float* ey;   // along the output columns' axis (G2)
+    const float* lam;  // modal Helmholtz constants per layer (G2)
+    int member, m0, n0, width;
+};
+template <int PASS>
+__device__ __forceinline__ TcTile tc_tile(const MemberDev* members, const GemmTile& tl, int64_t xplane, int64_t yplane,
+                                          int tile_n) {
+    TcTile t;
+    t.member = tl.member;
+    if (tl.member < 0) return t;  // a padding entry of the balanced schedule: nothing is read
+    const MemberDev& M = members[tl.member];
+    t.g = tc_geom<PASS>(M, xplane, yplane);
+    t.ex = M.ex;
+    t.ey = M.ey;
+    t.lam = M.lam;
+    t.m0 = tl.mt * TC_BM;
+    t.n0 = tl.nt * tile_n;
+    t.width = tc_tile_width(t.g.Nn, tl.nt, tile_n);
+    return t;
+}
+
+// G2's divisor row term ex[r] - lam[l] of the accumulator row that `lane` of lane quarter
+// `quarter` holds (0 for the other passes and for rows past the member's last).
+template <int PASS>
+__device__ __forceinline__ float tc_rowterm(const TcTile& T, int quarter, int lane) {
+    if constexpr (PASS != G2_FWD_Y) return 0.f;
+    const int m = T.m0 + quarter * 32 + lane;
+    if (m >= T.g.Mtot) return 0.f;
+    const int l = m / T.g.Mb;
+    return T.ex[m - l * T.g.Mb] - T.lam[l];
+}
+
 // Issue the MMAs of one k-block (operands at shared addresses sa / sb) into tmem_d: `ksteps`
 // UMMA_K-wide steps (the last k-block of a member stops at its K; the zero fill beyond it
 // contributes nothing) at output width n.
@@ -182,27 +219,30 @@ __device__ __forceinline__ void tc_store_bf16x2(__nv_bfloat16* p, int64_t plane,
 // instruction writes 32 consecutive elements of one output row.  Every lane of the warp calls
 // it (tcgen05.ld is warp-collective); `valid` false skips the stores.  G2 divides by
 // ex[r] + ey[n] - lam[l] (row term per lane, column term shuffled from the lane that loaded
-// it); G4 adds to psi_hat when `accumulate` is set (refinement).
+// it, loaded before the accumulator is read); G4 adds to psi_hat when `accumulate` is set
+// (refinement).  `rowterm` is tc_rowterm's value for this lane.
 template <int PASS>
-__device__ __forceinline__ void tc_epilogue(const MemberDev& M, const TcGeom& g, void* Cv, int c_fmt, int accumulate,
-                                            int m0, int n0, int width, uint32_t tmem_acc, int quarter, int lane,
-                                            bool valid, int c0 = 0, int cstep = 1) {
+__device__ __forceinline__ void tc_epilogue(const TcTile& T, void* Cv, int c_fmt, int accumulate, uint32_t tmem_acc,
+                                            int quarter, int lane, bool valid, float rowterm, int c0 = 0,
+                                            int cstep = 1) {
+    const TcGeom& g = T.g;
     const int Mtot = g.Mtot, Mb = g.Mb, ldo = g.ldo;
-    const int Nn = g.Nn;                    // columns of the pass (layer stride of the output)
-    const int nend = min(Nn, n0 + width);   // this tile's columns end here
+    const int Nn = g.Nn;                      // columns of the pass (layer stride of the output)
+    const int n0 = T.n0;
+    const int nend = min(Nn, n0 + T.width);   // this tile's columns end here
     const int64_t cplane = g.cplane;
-    const int m = m0 + quarter * 32 + lane;
+    const int m = T.m0 + quarter * 32 + lane;
     const bool row_ok = valid && m < Mtot;
     const int l = m < Mtot ? m / Mb : 0;
     const int r = m - l * Mb;
-    float rowterm = 0.f;
-    if constexpr (PASS == G2_FWD_Y) rowterm = (m < Mtot ? M.ex[r] : 0.f) - M.lam[l];
     float* Cf = static_cast<float*>(Cv) + g.cbase;
     __nv_bfloat16* Cb = static_cast<__nv_bfloat16*>(Cv) + g.cbase;
     const int64_t obase = (int64_t)l * Nn * ldo + r;
     for (int c = c0; c < (TC_BN + 31) / 32; c += cstep) {
         const int nb = n0 + c * 32;
-        if (!valid || nb >= nend) break;  // warp-uniform (and the same for all four warps)
+        if (!valid || nb >= nend) break;  // warp-uniform (and the same for every epilogue warp)
+        float eyl = 1.f;
+        if constexpr (PASS == G2_FWD_Y) eyl = nb + lane < nend ? T.ey[nb + lane] : 1.f;
         uint32_t v[32];
         const uint32_t taddr = tmem_acc + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(c * 32);
         QG_LD32(v, taddr);
@@ -210,7 +250,6 @@ __device__ __forceinline__ void tc_epilogue(const MemberDev& M, const TcGeom& g,
         if constexpr (PASS == G2_FWD_Y) {
             // spectral divide: the fast division is exact to ~2 ulp, far inside the BF16x3 /
             // TF32 error of the transform itself
-            const float eyl = nb + lane < nend ? M.ey[nb + lane] : 1.f;
 #pragma unroll
             for (int j = 0; j < 32; ++j)
                 v[j] = __float_as_uint(__fdividef(__uint_as_float(v[j]), rowterm + __shfl_sync(0xffffffffu, eyl, j)));
