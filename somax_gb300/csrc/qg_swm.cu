@@ -1143,6 +1143,10 @@ float swm_time(qg_swm_plan* p, F&& run) {
 void swm_tune(qg_swm_plan* p, const Tableau* tb) {
     const int ns = tb->n;
     if (p->cl_C[ns] >= 0) return;
+    // the timing runs overwrite the plan's stage, derivative and projection buffers on the
+    // plan's own stream: work of earlier calls still reading them on the caller's stream
+    // finishes first
+    cudaDeviceSynchronize();
     const bool prof = p->profiling;
     p->profiling = false;
     const qg_swm_desc& ds = p->desc;
