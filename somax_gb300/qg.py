@@ -215,8 +215,10 @@ class Plan:
         members allow it, False = never."""
         if not torch.cuda.is_available():
             raise RuntimeError("somax_gb300 needs a CUDA device (no CPU fallback)")
-        self.device = torch.device(device or "cuda", torch.cuda.current_device()) if device is None \
-            else torch.device(device)
+        d = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+        if d.type == "cuda" and d.index is None:
+            d = torch.device("cuda", torch.cuda.current_device())
+        self.device = d
         L = _lib.lib()
         arr = (MemberDesc * len(members))()
         for i, m in enumerate(members):
@@ -260,6 +262,8 @@ class Plan:
     def _check_field(self, t: torch.Tensor, name: str):
         if not isinstance(t, torch.Tensor) or t.device.type != "cuda" or t.dtype != torch.float32:
             raise TypeError(f"{name} must be a float32 CUDA tensor")
+        if t.device != self.device:
+            raise ValueError(f"{name} is on {t.device}, the plan on {self.device}")
         if not t.is_contiguous() or t.numel() != self.state_size:
             raise ValueError(f"{name} must be contiguous with {self.state_size} elements, got {tuple(t.shape)}")
 

@@ -172,6 +172,7 @@ class ReparameterizedQG:
         from .swm import _SCHEMES
 
         sp = self.swm.plan(y.device)
+        sp._check(y, "state")
         qp = self.plan(y.device)
         pv = self.swm._param_vector(y.device)
         check(sp._L.qg_reparam_step(sp._h, qp._h, C.c_void_p(y.data_ptr()), C.c_void_p(pv.data_ptr()), float(dt),
@@ -272,6 +273,8 @@ class _ReparamStepper:
     def step(self, y, p, dt, k, scheme, apply_bc):
         from .swm import _SCHEMES
 
+        self.sp._check(y, "state")
+        p = self.sp._params(p)
         sp, qp = self._h()
         check(self.L.qg_reparam_step(sp, qp, C.c_void_p(y.data_ptr()), C.c_void_p(p.data_ptr()), float(dt), int(k),
                                      _SCHEMES[scheme], _lib.K["QG_STEP_APPLY_BC"] if apply_bc else 0,
@@ -281,6 +284,9 @@ class _ReparamStepper:
     def step_vjp(self, y0, p, dt, scheme, g):
         from .swm import _SCHEMES
 
+        self.sp._check(y0, "state")
+        self.sp._check(g, "cotangent")
+        p = self.sp._params(p)
         sp, qp = self._h()
         need = int(self.L.qg_reparam_step_vjp_workspace(sp, _SCHEMES[scheme]))
         if scheme not in self.ws or self.ws[scheme].numel() < need:
@@ -294,6 +300,7 @@ class _ReparamStepper:
         return yb, pb
 
     def bc_vjp(self, g):
+        self.sp._check(g, "cotangent")
         sp, qp = self._h()
         check(self.L.qg_reparam_bc_vjp(sp, qp, C.c_void_p(g.data_ptr()), _stream_handle(g.device)),
               "qg_reparam_bc_vjp")

@@ -96,7 +96,10 @@ class SwmPlan:
 
     def __init__(self, desc: "_lib.SwmDesc", device):
         L = _lib.lib()
-        self.device = torch.device(device)
+        d = torch.device(device)
+        if d.type == "cuda" and d.index is None:
+            d = torch.device("cuda", torch.cuda.current_device())
+        self.device = d
         h = C.c_void_p()
         with torch.cuda.device(self.device):
             check(L.qg_swm_create(C.byref(desc), C.byref(h)), "qg_swm_create")
@@ -115,12 +118,23 @@ class SwmPlan:
     def _check(self, t, name):
         if not isinstance(t, torch.Tensor) or t.device.type != "cuda" or t.dtype != torch.float32:
             raise TypeError(f"{name} must be a float32 CUDA tensor")
+        if t.device != self.device:
+            raise ValueError(f"{name} is on {t.device}, the plan on {self.device}")
         if not t.is_contiguous() or t.numel() != self.state_size:
             raise ValueError(f"{name} must be contiguous with {self.state_size} elements")
 
+    def _params(self, params) -> torch.Tensor:
+        """(nu, kappa, tau0) as the contiguous float32 tensor on the plan's device the library reads."""
+        params = torch.as_tensor(params).detach().to(device=self.device, dtype=torch.float32).contiguous()
+        if params.numel() != 3:
+            raise ValueError("params must hold 3 values (nu, kappa, tau0)")
+        return params
+
     def rhs(self, y: torch.Tensor, params: torch.Tensor, apply_bc: bool, out=None) -> torch.Tensor:
         self._check(y, "state")
+        params = self._params(params)
         out = torch.empty_like(y) if out is None else out
+        self._check(out, "out")
         check(self._L.qg_swm_rhs(self._h, C.c_void_p(y.data_ptr()), C.c_void_p(out.data_ptr()),
                                  C.c_void_p(params.data_ptr()), K["QG_RHS_APPLY_BC"] if apply_bc else 0,
                                  _stream_handle(y.device)), "qg_swm_rhs")
@@ -133,6 +147,7 @@ class SwmPlan:
 
     def step(self, y: torch.Tensor, params: torch.Tensor, dt: float, n_steps: int, scheme: str, apply_bc: bool):
         self._check(y, "state")
+        params = self._params(params)
         check(self._L.qg_swm_step(self._h, C.c_void_p(y.data_ptr()), C.c_void_p(params.data_ptr()), float(dt),
                                   int(n_steps), _SCHEMES[scheme], K["QG_STEP_APPLY_BC"] if apply_bc else 0,
                                   _stream_handle(y.device)), "qg_swm_step")
@@ -147,6 +162,7 @@ class SwmPlan:
         ``tend_bar`` (``qg_swm_rhs_vjp``)."""
         self._check(y, "state")
         self._check(tend_bar, "tend_bar")
+        params = self._params(params)
         out = torch.empty_like(y)
         pb = torch.empty(3, dtype=torch.float32, device=y.device)
         check(self._L.qg_swm_rhs_vjp(self._h, C.c_void_p(y.data_ptr()), C.c_void_p(params.data_ptr()),
@@ -167,6 +183,7 @@ class SwmPlan:
         result (``qg_swm_step_vjp``; the workspace is kept per scheme)."""
         self._check(y0, "state")
         self._check(g, "cotangent")
+        params = self._params(params)
         # the state and the cotangent are staged in fixed buffers (with the workspace, per
         # scheme), so that the library replays the step's captured adjoint graph every step
         bufs = getattr(self, "_vjp_bufs", {})
@@ -194,6 +211,7 @@ class SwmPlan:
         staged buffers, dt, k and the scheme repeat)."""
         self._check(y_start, "state")
         self._check(g, "cotangent")
+        params = self._params(params)
         bufs = getattr(self, "_seg_bufs", {})
         self._seg_bufs = bufs
         key = (scheme, int(k))
@@ -218,6 +236,8 @@ class SwmPlan:
         its non-finite entries, as a float64 device tensor of 4 values (``qg_swm_state_stats``)."""
         if not isinstance(x, torch.Tensor) or x.device.type != "cuda" or x.dtype != torch.float32:
             raise TypeError("x must be a float32 CUDA tensor")
+        if x.device != self.device:
+            raise ValueError(f"x is on {x.device}, the plan on {self.device}")
         x = x.contiguous()
         out = torch.empty(4, device=x.device, dtype=torch.float64)
         check(self._L.qg_swm_state_stats(self._h, C.c_void_p(x.data_ptr()), int(x.numel()),

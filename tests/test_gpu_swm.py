@@ -243,3 +243,28 @@ def test_field_stats_and_profiling_counters():
             assert cnt == launches and (ms > 0) == (launches > 0), (engine, k, cnt, ms)
         pl.set_profiling(False)
     assert pl.status() == 0
+
+
+def test_plan_argument_checks():
+    """The plan's calls take the parameters as any 3-value sequence (moved to the plan's device as
+    float32) and refuse, before any launch, a state on the host, of the wrong size or on another
+    device, and a parameter vector of the wrong length."""
+    m, o = pair((16, 16), (500.0, 500.0), (9.81, 0.02), "wall")
+    y = torch.tensor(state(o, 3), dtype=torch.float32, device="cuda").reshape(-1)
+    plan = m.plan(y.device)
+    pv = m._param_vector(y.device)
+    ref = plan.rhs(y, pv, True)
+    torch.testing.assert_close(plan.rhs(y, [float(v) for v in pv.cpu()], True), ref, rtol=0, atol=0)
+    torch.testing.assert_close(plan.rhs(y, pv.double().cpu(), True), ref, rtol=0, atol=0)
+    with pytest.raises(ValueError):
+        plan.rhs(y, pv[:2], True)
+    with pytest.raises(ValueError):
+        plan.step(y.clone(), torch.zeros(4, device="cuda"), 10.0, 1, "heun", True)
+    with pytest.raises(TypeError):
+        plan.rhs(y.cpu(), pv, True)
+    with pytest.raises(ValueError):
+        plan.rhs(y[:-1], pv, True)
+    with pytest.raises(ValueError):
+        plan.rhs(y, pv, True, out=torch.empty(y.numel() - 1, device="cuda"))
+    with pytest.raises(TypeError):
+        plan.field_stats(y.cpu())
