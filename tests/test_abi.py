@@ -80,3 +80,66 @@ def test_entry_points_reject_null(L):
     assert L.qg_step(None, None, None, 1.0, 1, 2, 0, None) == _lib.K["QG_ERR_NULL"]
     assert L.qg_status(None, None, None) == _lib.K["QG_ERR_NULL"]
     assert L.qg_plan_state_size(None) == -1
+
+
+def test_every_declared_function_has_a_signature(L):
+    """The ctypes binding declares the result and argument types of every entry point of the
+    header, so a Python caller never passes a 64-bit pointer through an implicit int."""
+    for n in _lib.declared_functions():
+        assert getattr(L, n).argtypes is not None, f"{n} has no ctypes signature in somax_gb300/_lib.py"
+
+
+def test_every_plan_entry_point_rejects_null(L):
+    """Every entry point that takes a plan answers a NULL plan (and NULL buffers) with QG_ERR_NULL,
+    a size query with -1, before any CUDA call."""
+    null = _lib.K["QG_ERR_NULL"]
+    n = None
+    calls = {
+        "qg_rhs_vjp": (n, n, n, n, n, n, 0, n),
+        "qg_invert_vjp": (n, n, n, n),
+        "qg_step_vjp": (n, n, n, 1.0, _lib.K["QG_SCHEME_SSPRK3"], n, n, n, n),
+        "qg_project": (n, n, n, n, n, n, n, n, n),
+        "qg_project_vjp": (n, n, n, n, n, n, n, n),
+        "qg_diagnose": (n, n, n, n, n),
+        "qg_diagnose_fields": (n, n, n, n, n, n, n, n, n),
+        "qg_state_stats": (n, n, n, n),
+        "qg_set_profiling": (n, 1),
+        "qg_kernel_stats": (n, 0, n, n),
+        "qg_plan_tuning": (n, n, n, 0),
+        "qg_plan_gemm_tuning": (n, n, n, 0),
+        "qg_plan_engine": (n, n, n, 0),
+        "qg_plan_member_modes": (n, 0, n, n, n),
+        "qg_plan_set_wait_limit": (n, 100),
+        "qg_plan_set_parallel_sweep": (n, 1),
+        "qg_invert_static": (n, n, n, n),
+        "qg_swm_rhs": (n, n, n, n, 0, n),
+        "qg_swm_apply_bc": (n, n, n),
+        "qg_swm_step": (n, n, n, 1.0, 1, _lib.K["QG_SCHEME_TSIT5"], 0, n),
+        "qg_swm_rhs_vjp": (n, n, n, n, n, n, 0, n),
+        "qg_swm_bc_vjp": (n, n, n),
+        "qg_swm_step_vjp": (n, n, n, 1.0, _lib.K["QG_SCHEME_TSIT5"], n, n, n, n),
+        "qg_swm_segment_vjp": (n, n, n, 1.0, 2, _lib.K["QG_SCHEME_TSIT5"], n, n, n, n),
+        "qg_swm_state_stats": (n, n, 4, n, n),
+        "qg_swm_set_profiling": (n, 1),
+        "qg_swm_kernel_stats": (n, 0, n, n),
+        "qg_swm_set_engine": (n, 0),
+        "qg_swm_status": (n, n, n),
+        "qg_reparam_step": (n, n, n, n, 1.0, 1, _lib.K["QG_SCHEME_TSIT5"], 0, n),
+        "qg_reparam_bc_vjp": (n, n, n, n),
+        "qg_reparam_step_vjp": (n, n, n, n, 1.0, _lib.K["QG_SCHEME_TSIT5"], n, n, n, n),
+    }
+    for name, args in calls.items():
+        assert getattr(L, name)(*args) == null, name
+    assert L.qg_swm_engine(None, _lib.K["QG_SCHEME_TSIT5"], None, None) == -null
+    sizes = {
+        "qg_plan_member_offset": (n, 0),
+        "qg_step_vjp_workspace": (n, _lib.K["QG_SCHEME_SSPRK3"]),
+        "qg_swm_state_size": (n,),
+        "qg_swm_step_vjp_workspace": (n, _lib.K["QG_SCHEME_TSIT5"]),
+        "qg_swm_segment_vjp_workspace": (n, _lib.K["QG_SCHEME_TSIT5"], 2),
+        "qg_reparam_step_vjp_workspace": (n, _lib.K["QG_SCHEME_TSIT5"]),
+    }
+    for name, args in sizes.items():
+        assert getattr(L, name)(*args) == -1, name
+    L.qg_plan_destroy(None)
+    L.qg_swm_destroy(None)
