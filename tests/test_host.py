@@ -41,6 +41,59 @@ def test_tableaus_consistent():
         assert len(a) == len(b)
 
 
+def _order_conditions(a, b):
+    """Residuals of the Butcher order conditions up to order 4 (c_i = sum_j a_ij)."""
+    n = len(b)
+    A = np.zeros((n, n))
+    for i, row in enumerate(a):
+        A[i, :len(row)] = row
+    b = np.asarray(b, dtype=float)
+    c = A.sum(axis=1)
+    return [b.sum() - 1, b @ c - 1 / 2,
+            b @ c**2 - 1 / 3, b @ A @ c - 1 / 6,
+            b @ c**3 - 1 / 4, (b * c) @ A @ c - 1 / 8, b @ A @ c**2 - 1 / 12, b @ A @ A @ c - 1 / 24]
+
+
+def test_tableau_orders():
+    """Each scheme meets the order conditions of its order (Euler 1, Heun 2, SSP-RK3 3, Tsit5 at
+    least 4 to the rounding of its published coefficients), and Tsit5's stage times are the
+    published c = 0.161, 0.327, 0.9, 0.98002554..., 1, 1."""
+    n_cond = {"euler": 1, "heun": 2, "ssprk3": 4, "tsit5": 8}
+    for s, k in n_cond.items():
+        a, b = tableaus.rk_tableau(s)
+        r = _order_conditions(a, b)[:k]
+        assert max(abs(x) for x in r) < 1e-12, (s, r)
+    a, _ = tableaus.rk_tableau("tsit5")
+    c = [sum(row) for row in a]
+    np.testing.assert_allclose(c, [0.0, 0.161, 0.327, 0.9, 0.9800255409045097, 1.0], rtol=0, atol=1e-13)
+
+
+def test_tableau_copies_agree():
+    """The library's Tsit5 tableau (somax_gb300/csrc/qg_plan.cu) and the float64 oracle's are the
+    host tableau, digit for digit."""
+    import re
+    from pathlib import Path
+
+    from oracle import qg as OQ
+
+    a, b = tableaus.rk_tableau("tsit5")
+    src = (Path(__file__).resolve().parents[1] / "somax_gb300" / "csrc" / "qg_plan.cu").read_text()
+    block = src[src.index("static const Tableau tsit5"):]
+    block = block[:block.index("};")]
+    nums = [float(x) for x in re.findall(r"-?\d+\.\d+(?:e-?\d+)?|(?<![\w.])-?\d+(?![\w.])", block.split("=", 1)[1])]
+    n = nums[0]
+    assert n == 6
+    A = np.array(nums[1:37]).reshape(6, 6)
+    B = np.array(nums[37:43])
+    for i, row in enumerate(a):
+        np.testing.assert_array_equal(A[i, :len(row)], row)
+        assert np.all(A[i, len(row):] == 0)
+    np.testing.assert_array_equal(B, b)
+    for i, row in enumerate(a):
+        np.testing.assert_array_equal(OQ._TSIT5_A[i], row)
+    np.testing.assert_array_equal(OQ._TSIT5_B[:6], b)
+
+
 def test_initial_pv_properties():
     cfg = testcases.C1
     q = testcases.initial_pv(cfg, seed=3)
